@@ -1,0 +1,326 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 SPH step: particle-updates/s on the 1,048,576-particle dam break.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One step = grid rebuild + density/pressure + force/integrate over all particles
+(the reference's three dispatches, Main.cpp:291-304). The timed region is K steps of
+the dam break after W warm-up steps from its initial state; every step is timed with
+CUDA events on the simulation stream and L2 is flushed (256 MiB write) between steps,
+outside the events. Prints one JSON line (rank 0).
+
+--impl reference times the CPU implementation of the same step on the host cores: the
+FP64 restatement of the reference shaders (oracle/), grid back-end, all host threads, on
+a 131,072-particle dam break of the same construction (one step of it per bench step).
+For N > 1 every rank advances its own replica (the path does not shard: "replicas only").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+sys.path[:0] = [str(REPO / "npr-sph_gb300"), str(REPO)]
+
+METRIC = "SPH particle-updates/s at 1M on 1 GB300: learned vs plain at <=1% density err"
+UNIT = "particle-updates/s"
+# Algorithmic HBM bytes per particle-update (each particle's data leaves HBM once per pass):
+#   sort (read pos, vel; write sorted pos, vel)          64
+#   density (read pos; write rho, p)                     24
+#   force+integrate (read pos, vel, rho, p; write pos, vel) 72
+B_ALG = {"sort": 64, "density": 24, "force_integrate": 72}
+B_ALG_STEP = sum(B_ALG.values())
+KERNELS_PER_STEP = 5  # scan, scatter, gather, density, force_integrate
+L2_FLUSH_BYTES = 256 << 20
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def max_over_ranks(value: float, world: int) -> float:
+    """Max of a per-rank float over all ranks (identity for one rank)."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    dev = torch.device("cuda", torch.cuda.current_device()) if dist.get_backend() == "nccl" else torch.device("cpu")
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int) -> None:
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def measured_peaks() -> tuple[dict, str]:
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        return json.loads(p.read_text()), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ["clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.hw_slowdown",
+              "clocks_event_reasons.hw_thermal_slowdown", "clocks_event_reasons.sw_thermal_slowdown",
+              "clocks_event_reasons.sw_power_cap"]
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={','.join(self.FIELDS)}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) != len(self.FIELDS):
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = max(mx, float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_oracle_rate(seconds: float, nthreads: int = 0) -> dict:
+    """FP64 oracle steps on a 131,072-particle dam break until `seconds` have passed."""
+    import nprsph as S
+    from oracle import oracle as O
+
+    sc = S.dam_break(32, 64, 64, seed=2)
+    n = len(sc.particles)
+    pos = np.ascontiguousarray(sc.particles["pos"][:, :3], dtype=np.float64)
+    vel = np.ascontiguousarray(sc.particles["vel"][:, :3], dtype=np.float64)
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        O.run_f64(sc.params, pos, vel, 1, backend="grid", nthreads=nthreads)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= seconds and steps >= 3:
+            break
+    cores = nthreads or O.max_threads()
+    return {"value": n * steps / el, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"FP64 oracle (grid back-end, OpenMP) on a {n}-particle dam break "
+                      f"(32x64x64 block, 0.5h lattice, 4:1:1 box), {steps} steps from its initial state in {el:.1f} s"}
+
+
+def run_reference(args) -> None:
+    """CPU implementation of the step (the FP64 restatement of the reference shaders) on the host cores."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import nprsph as S
+    from oracle import oracle as O
+
+    O.lib()
+    sc = S.dam_break(32, 64, 64, seed=2)
+    n = len(sc.particles)
+    pos = np.ascontiguousarray(sc.particles["pos"][:, :3], dtype=np.float64)
+    vel = np.ascontiguousarray(sc.particles["vel"][:, :3], dtype=np.float64)
+    O.run_f64(sc.params, pos, vel, args.warmup, backend="grid")
+    t0 = time.perf_counter()
+    O.run_f64(sc.params, pos, vel, args.steps, backend="grid")
+    el = time.perf_counter() - t0
+    v = n * args.steps / el
+    cores = O.max_threads()
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "dam break, 131,072-particle sample (32x64x64 block of the 1,048,576-particle "
+                                   "64x128x128 construction) per step", "particles": n},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{args.steps} FP64 oracle steps of the {n}-particle dam break after "
+                                       f"{args.warmup} warm-up steps"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gpu_launches": 0}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args) -> None:
+    import torch
+    import nprsph as S
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.Stream(device=dev)
+    sc = S.dam_break(seed=2 + rank)
+    n = len(sc.particles)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    sim = S.Sim(sc.params, n_max=n, stream=stream.cuda_stream)
+    if args.autotune:
+        sim.upload(sc.particles)
+        sim.autotune(5)
+    sim.upload(sc.particles)
+    sim.step(args.warmup)
+    sim.synchronize()
+
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(dev.index) as clk:
+        with torch.cuda.stream(stream):
+            for k in range(args.steps):
+                flush.add_(1.0)  # L2 flush, outside the timed events
+                ev[k][0].record(stream)
+                sim.step(1)
+                ev[k][1].record(stream)
+        torch.cuda.synchronize()
+    sim.synchronize()
+    barrier(world)
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    local_s = sum(step_ms) / 1e3
+    total_s = max_over_ranks(local_s, world)
+    diag = sim.reduce()
+
+    # Per-pass device times over the same trajectory (events between passes, eager launches).
+    sim.upload(sc.particles)
+    sim.step(args.warmup)
+    sim.enable_timing(True)
+    with torch.cuda.stream(stream):
+        pass_ms = np.zeros(3)
+        for k in range(args.steps):
+            flush.add_(1.0)
+            sim.step(1)
+            pass_ms += np.array(sim.pass_times())
+    sim.enable_timing(False)
+    pass_avg = pass_ms / args.steps
+
+    # End to end through the C ABI with host buffers: upload + step + download each step.
+    host_in = torch.empty(n * 64, dtype=torch.uint8, pin_memory=True).numpy().view(S.PARTICLE_DTYPE)
+    host_out = torch.empty(n * 64, dtype=torch.uint8, pin_memory=True).numpy().view(S.PARTICLE_DTYPE)
+    host_in[:] = sc.particles
+    sim.upload(host_in)
+    sim.step(args.warmup)
+    sim.download(host_in)
+    e2e_steps = min(args.steps, 200)
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        sim.upload(host_in)
+        sim.step(1)
+        sim.download(host_out)
+        host_in, host_out = host_out, host_in
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    blk, sten = sim.get_launch()
+    sim.close()
+
+    if rank != 0:
+        return
+    peaks, src = measured_peaks()
+    hbm = float(peaks["hbm_gbs"])
+    value = world * n * args.steps / total_s
+    fi_ms = pass_avg[2]
+    achieved = B_ALG["force_integrate"] * n / (fi_ms * 1e-3) / 1e9
+    step_achieved = B_ALG_STEP * n * args.steps / local_s / 1e9
+    cpu = cpu_oracle_rate(args.cpu_seconds) if args.cpu_seconds > 0 else None
+    traffic = None
+    prof = REPO / "profiles" / "force_integrate_traffic.json"
+    if prof.exists():
+        traffic = json.loads(prof.read_text()).get("bytes_per_launch_1m")
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "dam break: 1,048,576 particles (64x128x128 block, 0.5h lattice, jitter 0.01h) "
+                               "against the x=0 wall of a 5.12x1.28x1.28 box, g=-9.81, dt=1e-4, plain SPH",
+                   "particles": n, "timed_steps": [args.warmup, args.warmup + args.steps],
+                   "l2": "flushed between steps (256 MiB write outside the timed events)",
+                   "launch": {"threads_per_block": blk, "stencil": sten}, "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "kernel": "force_integrate", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": traffic, "peak_source": f"{src} hbm_gbs",
+                     "bytes_per_particle": B_ALG["force_integrate"],
+                     "step_achieved": step_achieved, "step_frac": step_achieved / hbm,
+                     "step_bytes_per_particle": B_ALG_STEP},
+        "passes_ms": {"sort": pass_avg[0], "density": pass_avg[1], "force_integrate": pass_avg[2]},
+        "cpu_baseline": cpu,
+        "e2e": {"value": world * n * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * 64,
+                "d2h_bytes_per_step": n * 64, "steps": e2e_steps,
+                "path": "sph_upload_aos + sph_step(1) + sph_download_aos, pinned host AoS records"},
+        "gpu_launches": KERNELS_PER_STEP * args.steps,
+        "clocks": clk.summary(),
+        "final_state": {"mean_rho": diag.mean_rho, "nonfinite": int(diag.nonfinite), "step": int(diag.step)},
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample length (0: skip)")
+    ap.add_argument("--autotune", action="store_true", help="pick the launch shape by timing before the run")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,224 @@
+/*
+ * sph_gb300.h -- C ABI of the GB300 SPH step.
+ *
+ * This library replaces the reference's per-frame SPH step, which is three
+ * OpenGL compute dispatches over one particle SSBO:
+ *
+ *   glUseProgram(compute_programs[0]); glDispatchCompute(10,1,1); glMemoryBarrier(...);  // rho_pres_comp.glsl
+ *   glUseProgram(compute_programs[1]); glDispatchCompute(10,1,1); glMemoryBarrier(...);  // force_comp.glsl
+ *   glUseProgram(compute_programs[2]); glDispatchCompute(10,1,1); glMemoryBarrier(...);  // integrate_comp.glsl
+ *
+ * (NPR-SPH/Main.cpp:291-304), with one call:  sph_step(ctx, 1).
+ *
+ * Conventions
+ *   - Every function returns sph_status (0 = OK, negative = error) except the
+ *     small getters. No C++ exception crosses this boundary.
+ *   - sph_last_error(ctx) returns a message for the last failed call on ctx.
+ *   - Host arrays are owned by the caller and only touched during the call.
+ *     Device buffers are owned by the context.
+ *   - A context is used by one host thread at a time. Separate contexts are
+ *     independent (they may share a device).
+ *   - No torch or CUDA types appear in the signatures. A CUDA stream is passed
+ *     as void* (a cudaStream_t); NULL selects a stream owned by the context.
+ */
+#ifndef SPH_GB300_H
+#define SPH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPH_ABI_VERSION 1
+
+typedef int32_t sph_status;
+#define SPH_OK                  0
+#define SPH_ERR_INVALID_ARG    (-1)  /* bad pointer, size or parameter value */
+#define SPH_ERR_CUDA           (-2)  /* a CUDA runtime call failed */
+#define SPH_ERR_OUT_OF_MEMORY  (-3)
+#define SPH_ERR_CAPACITY       (-4)  /* more particles than the context was created for */
+#define SPH_ERR_NOT_READY      (-5)  /* e.g. sph_step before any upload */
+#define SPH_ERR_DEVICE         (-6)  /* a kernel raised its device error word */
+#define SPH_ERR_UNSUPPORTED    (-7)
+
+/*
+ * One particle, 64 bytes: the reference's `struct Particle`
+ * (NPR-SPH/Main.cpp:93-99; std430 copy in rho_pres_comp.glsl:12-18).
+ *   pos.xyz position (w = 1 from make_grid, Main.cpp:499)
+ *   vel.xyz velocity
+ *   force.xyz force density of the last step (written only when
+ *             SPH_FLAG_KEEP_FORCE is set; the fused step does not need it)
+ *   extras[0] density rho, extras[1] pressure, extras[2] age (never written)
+ */
+typedef struct sph_particle {
+    float pos[4];
+    float vel[4];
+    float force[4];
+    float extras[4];
+} sph_particle;
+
+/* Flags of sph_params.flags */
+#define SPH_FLAG_KEEP_FORCE  0x1u  /* also store force.xyz every step (for download) */
+
+/*
+ * Every uniform and compile-time constant of the three shaders, as runtime
+ * fields. sph_params_default() gives the reference's literal values.
+ */
+typedef struct sph_params {
+    /* ConstantsUniform, std140 binding 1 (Main.cpp:110-116; rho_pres_comp.glsl:25-31) */
+    float mass;             /* 0.02 */
+    float smoothing_coeff;  /* 4.0; h = smoothing_coeff * particle_radius (rho_pres_comp.glsl:40) */
+    float visc;             /* 3000 (mu) */
+    float resting_rho;      /* 1000 (rho0) */
+    /* BoundaryUniform, std140 binding 2 (Main.cpp:118-122; integrate_comp.glsl:27-31) */
+    float upper[4];         /* (0.5, 1.0, 0.5, 1) */
+    float lower[4];         /* (-0.1, -0.35, -0.1, 1) */
+    /* Shader compile-time constants */
+    float particle_radius;  /* PARTICLE_RADIUS 0.005 (rho_pres_comp.glsl:5) */
+    float gas_const;        /* GAS_CONST 2000 (rho_pres_comp.glsl:33), stiffness k */
+    float gravity[3];       /* G = (0, -9806.65, 0) (force_comp.glsl:33) */
+    float dt;               /* 1/NUM_PARTICLES = 1e-4 (integrate_comp.glsl:33) */
+    float damping;          /* DAMPING 0.3 (integrate_comp.glsl:8) */
+    /* New: neighbour grid. Cell edge = h * max(cell_scale, 1 + 2^-10). 0 => default. */
+    float cell_scale;
+    uint32_t flags;         /* SPH_FLAG_* */
+    uint32_t reserved[3];   /* must be zero */
+} sph_params;
+
+/* FP64 diagnostics of the current state (drift judge). */
+typedef struct sph_diag {
+    double momentum[3];       /* sum m v */
+    double kinetic_energy;    /* sum 1/2 m |v|^2 */
+    double potential_energy;  /* sum -m G.x */
+    double mean_rho;          /* sum rho / n (rho of the last density pass) */
+    double min_rho;
+    double max_rho;
+    double mean_abs_rho_dev;  /* sum |rho - rho0| / rho0 / n */
+    uint64_t nonfinite;       /* particles with a NaN/Inf in pos, vel or rho */
+    uint64_t n;               /* particles */
+    uint64_t step;            /* steps taken since the last upload */
+} sph_diag;
+
+typedef struct sph_ctx sph_ctx;
+
+/* ---- library ----------------------------------------------------------- */
+
+/* "sph_gb300 <version> sm_103a". */
+const char* sph_version(void);
+
+/* Fill *p with the reference's literal values (see sph_params). */
+void sph_params_default(sph_params* p);
+
+/* SPH_OK if p is usable (h > 0, mass > 0, rho0 > 0, dt > 0, lower < upper, ...). */
+sph_status sph_params_validate(const sph_params* p);
+
+/* Smallest float T with sqrtf(T) >= h: for the FP32 pair distance
+ * d2 = (dx*dx + dy*dy) + dz*dz, `sqrtf(d2) < h` (the shaders' `length(delta) <
+ * smoothing_length`, rho_pres_comp.glsl:49-50) holds exactly when d2 < T. */
+float sph_cutoff_d2(float h);
+
+/* Grid geometry for p: cell edge and cells per axis. */
+sph_status sph_grid_dims(const sph_params* p, float* cell_edge, int32_t dims[3]);
+
+/* ---- context: replaces the SSBO, the UBOs and the three dispatches ---- */
+
+/* Allocate device state for up to n_max particles on the current device.
+ * Mirrors the SSBO/UBO creation in init_particles / initOpenGL
+ * (Main.cpp:510-527, :631-641). stream: cudaStream_t or NULL. */
+sph_status sph_create(const sph_params* p, uint32_t n_max, void* stream, sph_ctx** out);
+sph_status sph_destroy(sph_ctx* ctx);
+const char* sph_last_error(const sph_ctx* ctx);
+
+/* Replace the uniforms; takes effect at the next step.
+ * Mirrors sendUniforms (Main.cpp:274-278). */
+sph_status sph_set_params(sph_ctx* ctx, const sph_params* p);
+sph_status sph_get_params(const sph_ctx* ctx, sph_params* p);
+
+/* Load particles from host memory (pageable or pinned), in caller order.
+ * Mirrors glBufferData of the SSBO (Main.cpp:524-527). Resets the step count. */
+sph_status sph_upload_aos(sph_ctx* ctx, const sph_particle* host, uint32_t n);
+/* Write the current state to host memory in the caller's original order:
+ * pos, vel, extras = (rho, pres, age of the input), force if KEEP_FORCE. */
+sph_status sph_download_aos(sph_ctx* ctx, sph_particle* host, uint32_t n);
+/* Same two calls for an AoS buffer in device memory (the SSBO's place). */
+sph_status sph_upload_aos_device(sph_ctx* ctx, const sph_particle* dev, uint32_t n);
+sph_status sph_download_aos_device(sph_ctx* ctx, sph_particle* dev, uint32_t n);
+
+/* Advance n_steps steps: density/pressure -> force -> integrate, each step
+ * preceded by the grid rebuild. Replaces Main.cpp:291-304. Asynchronous on
+ * the context's stream; errors of earlier asynchronous work surface here or
+ * at sph_synchronize. */
+sph_status sph_step(sph_ctx* ctx, int32_t n_steps);
+sph_status sph_synchronize(sph_ctx* ctx);
+
+/* FP64 reductions of the current state (synchronous). */
+sph_status sph_reduce(sph_ctx* ctx, sph_diag* out);
+
+uint32_t sph_num_particles(const sph_ctx* ctx);
+uint64_t sph_step_count(const sph_ctx* ctx);
+
+/* Per-pass device time of the last sph_step call in milliseconds, summed over
+ * its steps, when the context was created with SPH_FLAG_* timing enabled by
+ * sph_enable_timing(ctx, 1). passes: 0 grid, 1 density, 2 force+integrate. */
+sph_status sph_enable_timing(sph_ctx* ctx, int32_t on);
+sph_status sph_pass_times(sph_ctx* ctx, float out_ms[3]);
+
+/* Neighbour sets of query particles (ids = indices in upload order) on the
+ * current positions: count of j with `length(x_i - x_j) < h` (self
+ * included) and an order-independent 64-bit digest sum_j mix64(j).
+ * brute_force = 0: the uniform grid the step uses; 1: all-pairs scan.
+ * New (no reference counterpart): the check that the grid loses no pair. */
+sph_status sph_neighbor_digest(sph_ctx* ctx, const uint32_t* query_ids, uint32_t n_query,
+                               int32_t brute_force, uint32_t* count_out, uint64_t* digest_out);
+
+/* ---- batched scenes (new; no reference counterpart) --------------------
+ * n_scene independent boxes, each with its own sph_params and particle count,
+ * advance together: one launch per pass covers every scene, and the passes of
+ * a step are replayed from one captured CUDA graph. Uploads and downloads use
+ * the scenes' records concatenated in scene order (sum of counts records).
+ * sph_step, sph_synchronize, sph_download_*, sph_neighbor_digest, sph_reduce
+ * (totals over all scenes) work on a batch context as on a single scene. */
+sph_status sph_create_batch(const sph_params* params, const uint32_t* counts, uint32_t n_scene,
+                            void* stream, sph_ctx** out);
+uint32_t sph_num_scenes(const sph_ctx* ctx);
+/* out[n_scene]: FP64 diagnostics of every scene. */
+sph_status sph_reduce_scenes(sph_ctx* ctx, sph_diag* out, uint32_t n_scene);
+
+/* ---- launch shape and autotuner (new) ----------------------------------
+ * threads_per_block of the pair passes (64..1024, multiple of 32) and
+ * stencil (1: cell edge >= h, 27 cells; 2: cell edge >= h/2, 125 smaller cells).
+ * sph_autotune times `trial_steps` steps of every candidate shape on the
+ * current state (restoring it afterwards) and keeps the fastest. */
+sph_status sph_set_launch(sph_ctx* ctx, int32_t threads_per_block, int32_t stencil);
+sph_status sph_get_launch(const sph_ctx* ctx, int32_t* threads_per_block, int32_t* stencil);
+sph_status sph_autotune(sph_ctx* ctx, int32_t trial_steps, float* best_ms_per_step);
+
+/* ---- scene generators (host only; no GPU needed) ----------------------- */
+
+/* The reference's make_grid()+init_particles() (Main.cpp:488-539): 10x100x10
+ * lattice at `spacing` (PARTICLE_RADIUS), i-j-k loop order, w = 1, all other
+ * fields zero. n must be 10000. */
+sph_status sph_scene_reference_grid(sph_particle* out, uint32_t n, float spacing);
+
+/* n particles on a cubic lattice of `spacing` inside [lo, hi], first point at
+ * lo + spacing/2, filled x fastest, then z, then y (bottom layer first); each
+ * coordinate jittered by U(-jitter, +jitter) from `seed`. Zero velocity, w = 1.
+ * SPH_ERR_CAPACITY if the region holds fewer than n points. */
+sph_status sph_scene_fill(sph_particle* out, uint32_t n, const float lo[3], const float hi[3],
+                          float spacing, float jitter, uint64_t seed);
+
+/* The n lattice points (spacing, jittered as above) nearest to `center`:
+ * a ball of fluid for a sphere-drop scene. */
+sph_status sph_scene_ball(sph_particle* out, uint32_t n, const float center[3],
+                          float spacing, float jitter, uint64_t seed);
+
+/* Add vel.x += amplitude * sin(pi * (pos.x - x0) / length) (sloshing field). */
+sph_status sph_scene_slosh(sph_particle* out, uint32_t n, float amplitude, float x0, float length);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* SPH_GB300_H */

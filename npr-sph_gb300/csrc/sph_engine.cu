@@ -1,0 +1,598 @@
+// sph_engine.cu -- the context behind the C ABI: device buffers, scene table,
+// the captured per-step CUDA graph, uploads/downloads, reductions, neighbour
+// queries and the launch-shape autotuner.
+//
+// One step = the reference's three dispatches (Main.cpp:291-304) re-planned:
+//   scan -> scatter -> gather   (cell sort; the hash ran in the previous step's
+//                                integrate epilogue, or eagerly after an upload)
+//   density                     (rho_pres_comp.glsl)
+//   force + integrate + hash    (force_comp.glsl + integrate_comp.glsl)
+// captured once into a CUDA graph and replayed per step.
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "sph_host.h"
+#include "sph_internal.h"
+
+using namespace sphgb;
+
+struct sph_ctx {
+    int device = 0;
+    std::string err;
+    std::vector<sph_params> params;   // per scene
+    std::vector<uint32_t> counts;     // particles per scene
+    bool batched = false;
+    uint32_t n_max = 0;
+    Buffers b;
+    std::vector<SceneDev> sc_h;
+    SceneDev s0{};
+    LaunchCfg cfg;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    bool graph_dirty = true;
+    bool have_state = false, need_hash = true, stepped = false;
+    uint64_t steps = 0;
+    long long cell_cap = 0;
+    int tile_cap = 0;
+    double* diag_dev = nullptr;
+    int* scene_first_dev = nullptr;
+    bool timing = false;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    float pass_ms[3] = {0, 0, 0};
+    uint32_t* q_ids = nullptr;
+    uint32_t* q_cnt = nullptr;
+    unsigned long long* q_dig = nullptr;
+    int q_cap = 0;
+};
+
+namespace {
+
+sph_status fail(sph_ctx* c, sph_status code, const std::string& msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+#define CK(call)                                                                          \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess)                                                            \
+            return fail(ctx, e_ == cudaErrorMemoryAllocation ? SPH_ERR_OUT_OF_MEMORY : SPH_ERR_CUDA, \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));             \
+    } while (0)
+
+#define GUARD_BEGIN try {
+#define GUARD_END                                                                         \
+    }                                                                                     \
+    catch (const std::bad_alloc&) { return fail(ctx, SPH_ERR_OUT_OF_MEMORY, "host allocation failed"); } \
+    catch (...) { return fail(ctx, SPH_ERR_INVALID_ARG, "unexpected host exception"); }
+
+template <class T>
+cudaError_t dalloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    return cudaMalloc((void**)p, count * sizeof(T));
+}
+
+void free_graph(sph_ctx* ctx) {
+    if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+    if (ctx->graph) cudaGraphDestroy(ctx->graph);
+    ctx->gexec = nullptr;
+    ctx->graph = nullptr;
+    ctx->graph_dirty = true;
+}
+
+// Recompute the scene table (cell ranges, particle ranges, constants) and grow
+// the cell arrays when needed. Leaves count zeroed and asks for a fresh hash.
+sph_status rebuild_geometry(sph_ctx* ctx) {
+    std::vector<SceneDev> sc(ctx->params.size());
+    long long cell = 0, first = 0;
+    const bool keep = (ctx->params[0].flags & SPH_FLAG_KEEP_FORCE) != 0;
+    for (size_t i = 0; i < sc.size(); ++i) {
+        sc[i] = make_scene_dev(ctx->params[i], ctx->cfg.stencil, (int)cell, (int)first, (int)ctx->counts[i], keep);
+        cell += (long long)sc[i].dim[0] * sc[i].dim[1] * sc[i].dim[2];
+        first += ctx->counts[i];
+        if (cell >= (1ll << 31) - 1) return fail(ctx, SPH_ERR_INVALID_ARG, "too many grid cells");
+    }
+    if (cell > ctx->cell_cap) {
+        cudaFree(ctx->b.count);
+        cudaFree(ctx->b.start);
+        cudaFree(ctx->b.scan_state);
+        ctx->b.count = ctx->b.start = nullptr;
+        ctx->b.scan_state = nullptr;
+        long long cap = cell + cell / 8;
+        int tiles = (int)((cap + kScanTile - 1) / kScanTile);
+        CK(dalloc(&ctx->b.count, (size_t)cap));
+        CK(dalloc(&ctx->b.start, (size_t)cap + 1));
+        CK(dalloc(&ctx->b.scan_state, (size_t)tiles));
+        CK(cudaMemsetAsync(ctx->b.scan_state, 0, sizeof(unsigned long long) * tiles, ctx->stream));
+        CK(cudaMemsetAsync(ctx->b.scan_ticket, 0, sizeof(int) * 2, ctx->stream));
+        ctx->cell_cap = cap;
+        ctx->tile_cap = tiles;
+    }
+    CK(cudaMemsetAsync(ctx->b.count, 0, sizeof(int) * (size_t)cell, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->b.scenes, sc.data(), sizeof(SceneDev) * sc.size(), cudaMemcpyHostToDevice, ctx->stream));
+    std::vector<int> sf(sc.size() + 1);
+    for (size_t i = 0; i < sc.size(); ++i) sf[i] = sc[i].first;
+    sf[sc.size()] = (int)first;
+    CK(cudaMemcpyAsync(ctx->scene_first_dev, sf.data(), sizeof(int) * sf.size(), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));  // host vectors die here
+    ctx->sc_h = sc;
+    ctx->s0 = sc[0];
+    ctx->b.ncell = (int)cell;
+    ctx->b.nscene = (int)sc.size();
+    ctx->need_hash = true;
+    free_graph(ctx);
+    return SPH_OK;
+}
+
+void enqueue_sort(sph_ctx* ctx) {
+    launch_scan(ctx->b, ctx->stream);
+    launch_scatter(ctx->b, ctx->stream);
+    launch_gather(ctx->b, ctx->stream);
+}
+
+void enqueue_pairs(sph_ctx* ctx) {
+    launch_density(ctx->b, ctx->s0, ctx->batched, ctx->cfg, ctx->stream);
+    launch_force_integrate(ctx->b, ctx->s0, ctx->batched, ctx->cfg, ctx->stream);
+}
+
+sph_status capture_graph(sph_ctx* ctx) {
+    free_graph(ctx);
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_sort(ctx);
+    enqueue_pairs(ctx);
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &ctx->graph);
+    if (e != cudaSuccess) return fail(ctx, SPH_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    CK(cudaGraphInstantiate(&ctx->gexec, ctx->graph, 0));
+    ctx->graph_dirty = false;
+    return SPH_OK;
+}
+
+sph_status check_device_error(sph_ctx* ctx) {
+    uint32_t e = 0;
+    CK(cudaMemcpyAsync(&e, ctx->b.err, sizeof(e), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (e) {
+        CK(cudaMemsetAsync(ctx->b.err, 0, sizeof(uint32_t), ctx->stream));
+        char buf[128];
+        std::snprintf(buf, sizeof(buf), "device error word 0x%x (1: scan look-back timeout, 4: slot out of range)", e);
+        return fail(ctx, SPH_ERR_DEVICE, buf);
+    }
+    return SPH_OK;
+}
+
+sph_status run_steps(sph_ctx* ctx, int n) {
+    if (ctx->timing) {
+        for (int s = 0; s < n; ++s) {
+            CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+            if (ctx->need_hash) { launch_hash(ctx->b, ctx->s0, ctx->batched, ctx->stream); ctx->need_hash = false; }
+            enqueue_sort(ctx);
+            CK(cudaEventRecord(ctx->ev[1], ctx->stream));
+            launch_density(ctx->b, ctx->s0, ctx->batched, ctx->cfg, ctx->stream);
+            CK(cudaEventRecord(ctx->ev[2], ctx->stream));
+            launch_force_integrate(ctx->b, ctx->s0, ctx->batched, ctx->cfg, ctx->stream);
+            CK(cudaEventRecord(ctx->ev[3], ctx->stream));
+            CK(cudaEventSynchronize(ctx->ev[3]));
+            for (int k = 0; k < 3; ++k) {
+                float ms = 0;
+                CK(cudaEventElapsedTime(&ms, ctx->ev[k], ctx->ev[k + 1]));
+                ctx->pass_ms[k] += ms;
+            }
+        }
+    } else {
+        if (ctx->need_hash) {
+            launch_hash(ctx->b, ctx->s0, ctx->batched, ctx->stream);
+            ctx->need_hash = false;
+        }
+        if (ctx->graph_dirty) {
+            sph_status st = capture_graph(ctx);
+            if (st) return st;
+        }
+        for (int s = 0; s < n; ++s) CK(cudaGraphLaunch(ctx->gexec, ctx->stream));
+    }
+    CK(cudaGetLastError());
+    ctx->steps += (uint64_t)n;
+    ctx->stepped = true;
+    return SPH_OK;
+}
+
+sph_status create_impl(const sph_params* params, const uint32_t* counts, uint32_t nscene, uint32_t n_max,
+                       bool batched, void* stream, sph_ctx** out) {
+    sph_ctx* ctx = nullptr;
+    if (!params || !out || nscene == 0) return SPH_ERR_INVALID_ARG;
+    *out = nullptr;
+    for (uint32_t i = 0; i < nscene; ++i)
+        if (sph_params_validate(&params[i]) != SPH_OK) return SPH_ERR_INVALID_ARG;
+    // Every scene of a batch must agree on the KEEP_FORCE flag.
+    for (uint32_t i = 1; i < nscene; ++i)
+        if ((params[i].flags ^ params[0].flags) & SPH_FLAG_KEEP_FORCE) return SPH_ERR_INVALID_ARG;
+    if (n_max == 0 || n_max > (1u << 30)) return SPH_ERR_INVALID_ARG;
+    ctx = new (std::nothrow) sph_ctx;
+    if (!ctx) return SPH_ERR_OUT_OF_MEMORY;
+    GUARD_BEGIN
+    ctx->params.assign(params, params + nscene);
+    if (counts) ctx->counts.assign(counts, counts + nscene);
+    else ctx->counts.assign(1, 0);
+    ctx->batched = batched;
+    ctx->n_max = n_max;
+    sph_status st = SPH_OK;
+    auto bail = [&](sph_status s) { sph_destroy(ctx); return s; };
+    if (cudaGetDevice(&ctx->device) != cudaSuccess) return bail(SPH_ERR_CUDA);
+    if (stream) {
+        ctx->stream = (cudaStream_t)stream;
+    } else {
+        if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(SPH_ERR_CUDA);
+        ctx->own_stream = true;
+    }
+    Buffers& b = ctx->b;
+    size_t n = n_max;
+    if (dalloc(&b.pos, n) || dalloc(&b.vel, n) || dalloc(&b.pos_s, n) || dalloc(&b.vel_s, n) ||
+        dalloc(&b.rhop, n) || dalloc(&b.force_s, n) || dalloc(&b.force_up, n) || dalloc(&b.aux, n) ||
+        dalloc(&b.key, n) || dalloc(&b.rank, n) || dalloc(&b.perm, n) || dalloc(&b.slot_of_id, n) ||
+        dalloc(&b.err, 1) || dalloc(&b.scan_ticket, 2) || dalloc(&b.scenes, nscene) ||
+        dalloc(&b.partials, reduce_partials_doubles((int)nscene)) ||
+        dalloc(&ctx->diag_dev, (size_t)nscene * kDiagFields) || dalloc(&ctx->scene_first_dev, nscene + 1))
+        return bail(SPH_ERR_OUT_OF_MEMORY);
+    if (cudaMemsetAsync(b.err, 0, sizeof(uint32_t), ctx->stream) ||
+        cudaMemsetAsync(b.scan_ticket, 0, sizeof(int) * 2, ctx->stream))
+        return bail(SPH_ERR_CUDA);
+    for (auto& e : ctx->ev)
+        if (cudaEventCreate(&e) != cudaSuccess) return bail(SPH_ERR_CUDA);
+    b.n = 0;
+    st = rebuild_geometry(ctx);
+    if (st) return bail(st);
+    *out = ctx;
+    return SPH_OK;
+    GUARD_END
+}
+
+sph_status upload_common(sph_ctx* ctx, const sph_particle* src, uint32_t n, bool host) {
+    if (!ctx) return SPH_ERR_INVALID_ARG;
+    if (!src) return fail(ctx, SPH_ERR_INVALID_ARG, "null particle pointer");
+    if (n > ctx->n_max) return fail(ctx, SPH_ERR_CAPACITY, "more particles than n_max");
+    if (ctx->batched) {
+        uint64_t tot = 0;
+        for (uint32_t c : ctx->counts) tot += c;
+        if (tot != n) return fail(ctx, SPH_ERR_INVALID_ARG, "batch upload must hold the sum of the scene counts");
+    }
+    GUARD_BEGIN
+    CK(cudaSetDevice(ctx->device));
+    const sph_particle* dev = src;
+    if (host) {
+        if (!ctx->b.aos) CK(dalloc(&ctx->b.aos, ctx->n_max));
+        CK(cudaMemcpyAsync(ctx->b.aos, src, sizeof(sph_particle) * n, cudaMemcpyHostToDevice, ctx->stream));
+        dev = ctx->b.aos;
+    }
+    if (!ctx->batched && (int)n != ctx->b.n) {
+        ctx->counts[0] = n;
+        ctx->b.n = (int)n;
+        sph_status st = rebuild_geometry(ctx);
+        if (st) return st;
+    }
+    ctx->b.n = (int)n;
+    launch_aos_to_soa(ctx->b, dev, ctx->scene_first_dev, ctx->stream);
+    CK(cudaMemsetAsync(ctx->b.count, 0, sizeof(int) * (size_t)ctx->b.ncell, ctx->stream));
+    CK(cudaGetLastError());
+    ctx->have_state = true;
+    ctx->need_hash = true;
+    ctx->stepped = false;
+    ctx->steps = 0;
+    if (host) CK(cudaStreamSynchronize(ctx->stream));  // caller may reuse its buffer on return
+    return SPH_OK;
+    GUARD_END
+}
+
+sph_status download_common(sph_ctx* ctx, sph_particle* dst, uint32_t n, bool host) {
+    if (!ctx) return SPH_ERR_INVALID_ARG;
+    if (!dst) return fail(ctx, SPH_ERR_INVALID_ARG, "null particle pointer");
+    if (!ctx->have_state) return fail(ctx, SPH_ERR_NOT_READY, "no particles uploaded");
+    if ((int)n != ctx->b.n) return fail(ctx, SPH_ERR_INVALID_ARG, "n must equal the uploaded particle count");
+    GUARD_BEGIN
+    CK(cudaSetDevice(ctx->device));
+    sph_particle* dev = dst;
+    if (host) {
+        if (!ctx->b.aos) CK(dalloc(&ctx->b.aos, ctx->n_max));
+        dev = ctx->b.aos;
+    }
+    const bool keep = (ctx->params[0].flags & SPH_FLAG_KEEP_FORCE) && ctx->stepped;
+    launch_soa_to_aos(ctx->b, keep, dev, ctx->stream);
+    CK(cudaGetLastError());
+    if (host) CK(cudaMemcpyAsync(dst, ctx->b.aos, sizeof(sph_particle) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    return check_device_error(ctx);  // synchronises
+    GUARD_END
+}
+
+void fill_diag(const double* d, uint64_t step, sph_diag* o) {
+    for (int a = 0; a < 3; ++a) o->momentum[a] = d[a];
+    o->kinetic_energy = d[3];
+    o->potential_energy = d[4];
+    double cnt = d[10];
+    o->mean_rho = cnt > 0 ? d[5] / cnt : 0.0;
+    o->min_rho = cnt > 0 ? d[6] : 0.0;
+    o->max_rho = cnt > 0 ? d[7] : 0.0;
+    o->mean_abs_rho_dev = cnt > 0 ? d[8] / cnt : 0.0;
+    o->nonfinite = (uint64_t)d[9];
+    o->n = (uint64_t)(d[9] + d[10]);
+    o->step = step;
+}
+
+sph_status reduce_all(sph_ctx* ctx, std::vector<double>& h) {
+    CK(cudaSetDevice(ctx->device));
+    launch_reduce(ctx->b, nullptr, ctx->b.nscene, ctx->diag_dev, ctx->stream);
+    CK(cudaGetLastError());
+    h.assign((size_t)ctx->b.nscene * kDiagFields, 0.0);
+    CK(cudaMemcpyAsync(h.data(), ctx->diag_dev, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, ctx->stream));
+    return check_device_error(ctx);
+}
+
+}  // namespace
+
+extern "C" {
+
+sph_status sph_create(const sph_params* p, uint32_t n_max, void* stream, sph_ctx** out) {
+    return create_impl(p, nullptr, 1, n_max, false, stream, out);
+}
+
+sph_status sph_create_batch(const sph_params* params, const uint32_t* counts, uint32_t n_scene, void* stream,
+                            sph_ctx** out) {
+    if (!counts || n_scene == 0) return SPH_ERR_INVALID_ARG;
+    uint64_t tot = 0;
+    for (uint32_t i = 0; i < n_scene; ++i) {
+        if (counts[i] == 0) return SPH_ERR_INVALID_ARG;
+        tot += counts[i];
+    }
+    if (tot > (1u << 30)) return SPH_ERR_INVALID_ARG;
+    return create_impl(params, counts, n_scene, (uint32_t)tot, true, stream, out);
+}
+
+sph_status sph_destroy(sph_ctx* ctx) {
+    if (!ctx) return SPH_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    free_graph(ctx);
+    Buffers& b = ctx->b;
+    void* ptrs[] = {b.pos, b.vel, b.pos_s, b.vel_s, b.rhop, b.force_s, b.force_up, b.aux, b.aos, b.key, b.rank,
+                    b.perm, b.count, b.start, b.scan_state, b.scan_ticket, b.slot_of_id, b.err, b.partials,
+                    b.scenes, ctx->diag_dev, ctx->scene_first_dev, ctx->q_ids, ctx->q_cnt, ctx->q_dig};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    for (auto& e : ctx->ev)
+        if (e) cudaEventDestroy(e);
+    if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return SPH_OK;
+}
+
+const char* sph_last_error(const sph_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+sph_status sph_set_params(sph_ctx* ctx, const sph_params* p) {
+    if (!ctx || !p) return SPH_ERR_INVALID_ARG;
+    if (ctx->batched) return fail(ctx, SPH_ERR_UNSUPPORTED, "a batch takes its parameters at creation");
+    if (sph_params_validate(p) != SPH_OK) return fail(ctx, SPH_ERR_INVALID_ARG, "invalid sph_params");
+    GUARD_BEGIN
+    CK(cudaSetDevice(ctx->device));
+    ctx->params[0] = *p;
+    sph_status st = rebuild_geometry(ctx);  // drops the fused hash of the last step
+    return st;
+    GUARD_END
+}
+
+sph_status sph_get_params(const sph_ctx* ctx, sph_params* p) {
+    if (!ctx || !p) return SPH_ERR_INVALID_ARG;
+    *p = ctx->params[0];
+    return SPH_OK;
+}
+
+sph_status sph_upload_aos(sph_ctx* ctx, const sph_particle* host, uint32_t n) {
+    return upload_common(ctx, host, n, true);
+}
+sph_status sph_upload_aos_device(sph_ctx* ctx, const sph_particle* dev, uint32_t n) {
+    return upload_common(ctx, dev, n, false);
+}
+sph_status sph_download_aos(sph_ctx* ctx, sph_particle* host, uint32_t n) {
+    return download_common(ctx, host, n, true);
+}
+sph_status sph_download_aos_device(sph_ctx* ctx, sph_particle* dev, uint32_t n) {
+    return download_common(ctx, dev, n, false);
+}
+
+sph_status sph_step(sph_ctx* ctx, int32_t n_steps) {
+    if (!ctx) return SPH_ERR_INVALID_ARG;
+    if (n_steps < 0) return fail(ctx, SPH_ERR_INVALID_ARG, "n_steps < 0");
+    if (!ctx->have_state) return fail(ctx, SPH_ERR_NOT_READY, "no particles uploaded");
+    if (n_steps == 0 || ctx->b.n == 0) return SPH_OK;
+    GUARD_BEGIN
+    CK(cudaSetDevice(ctx->device));
+    if (ctx->timing) for (float& t : ctx->pass_ms) t = 0.0f;
+    return run_steps(ctx, n_steps);
+    GUARD_END
+}
+
+sph_status sph_synchronize(sph_ctx* ctx) {
+    if (!ctx) return SPH_ERR_INVALID_ARG;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return check_device_error(ctx);
+}
+
+sph_status sph_reduce(sph_ctx* ctx, sph_diag* out) {
+    if (!ctx || !out) return SPH_ERR_INVALID_ARG;
+    if (!ctx->have_state) return fail(ctx, SPH_ERR_NOT_READY, "no particles uploaded");
+    GUARD_BEGIN
+    std::vector<double> h;
+    sph_status st = reduce_all(ctx, h);
+    if (st) return st;
+    double tot[kDiagFields];
+    for (int f = 0; f < kDiagFields; ++f) tot[f] = f == 6 ? INFINITY : (f == 7 ? -INFINITY : 0.0);
+    for (int s = 0; s < ctx->b.nscene; ++s)
+        for (int f = 0; f < kDiagFields; ++f) {
+            double x = h[(size_t)s * kDiagFields + f];
+            tot[f] = f == 6 ? std::min(tot[f], x) : (f == 7 ? std::max(tot[f], x) : tot[f] + x);
+        }
+    fill_diag(tot, ctx->steps, out);
+    return SPH_OK;
+    GUARD_END
+}
+
+sph_status sph_reduce_scenes(sph_ctx* ctx, sph_diag* out, uint32_t n_scene) {
+    if (!ctx || !out) return SPH_ERR_INVALID_ARG;
+    if (!ctx->have_state) return fail(ctx, SPH_ERR_NOT_READY, "no particles uploaded");
+    if ((int)n_scene != ctx->b.nscene) return fail(ctx, SPH_ERR_INVALID_ARG, "n_scene mismatch");
+    GUARD_BEGIN
+    std::vector<double> h;
+    sph_status st = reduce_all(ctx, h);
+    if (st) return st;
+    for (uint32_t s = 0; s < n_scene; ++s) fill_diag(&h[(size_t)s * kDiagFields], ctx->steps, &out[s]);
+    return SPH_OK;
+    GUARD_END
+}
+
+uint32_t sph_num_particles(const sph_ctx* ctx) { return ctx ? (uint32_t)ctx->b.n : 0u; }
+uint64_t sph_step_count(const sph_ctx* ctx) { return ctx ? ctx->steps : 0ull; }
+uint32_t sph_num_scenes(const sph_ctx* ctx) { return ctx ? (uint32_t)ctx->b.nscene : 0u; }
+
+sph_status sph_enable_timing(sph_ctx* ctx, int32_t on) {
+    if (!ctx) return SPH_ERR_INVALID_ARG;
+    ctx->timing = on != 0;
+    for (float& t : ctx->pass_ms) t = 0.0f;
+    return SPH_OK;
+}
+
+sph_status sph_pass_times(sph_ctx* ctx, float out_ms[3]) {
+    if (!ctx || !out_ms) return SPH_ERR_INVALID_ARG;
+    if (!ctx->timing) return fail(ctx, SPH_ERR_NOT_READY, "timing not enabled");
+    for (int k = 0; k < 3; ++k) out_ms[k] = ctx->pass_ms[k];
+    return SPH_OK;
+}
+
+sph_status sph_neighbor_digest(sph_ctx* ctx, const uint32_t* query_ids, uint32_t n_query, int32_t brute_force,
+                               uint32_t* count_out, uint64_t* digest_out) {
+    if (!ctx) return SPH_ERR_INVALID_ARG;
+    if (!query_ids || !count_out || !digest_out) return fail(ctx, SPH_ERR_INVALID_ARG, "null pointer");
+    if (!ctx->have_state) return fail(ctx, SPH_ERR_NOT_READY, "no particles uploaded");
+    if (n_query == 0) return SPH_OK;
+    GUARD_BEGIN
+    CK(cudaSetDevice(ctx->device));
+    if ((int)n_query > ctx->q_cap) {
+        cudaFree(ctx->q_ids); cudaFree(ctx->q_cnt); cudaFree(ctx->q_dig);
+        ctx->q_ids = nullptr; ctx->q_cnt = nullptr; ctx->q_dig = nullptr;
+        ctx->q_cap = 0;
+        CK(dalloc(&ctx->q_ids, n_query));
+        CK(dalloc(&ctx->q_cnt, n_query));
+        CK(dalloc(&ctx->q_dig, n_query));
+        ctx->q_cap = (int)n_query;
+    }
+    if (ctx->need_hash) launch_hash(ctx->b, ctx->s0, ctx->batched, ctx->stream);
+    enqueue_sort(ctx);  // sorted copy of the current positions; the state itself is untouched
+    launch_slot_of_id(ctx->b, ctx->stream);
+    ctx->need_hash = true;  // the scan consumed the cell counts
+    CK(cudaMemcpyAsync(ctx->q_ids, query_ids, sizeof(uint32_t) * n_query, cudaMemcpyHostToDevice, ctx->stream));
+    launch_neighbor_digest(ctx->b, ctx->s0, ctx->batched, ctx->cfg.stencil, ctx->q_ids, (int)n_query,
+                           brute_force ? 1 : 0, ctx->q_cnt, ctx->q_dig, ctx->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(count_out, ctx->q_cnt, sizeof(uint32_t) * n_query, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(digest_out, ctx->q_dig, sizeof(uint64_t) * n_query, cudaMemcpyDeviceToHost, ctx->stream));
+    return check_device_error(ctx);
+    GUARD_END
+}
+
+sph_status sph_set_launch(sph_ctx* ctx, int32_t tpb, int32_t stencil) {
+    if (!ctx) return SPH_ERR_INVALID_ARG;
+    if (tpb < 64 || tpb > 1024 || (tpb % 32) || (stencil != 1 && stencil != 2))
+        return fail(ctx, SPH_ERR_INVALID_ARG, "threads_per_block in [64,1024] multiple of 32, stencil 1 or 2");
+    GUARD_BEGIN
+    CK(cudaSetDevice(ctx->device));
+    bool geo = stencil != ctx->cfg.stencil;
+    ctx->cfg.block = tpb;
+    ctx->cfg.stencil = stencil;
+    if (geo) return rebuild_geometry(ctx);
+    free_graph(ctx);
+    return SPH_OK;
+    GUARD_END
+}
+
+sph_status sph_get_launch(const sph_ctx* ctx, int32_t* tpb, int32_t* stencil) {
+    if (!ctx || !tpb || !stencil) return SPH_ERR_INVALID_ARG;
+    *tpb = ctx->cfg.block;
+    *stencil = ctx->cfg.stencil;
+    return SPH_OK;
+}
+
+sph_status sph_autotune(sph_ctx* ctx, int32_t trial_steps, float* best_ms) {
+    if (!ctx) return SPH_ERR_INVALID_ARG;
+    if (!ctx->have_state) return fail(ctx, SPH_ERR_NOT_READY, "no particles uploaded");
+    if (trial_steps < 1) return fail(ctx, SPH_ERR_INVALID_ARG, "trial_steps < 1");
+    GUARD_BEGIN
+    CK(cudaSetDevice(ctx->device));
+    const size_t n = (size_t)ctx->b.n;
+    float4 *bp = nullptr, *bv = nullptr;
+    float2* br = nullptr;
+    CK(dalloc(&bp, n));
+    sph_status st = SPH_OK;
+    auto cleanup = [&]() { cudaFree(bp); cudaFree(bv); cudaFree(br); };
+    if (dalloc(&bv, n) || dalloc(&br, n)) { cleanup(); return fail(ctx, SPH_ERR_OUT_OF_MEMORY, "autotune backup"); }
+    // Save the state; every trial restarts from it.
+    cudaMemcpyAsync(bp, ctx->b.pos, n * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->stream);
+    cudaMemcpyAsync(bv, ctx->b.vel, n * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->stream);
+    cudaMemcpyAsync(br, ctx->b.rhop, n * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream);
+    const uint64_t steps0 = ctx->steps;
+    const bool stepped0 = ctx->stepped, timing0 = ctx->timing;
+    ctx->timing = false;
+    const int blocks[] = {128, 256, 512};
+    const int stencils[] = {1, 2};
+    float best = 1e30f;
+    LaunchCfg best_cfg = ctx->cfg;
+    for (int sten : stencils) {
+        for (int blk : blocks) {
+            st = sph_set_launch(ctx, blk, sten);
+            if (st) break;
+            auto restore = [&]() {
+                cudaMemcpyAsync(ctx->b.pos, bp, n * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->stream);
+                cudaMemcpyAsync(ctx->b.vel, bv, n * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->stream);
+                cudaMemcpyAsync(ctx->b.rhop, br, n * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream);
+                cudaMemsetAsync(ctx->b.count, 0, sizeof(int) * (size_t)ctx->b.ncell, ctx->stream);
+                ctx->need_hash = true;
+            };
+            restore();
+            st = run_steps(ctx, 1);  // warm-up (captures the graph)
+            if (st) break;
+            restore();
+            if (ctx->need_hash) { launch_hash(ctx->b, ctx->s0, ctx->batched, ctx->stream); ctx->need_hash = false; }
+            cudaEventRecord(ctx->ev[0], ctx->stream);
+            st = run_steps(ctx, trial_steps);
+            if (st) break;
+            cudaEventRecord(ctx->ev[1], ctx->stream);
+            cudaEventSynchronize(ctx->ev[1]);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
+            ms /= (float)trial_steps;
+            if (ms < best) { best = ms; best_cfg = ctx->cfg; }
+            restore();
+        }
+        if (st) break;
+    }
+    ctx->timing = timing0;
+    if (st == SPH_OK) st = sph_set_launch(ctx, best_cfg.block, best_cfg.stencil);
+    // Final restore under the chosen geometry.
+    cudaMemcpyAsync(ctx->b.pos, bp, n * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->stream);
+    cudaMemcpyAsync(ctx->b.vel, bv, n * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->stream);
+    cudaMemcpyAsync(ctx->b.rhop, br, n * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream);
+    cudaMemsetAsync(ctx->b.count, 0, sizeof(int) * (size_t)ctx->b.ncell, ctx->stream);
+    ctx->need_hash = true;
+    ctx->steps = steps0;
+    ctx->stepped = stepped0;
+    cudaStreamSynchronize(ctx->stream);
+    cleanup();
+    if (best_ms) *best_ms = best;
+    if (st) return st;
+    CK(cudaGetLastError());
+    return check_device_error(ctx);
+    GUARD_END
+}
+
+}  // extern "C"

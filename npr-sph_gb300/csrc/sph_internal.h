@@ -1,0 +1,112 @@
+// sph_internal.h -- device-side parameter block, buffer set and kernel
+// launchers shared by the translation units of libsph_gb300.so.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/sph_gb300.h"
+
+namespace sphgb {
+
+// Error bits of the device error word (ORed by kernels, read by the host).
+enum : uint32_t {
+    ERR_SCAN_SPIN = 1u << 0,   // a scan tile gave up waiting for its predecessor
+    ERR_BAD_CELL = 1u << 1,    // a cell key fell outside its scene's cell range
+    ERR_BAD_SLOT = 1u << 2,    // a slot/rank outside [0, n)
+};
+
+// Per-scene constants of one step, derived on the host from sph_params
+// (all FP32; coefficients computed in FP64 then rounded).
+struct SceneDev {
+    float h;          // smoothing_coeff * particle_radius (rho_pres_comp.glsl:40), FP32 product
+    float cut_d2;     // smallest float T with sqrtf(T) >= h: neighbour iff d2 < T
+    float h2;         // h*h
+    float inv_edge;   // 1 / cell edge
+    float lo[3];      // lower wall (BoundaryUniform.lower), also the grid origin
+    float up[3];      // upper wall
+    int dim[3];       // cells per axis
+    int cell_base;    // first cell key of this scene in the global cell table
+    int first;        // first particle slot of this scene (sorted order)
+    int count;        // particles of this scene
+    float poly6c;     // mass*315/(64*PI*h^9)                  (rho_pres_comp.glsl:52)
+    float gas_k;      // GAS_CONST                              (rho_pres_comp.glsl:33)
+    float rho0;       // resting_rho
+    float pres_c;     // mass*45/(PI*h^6)/2: f_p += pres_c*(p_i+p_j)/rho_j*(h-r)^2*d/r (force_comp.glsl:59)
+    float visc_c;     // visc*mass*45/(PI*h^6): f_v += visc_c*(v_j-v_i)/rho_j*(h-r)   (force_comp.glsl:60,63)
+    float g[3];       // G                                      (force_comp.glsl:33)
+    float dt;         // integrate_comp.glsl:33
+    float damp;       // DAMPING (integrate_comp.glsl:8)
+    float mass;
+    int keep_force;
+    int pad_[2];
+};
+
+// Device buffers of one engine (single scene or a batch of scenes).
+// Sorted state lives in (pos_s, vel_s); the integrated state in (pos, vel).
+// pos.w carries the scene index and vel.w the particle id, both as int bits.
+struct Buffers {
+    float4* pos = nullptr;     // state after the last step (slot order of the last sort)
+    float4* vel = nullptr;
+    float4* pos_s = nullptr;   // state sorted by cell (this step)
+    float4* vel_s = nullptr;
+    float2* rhop = nullptr;    // (rho, pres) in the sorted slot order of the last step
+    float4* force_s = nullptr; // SPH_FLAG_KEEP_FORCE: force of the last step, sorted slot order
+    float4* force_up = nullptr;// force as uploaded, id order (returned when not kept)
+    float4* aux = nullptr;     // id order: uploaded (pos.w, vel.w, extras[2], extras[3])
+    sph_particle* aos = nullptr;  // device AoS staging for host uploads/downloads
+    int* key = nullptr;        // cell key of pos[s]
+    int* rank = nullptr;       // arrival rank of s within its cell
+    int* perm = nullptr;       // sorted slot -> state slot (before stabilising)
+    int* count = nullptr;      // particles per cell (zero between steps)
+    int* start = nullptr;      // first sorted slot of each cell; start[ncell] = n
+    unsigned long long* scan_state = nullptr;  // decoupled look-back tile descriptors
+    int* scan_ticket = nullptr;                // dynamic tile counter
+    int* slot_of_id = nullptr; // id -> sorted slot (neighbour queries)
+    uint32_t* err = nullptr;   // device error word
+    double* partials = nullptr;// reduction partials
+    SceneDev* scenes = nullptr;// scene table (batched mode)
+    int n = 0;
+    int ncell = 0;
+    int nscene = 1;
+};
+
+// Launch shape chosen by the autotuner.
+struct LaunchCfg {
+    int block = 256;     // threads per CTA of the pair kernels
+    int stencil = 1;     // cell edge = h/stencil, (2*stencil+1)^3 cells visited
+    int grid_cap = 0;    // persistent grid size (CTAs); 0 = one thread per particle
+};
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 16;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+// ---- launchers (sph_grid.cu) ----
+void launch_hash(const Buffers& b, const SceneDev& s0, bool batched, cudaStream_t st);
+void launch_scan(const Buffers& b, cudaStream_t st);
+void launch_scatter(const Buffers& b, cudaStream_t st);
+void launch_gather(const Buffers& b, cudaStream_t st);
+void launch_slot_of_id(const Buffers& b, cudaStream_t st);
+void launch_neighbor_digest(const Buffers& b, const SceneDev& s0, bool batched, int stencil,
+                            const uint32_t* qids, int nq, int brute, uint32_t* cnt,
+                            unsigned long long* dig, cudaStream_t st);
+// ---- launchers (sph_step.cu) ----
+void launch_density(const Buffers& b, const SceneDev& s0, bool batched, const LaunchCfg& c,
+                    cudaStream_t st);
+void launch_force_integrate(const Buffers& b, const SceneDev& s0, bool batched, const LaunchCfg& c,
+                            cudaStream_t st);
+// ---- launchers (sph_io.cu) ----
+// Per-scene FP64 sums into out[nscene * kDiagFields] (device), deterministic:
+// 0-2 sum m v, 3 kinetic, 4 potential, 5 sum rho, 6 min rho, 7 max rho,
+// 8 sum |rho-rho0|/rho0, 9 non-finite count, 10 finite count, 11 sum rho^2.
+constexpr int kDiagFields = 12;
+void launch_reduce(const Buffers& b, const SceneDev* host_scenes, int nscene, double* out_dev,
+                   cudaStream_t st);
+size_t reduce_partials_doubles(int nscene);
+void launch_aos_to_soa(const Buffers& b, const sph_particle* aos_dev, const int* scene_first, cudaStream_t st);
+void launch_soa_to_aos(const Buffers& b, bool force_from_step, sph_particle* aos_dev, cudaStream_t st);
+
+int device_sm_count();
+
+}  // namespace sphgb

@@ -1,0 +1,398 @@
+"""Python host binding of libsph_gb300.so (ctypes over the C ABI in include/sph_gb300.h).
+
+It mirrors the reference host loop's view of the SPH step (NPR-SPH/Main.cpp):
+the particle array (`struct Particle`, Main.cpp:93-99) is a numpy structured
+array PARTICLE_DTYPE, the uniforms (Main.cpp:110-122 plus the shader constants)
+are `Params`, and `Sim.step(n)` replaces the three dispatches of
+Main.cpp:291-304. There is no fallback: if the library is missing or was not
+built, importing this module raises.
+
+The scene helpers build the seeded synthetic scenes of the benchmark
+configurations (reference scene, dam break, batched boxes, slosh).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = Path(os.environ.get("SPH_GB300_LIB", _HERE / "libsph_gb300.so"))
+
+PARTICLE_DTYPE = np.dtype([("pos", "<f4", 4), ("vel", "<f4", 4), ("force", "<f4", 4), ("extras", "<f4", 4)])
+assert PARTICLE_DTYPE.itemsize == 64
+
+FLAG_KEEP_FORCE = 0x1
+
+OK, ERR_INVALID_ARG, ERR_CUDA, ERR_OUT_OF_MEMORY, ERR_CAPACITY, ERR_NOT_READY, ERR_DEVICE, ERR_UNSUPPORTED = (
+    0, -1, -2, -3, -4, -5, -6, -7)
+
+
+class Params(C.Structure):
+    """sph_params: ConstantsUniform + BoundaryUniform + shader constants (see include/sph_gb300.h)."""
+
+    _fields_ = [("mass", C.c_float), ("smoothing_coeff", C.c_float), ("visc", C.c_float),
+                ("resting_rho", C.c_float), ("upper", C.c_float * 4), ("lower", C.c_float * 4),
+                ("particle_radius", C.c_float), ("gas_const", C.c_float), ("gravity", C.c_float * 3),
+                ("dt", C.c_float), ("damping", C.c_float), ("cell_scale", C.c_float), ("flags", C.c_uint32),
+                ("reserved", C.c_uint32 * 3)]
+
+    @property
+    def h(self) -> float:
+        return float(np.float32(self.smoothing_coeff) * np.float32(self.particle_radius))
+
+    def copy(self) -> "Params":
+        p = Params()
+        C.memmove(C.byref(p), C.byref(self), C.sizeof(Params))
+        return p
+
+
+class Diag(C.Structure):
+    _fields_ = [("momentum", C.c_double * 3), ("kinetic_energy", C.c_double), ("potential_energy", C.c_double),
+                ("mean_rho", C.c_double), ("min_rho", C.c_double), ("max_rho", C.c_double),
+                ("mean_abs_rho_dev", C.c_double), ("nonfinite", C.c_uint64), ("n", C.c_uint64),
+                ("step", C.c_uint64)]
+
+    def as_dict(self) -> dict:
+        return {"momentum": list(self.momentum), "kinetic_energy": self.kinetic_energy,
+                "potential_energy": self.potential_energy, "mean_rho": self.mean_rho, "min_rho": self.min_rho,
+                "max_rho": self.max_rho, "mean_abs_rho_dev": self.mean_abs_rho_dev,
+                "nonfinite": int(self.nonfinite), "n": int(self.n), "step": int(self.step)}
+
+
+# Every symbol of include/sph_gb300.h with its ctypes signature.
+_P = C.c_void_p
+_SIGS = {
+    "sph_version": (C.c_char_p, []),
+    "sph_params_default": (None, [C.POINTER(Params)]),
+    "sph_params_validate": (C.c_int32, [C.POINTER(Params)]),
+    "sph_cutoff_d2": (C.c_float, [C.c_float]),
+    "sph_grid_dims": (C.c_int32, [C.POINTER(Params), C.POINTER(C.c_float), C.POINTER(C.c_int32)]),
+    "sph_create": (C.c_int32, [C.POINTER(Params), C.c_uint32, _P, C.POINTER(_P)]),
+    "sph_create_batch": (C.c_int32, [C.POINTER(Params), C.POINTER(C.c_uint32), C.c_uint32, _P, C.POINTER(_P)]),
+    "sph_destroy": (C.c_int32, [_P]),
+    "sph_last_error": (C.c_char_p, [_P]),
+    "sph_set_params": (C.c_int32, [_P, C.POINTER(Params)]),
+    "sph_get_params": (C.c_int32, [_P, C.POINTER(Params)]),
+    "sph_upload_aos": (C.c_int32, [_P, _P, C.c_uint32]),
+    "sph_download_aos": (C.c_int32, [_P, _P, C.c_uint32]),
+    "sph_upload_aos_device": (C.c_int32, [_P, _P, C.c_uint32]),
+    "sph_download_aos_device": (C.c_int32, [_P, _P, C.c_uint32]),
+    "sph_step": (C.c_int32, [_P, C.c_int32]),
+    "sph_synchronize": (C.c_int32, [_P]),
+    "sph_reduce": (C.c_int32, [_P, C.POINTER(Diag)]),
+    "sph_reduce_scenes": (C.c_int32, [_P, C.POINTER(Diag), C.c_uint32]),
+    "sph_num_particles": (C.c_uint32, [_P]),
+    "sph_num_scenes": (C.c_uint32, [_P]),
+    "sph_step_count": (C.c_uint64, [_P]),
+    "sph_enable_timing": (C.c_int32, [_P, C.c_int32]),
+    "sph_pass_times": (C.c_int32, [_P, C.POINTER(C.c_float)]),
+    "sph_neighbor_digest": (C.c_int32, [_P, _P, C.c_uint32, C.c_int32, _P, _P]),
+    "sph_set_launch": (C.c_int32, [_P, C.c_int32, C.c_int32]),
+    "sph_get_launch": (C.c_int32, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "sph_autotune": (C.c_int32, [_P, C.c_int32, C.POINTER(C.c_float)]),
+    "sph_scene_reference_grid": (C.c_int32, [_P, C.c_uint32, C.c_float]),
+    "sph_scene_fill": (C.c_int32, [_P, C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_float,
+                                   C.c_float, C.c_uint64]),
+    "sph_scene_ball": (C.c_int32, [_P, C.c_uint32, C.POINTER(C.c_float), C.c_float, C.c_float, C.c_uint64]),
+    "sph_scene_slosh": (C.c_int32, [_P, C.c_uint32, C.c_float, C.c_float, C.c_float]),
+}
+
+
+def _load() -> C.CDLL:
+    if not LIB_PATH.exists():
+        raise ImportError(f"{LIB_PATH} is not built: run `python npr-sph_gb300/build.py`")
+    lib = C.CDLL(str(LIB_PATH))
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+lib = _load()
+
+
+class SphError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"sph status {code}: {msg}")
+        self.code = code
+
+
+def _check(code: int, ctx=None, what: str = "") -> None:
+    if code != OK:
+        msg = lib.sph_last_error(ctx).decode() if ctx else what
+        raise SphError(code, msg or what)
+
+
+def _f3(v) -> C.Array:
+    return (C.c_float * 3)(*[float(x) for x in v])
+
+
+def default_params() -> Params:
+    """The reference's literal uniforms and shader constants."""
+    p = Params()
+    lib.sph_params_default(C.byref(p))
+    return p
+
+
+def cutoff_d2(h: float) -> float:
+    return float(lib.sph_cutoff_d2(C.c_float(h)))
+
+
+def grid_dims(p: Params) -> tuple[float, tuple[int, int, int]]:
+    e = C.c_float()
+    d = (C.c_int32 * 3)()
+    _check(lib.sph_grid_dims(C.byref(p), C.byref(e), d), what="sph_grid_dims")
+    return float(e.value), (d[0], d[1], d[2])
+
+
+def empty_particles(n: int) -> np.ndarray:
+    return np.zeros(n, dtype=PARTICLE_DTYPE)
+
+
+def _ptr(a) -> int:
+    if isinstance(a, np.ndarray):
+        if not a.flags["C_CONTIGUOUS"]:
+            raise ValueError("particle array must be C-contiguous")
+        return a.ctypes.data
+    return int(a.data_ptr())  # a torch tensor (device or pinned host)
+
+
+class Sim:
+    """One simulation context (single scene, or a batch of scenes)."""
+
+    def __init__(self, params, n_max: int | None = None, counts=None, stream=None):
+        self._ctx = C.c_void_p()
+        s = C.c_void_p(int(stream) if stream is not None else 0)
+        if counts is None:
+            _check(lib.sph_create(C.byref(params), int(n_max), s, C.byref(self._ctx)), what="sph_create")
+            self.n_scene = 1
+        else:
+            counts = np.ascontiguousarray(counts, dtype=np.uint32)
+            plist = (Params * len(counts))(*params)
+            _check(lib.sph_create_batch(plist, counts.ctypes.data_as(C.POINTER(C.c_uint32)), len(counts), s,
+                                        C.byref(self._ctx)), what="sph_create_batch")
+            self.n_scene = len(counts)
+            self._counts = counts
+
+    def close(self) -> None:
+        if self._ctx:
+            lib.sph_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def ctx(self):
+        return self._ctx
+
+    @property
+    def n(self) -> int:
+        return int(lib.sph_num_particles(self._ctx))
+
+    @property
+    def steps(self) -> int:
+        return int(lib.sph_step_count(self._ctx))
+
+    def set_params(self, p: Params) -> None:
+        _check(lib.sph_set_params(self._ctx, C.byref(p)), self._ctx)
+
+    def get_params(self) -> Params:
+        p = Params()
+        _check(lib.sph_get_params(self._ctx, C.byref(p)), self._ctx)
+        return p
+
+    def upload(self, particles: np.ndarray) -> None:
+        _check(lib.sph_upload_aos(self._ctx, _ptr(particles), len(particles)), self._ctx)
+
+    def download(self, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = empty_particles(self.n)
+        _check(lib.sph_download_aos(self._ctx, _ptr(out), len(out)), self._ctx)
+        return out
+
+    def upload_device(self, dev_ptr: int, n: int) -> None:
+        _check(lib.sph_upload_aos_device(self._ctx, C.c_void_p(dev_ptr), n), self._ctx)
+
+    def download_device(self, dev_ptr: int, n: int) -> None:
+        _check(lib.sph_download_aos_device(self._ctx, C.c_void_p(dev_ptr), n), self._ctx)
+
+    def step(self, n: int = 1) -> None:
+        _check(lib.sph_step(self._ctx, int(n)), self._ctx)
+
+    def synchronize(self) -> None:
+        _check(lib.sph_synchronize(self._ctx), self._ctx)
+
+    def reduce(self) -> Diag:
+        d = Diag()
+        _check(lib.sph_reduce(self._ctx, C.byref(d)), self._ctx)
+        return d
+
+    def reduce_scenes(self) -> list[Diag]:
+        arr = (Diag * self.n_scene)()
+        _check(lib.sph_reduce_scenes(self._ctx, arr, self.n_scene), self._ctx)
+        return list(arr)
+
+    def enable_timing(self, on: bool = True) -> None:
+        _check(lib.sph_enable_timing(self._ctx, 1 if on else 0), self._ctx)
+
+    def pass_times(self) -> list[float]:
+        a = (C.c_float * 3)()
+        _check(lib.sph_pass_times(self._ctx, a), self._ctx)
+        return [a[0], a[1], a[2]]
+
+    def neighbor_digest(self, query_ids, brute_force: bool = False):
+        q = np.ascontiguousarray(query_ids, dtype=np.uint32)
+        cnt = np.zeros(len(q), dtype=np.uint32)
+        dig = np.zeros(len(q), dtype=np.uint64)
+        _check(lib.sph_neighbor_digest(self._ctx, q.ctypes.data, len(q), 1 if brute_force else 0, cnt.ctypes.data,
+                                       dig.ctypes.data), self._ctx)
+        return cnt, dig
+
+    def set_launch(self, threads_per_block: int, stencil: int) -> None:
+        _check(lib.sph_set_launch(self._ctx, threads_per_block, stencil), self._ctx)
+
+    def get_launch(self) -> tuple[int, int]:
+        a, b = C.c_int32(), C.c_int32()
+        _check(lib.sph_get_launch(self._ctx, C.byref(a), C.byref(b)), self._ctx)
+        return a.value, b.value
+
+    def autotune(self, trial_steps: int = 5) -> float:
+        ms = C.c_float()
+        _check(lib.sph_autotune(self._ctx, trial_steps, C.byref(ms)), self._ctx)
+        return float(ms.value)
+
+
+# ---- scenes -------------------------------------------------------------------------------
+
+def scene_reference_grid() -> np.ndarray:
+    """make_grid()+init_particles() of Main.cpp:488-539 (10x100x10 lattice at 0.005)."""
+    a = empty_particles(10000)
+    _check(lib.sph_scene_reference_grid(_ptr(a), 10000, C.c_float(0.005)), what="sph_scene_reference_grid")
+    return a
+
+
+def scene_fill(n: int, lo, hi, spacing: float, jitter: float, seed: int) -> np.ndarray:
+    a = empty_particles(n)
+    _check(lib.sph_scene_fill(_ptr(a), n, _f3(lo), _f3(hi), C.c_float(spacing), C.c_float(jitter),
+                              C.c_uint64(seed)), what="sph_scene_fill")
+    return a
+
+
+def scene_ball(n: int, center, spacing: float, jitter: float, seed: int) -> np.ndarray:
+    a = empty_particles(n)
+    _check(lib.sph_scene_ball(_ptr(a), n, _f3(center), C.c_float(spacing), C.c_float(jitter), C.c_uint64(seed)),
+           what="sph_scene_ball")
+    return a
+
+
+def scene_slosh(a: np.ndarray, amplitude: float, x0: float, length: float) -> np.ndarray:
+    _check(lib.sph_scene_slosh(_ptr(a), len(a), C.c_float(amplitude), C.c_float(x0), C.c_float(length)),
+           what="sph_scene_slosh")
+    return a
+
+
+def workload_params(gravity_y: float = -9.81, dt: float = 1e-4, lower=None, upper=None, k=None, mu=None,
+                    flags: int = 0) -> Params:
+    """The benchmark scenes' uniforms: the reference's m, h, rho0, k, mu and damping, with
+    gravity (0, -9.81, 0) and a fixed dt of 1e-4 (the shader's 1/NUM_PARTICLES at 10k)."""
+    p = default_params()
+    p.gravity[1] = gravity_y
+    p.dt = dt
+    if lower is not None:
+        for a in range(3):
+            p.lower[a] = lower[a]
+    if upper is not None:
+        for a in range(3):
+            p.upper[a] = upper[a]
+    if k is not None:
+        p.gas_const = k
+    if mu is not None:
+        p.visc = mu
+    p.flags = flags
+    return p
+
+
+@dataclass
+class Scene:
+    name: str
+    params: Params
+    particles: np.ndarray
+    steps: int
+
+
+def reference_scene_10k(seed: int = 1) -> Scene:
+    """10,000 particles on a 0.5h lattice (jitter +-0.01h) filling the lower-corner quarter
+    (half of x, half of z, from the floor up) of the reference box; G = (0,-9.81,0); 200 steps."""
+    p = workload_params()
+    h = p.h
+    lo = [p.lower[a] for a in range(3)]
+    hi = [p.lower[0] + 0.5 * (p.upper[0] - p.lower[0]), p.upper[1], p.lower[2] + 0.5 * (p.upper[2] - p.lower[2])]
+    parts = scene_fill(10000, lo, hi, 0.5 * h, 0.01 * h, seed)
+    return Scene("reference_10k", p, parts, 200)
+
+
+def dam_break(nx: int = 64, ny: int = 128, nz: int = 128, seed: int = 2, flags: int = 0) -> Scene:
+    """Dam break: an nx*ny*nz block (spacing 0.5h, jitter +-0.01h) against the x = 0 wall of a
+    4:1:1 box whose y and z extents equal the block's (64x128x128 = 1,048,576 particles in
+    5.12 x 1.28 x 1.28); 1,000 steps."""
+    p0 = default_params()
+    s = 0.5 * p0.h
+    bx, by, bz = nx * s, ny * s, nz * s
+    L = max(by, bz)
+    p = workload_params(lower=(0.0, 0.0, 0.0), upper=(4 * L, by, bz), flags=flags)
+    parts = scene_fill(nx * ny * nz, (0.0, 0.0, 0.0), (bx, by, bz), s, 0.01 * p.h, seed)
+    return Scene(f"dam_break_{nx}x{ny}x{nz}", p, parts, 1000)
+
+
+def slosh_block(n_side: int = 256, seed: int = 5) -> Scene:
+    """n_side^3 block (spacing 0.5h) in a 2:1:1 box, v_x = 0.5 sin(pi x / L), L = box length."""
+    p0 = default_params()
+    s = 0.5 * p0.h
+    b = n_side * s
+    p = workload_params(lower=(0.0, 0.0, 0.0), upper=(2 * b, b, b))
+    parts = scene_fill(n_side ** 3, (0.0, 0.0, 0.0), (b, b, b), s, 0.01 * p.h, seed)
+    scene_slosh(parts, 0.5, 0.0, 2 * b)
+    return Scene(f"slosh_{n_side}^3", p, parts, 2000)
+
+
+def batched_scenes(n_scene: int = 256, seed: int = 3, n_lo: int = 2000, n_hi: int = 65536):
+    """n_scene independent boxes: counts log-uniform in [n_lo, n_hi], k ~ U[500, 3000],
+    mu ~ U[0.1, 2.0]; a coin flip picks a corner lattice or a sphere drop. Each box is a cube
+    of edge 2 * cbrt(count) * spacing (fluid fills an eighth of it). Returns
+    (params list, counts, concatenated particles)."""
+    rng = np.random.default_rng(seed)
+    p0 = default_params()
+    s = 0.5 * p0.h
+    plist, counts, parts = [], [], []
+    for i in range(n_scene):
+        cnt = int(round(math.exp(rng.uniform(math.log(n_lo), math.log(n_hi)))))
+        k = float(rng.uniform(500.0, 3000.0))
+        mu = float(rng.uniform(0.1, 2.0))
+        ball = bool(rng.integers(0, 2))
+        edge = 2.0 * math.ceil(cnt ** (1.0 / 3.0) + 1) * s
+        p = workload_params(lower=(0.0, 0.0, 0.0), upper=(edge, edge, edge), k=k, mu=mu)
+        if ball:
+            a = scene_ball(cnt, (0.5 * edge, 0.6 * edge, 0.5 * edge), s, 0.01 * p.h, seed * 1000003 + i)
+        else:
+            a = scene_fill(cnt, (0.0, 0.0, 0.0), (0.5 * edge, edge, 0.5 * edge), s, 0.01 * p.h,
+                           seed * 1000003 + i)
+        plist.append(p)
+        counts.append(cnt)
+        parts.append(a)
+    return plist, np.array(counts, dtype=np.uint32), np.concatenate(parts)

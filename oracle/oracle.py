@@ -1,0 +1,171 @@
+"""ctypes wrapper of the CPU oracle. TEST INFRASTRUCTURE ONLY.
+
+Only tests/, the smoke check of __graft_entry__ and the CPU legs of bench.py
+may import this module. It loads
+  oracle/liboracle.so          FP64 / FP32 restatement of the reference SPH step (sph_oracle.cpp)
+  oracle/_ref/libref_shader.so the reference's GLSL compute shaders compiled as C++ (optional:
+                               only where the reference tree was present at build time)
+and `build()` compiles them with make.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "liboracle.so"
+REF_LIB = HERE / "_ref" / "libref_shader.so"
+REF_SRC = Path("/root/reference/NPR-SPH")
+
+_P = C.c_void_p
+_I64 = C.c_int64
+
+
+def build(with_ref: bool = True) -> None:
+    """Always a full rebuild (a few seconds): the tree moves between x86-64 and aarch64 hosts,
+    and a library left from the other architecture must never be loaded."""
+    subprocess.run(["make", "-s", "-B", "-C", str(HERE)], check=True)
+    if with_ref and REF_SRC.is_dir():
+        subprocess.run(["make", "-s", "-B", "-C", str(HERE), "ref", f"REF_DIR={REF_SRC}"], check=True)
+
+
+_lib = None
+_ref = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            build(with_ref=False)
+        L = C.CDLL(str(LIB))
+        L.oracle_step_f64.restype = C.c_int
+        L.oracle_step_f64.argtypes = [_P, _I64, _P, _P, C.c_int, C.c_int, _P, _P, _P, _P, _P, _P, _P]
+        L.oracle_run_f64.restype = C.c_int
+        L.oracle_run_f64.argtypes = [_P, _I64, _P, _P, _P, _P, C.c_int, C.c_int, C.c_int]
+        L.oracle_step_f32_aos.restype = C.c_int
+        L.oracle_step_f32_aos.argtypes = [_P, _P, _I64, C.c_int, C.c_int, C.c_int, C.c_int]
+        L.oracle_neighbors.restype = C.c_int
+        L.oracle_neighbors.argtypes = [_P, _I64, _P, _I64, _P, C.c_int, C.c_int, _P, _P]
+        L.oracle_neighbor_lists.restype = C.c_int64
+        L.oracle_neighbor_lists.argtypes = [_P, _I64, _P, C.c_int, _P, _P, _I64]
+        L.oracle_cutoff_d2.restype = C.c_float
+        L.oracle_cutoff_d2.argtypes = [C.c_float]
+        L.oracle_mix64.restype = C.c_uint64
+        L.oracle_mix64.argtypes = [C.c_uint64]
+        L.oracle_max_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def ref_available() -> bool:
+    return REF_LIB.exists()
+
+
+def ref() -> C.CDLL:
+    global _ref
+    if _ref is None:
+        R = C.CDLL(str(REF_LIB))
+        R.ref_shader_step.restype = C.c_int
+        R.ref_shader_step.argtypes = [_P, C.c_int, _P, _P, _P, C.c_int]
+        R.ref_shader_num_particles.restype = C.c_int
+        _ref = R
+    return _ref
+
+
+BACKENDS = {"brute": 0, "grid": 1}
+
+
+def _pp(params) -> int:
+    return C.addressof(params)
+
+
+def step_f64(params, particles: np.ndarray, backend: str = "grid", nthreads: int = 0) -> dict:
+    """One FP64 step from the state of `particles` (64-byte records). Returns the density,
+    pressure, force, force scale, new position/velocity and wall margin per particle."""
+    n = len(particles)
+    pos = np.ascontiguousarray(particles["pos"][:, :3], dtype=np.float64)
+    vel = np.ascontiguousarray(particles["vel"][:, :3], dtype=np.float64)
+    out = {k: np.zeros(n) for k in ("rho", "pres", "fscale", "margin")}
+    for k in ("force", "pos", "vel"):
+        out[k] = np.zeros((n, 3))
+    rc = lib().oracle_step_f64(_pp(params), n, pos.ctypes.data, vel.ctypes.data, BACKENDS[backend], nthreads,
+                               out["rho"].ctypes.data, out["pres"].ctypes.data, out["force"].ctypes.data,
+                               out["fscale"].ctypes.data, out["pos"].ctypes.data, out["vel"].ctypes.data,
+                               out["margin"].ctypes.data)
+    assert rc == 0
+    return out
+
+
+def run_f64(params, pos: np.ndarray, vel: np.ndarray, n_steps: int, backend: str = "grid",
+            nthreads: int = 0) -> tuple[np.ndarray, np.ndarray]:
+    """n_steps FP64 steps in place on (n,3) float64 arrays. Returns (rho, pres) of the last step."""
+    n = len(pos)
+    assert pos.dtype == np.float64 and vel.dtype == np.float64 and pos.flags.c_contiguous
+    rho, pres = np.zeros(n), np.zeros(n)
+    rc = lib().oracle_run_f64(_pp(params), n, pos.ctypes.data, vel.ctypes.data, rho.ctypes.data,
+                              pres.ctypes.data, n_steps, BACKENDS[backend], nthreads)
+    assert rc == 0
+    return rho, pres
+
+
+def step_f32(params, particles: np.ndarray, n_steps: int = 1, backend: str = "brute", literal_nan: bool = False,
+             nthreads: int = 0) -> np.ndarray:
+    """FP32 literal mirror of the three shaders, n_steps steps on a copy of `particles`."""
+    a = np.ascontiguousarray(particles).copy()
+    rc = lib().oracle_step_f32_aos(_pp(params), a.ctypes.data, len(a), n_steps, BACKENDS[backend], nthreads,
+                                   1 if literal_nan else 0)
+    assert rc == 0
+    return a
+
+
+def neighbors(params, particles: np.ndarray, queries, backend: str = "grid", nthreads: int = 0):
+    pos4 = np.ascontiguousarray(particles["pos"], dtype=np.float32)
+    q = np.ascontiguousarray(queries, dtype=np.int64)
+    cnt = np.zeros(len(q), dtype=np.uint32)
+    dig = np.zeros(len(q), dtype=np.uint64)
+    rc = lib().oracle_neighbors(_pp(params), len(pos4), pos4.ctypes.data, len(q), q.ctypes.data, BACKENDS[backend],
+                                nthreads, cnt.ctypes.data, dig.ctypes.data)
+    assert rc == 0
+    return cnt, dig
+
+
+def neighbor_lists(params, particles: np.ndarray, backend: str = "grid", cap: int = 1 << 24):
+    pos4 = np.ascontiguousarray(particles["pos"], dtype=np.float32)
+    n = len(pos4)
+    off = np.zeros(n + 1, dtype=np.int64)
+    items = np.zeros(cap, dtype=np.int64)
+    tot = lib().oracle_neighbor_lists(_pp(params), n, pos4.ctypes.data, BACKENDS[backend], off.ctypes.data,
+                                      items.ctypes.data, cap)
+    assert tot <= cap
+    return off, items[:tot]
+
+
+def cutoff_d2(h: float) -> float:
+    return float(lib().oracle_cutoff_d2(h))
+
+
+def mix64(j: int) -> int:
+    return int(lib().oracle_mix64(j))
+
+
+def max_threads() -> int:
+    return int(lib().oracle_max_threads())
+
+
+def ref_shader_step(particles: np.ndarray, n_steps: int, constants=(0.02, 4.0, 3000.0, 1000.0),
+                    upper=(0.5, 1.0, 0.5, 1.0), lower=(-0.1, -0.35, -0.1, 1.0), nthreads: int = 0) -> np.ndarray:
+    """The reference shaders themselves (compiled as C++) on a copy of 10,000 records."""
+    R = ref()
+    assert len(particles) == R.ref_shader_num_particles()
+    a = np.ascontiguousarray(particles).copy()
+    c = (C.c_float * 4)(*constants)
+    u = (C.c_float * 4)(*upper)
+    lo = (C.c_float * 4)(*lower)
+    rc = R.ref_shader_step(a.ctypes.data, n_steps, c, u, lo, nthreads)
+    assert rc == 0
+    return a

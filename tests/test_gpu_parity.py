@@ -1,0 +1,229 @@
+"""GPU step vs the FP64 oracle, one step at a time from the GPU's own state (the step is
+chaotic, so trajectories are not compared; every step is). All calls go through the C ABI."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from gpu_helpers import check_step
+
+pytestmark = pytest.mark.gpu
+
+
+def run_parity(sph, orc, params, parts, steps, launch=None, stride=1):
+    params = params.copy()
+    params.flags |= sph.FLAG_KEEP_FORCE
+    with sph.Sim(params, n_max=len(parts)) as sim:
+        if launch:
+            sim.set_launch(*launch)
+        sim.upload(parts)
+        state = sim.download()
+        errs = []
+        for s in range(steps):
+            sim.step(1)
+            after = sim.download()
+            if s % stride == 0:
+                errs.append(check_step(orc, params, state, after))
+            state = after
+        sim.synchronize()
+    return errs
+
+
+def tiny(sph, pos, vel=None):
+    a = sph.empty_particles(len(pos))
+    a["pos"][:, :3] = np.asarray(pos, np.float32)
+    a["pos"][:, 3] = 1.0
+    if vel is not None:
+        a["vel"][:, :3] = np.asarray(vel, np.float32)
+    return a
+
+
+def test_isolated_and_small_clusters(sph, orc, gpu):
+    p = sph.default_params()
+    h = p.h
+    run_parity(sph, orc, p, tiny(sph, [[0.2, 0.3, 0.2]]), 3)
+    run_parity(sph, orc, p, tiny(sph, [[0.2, 0.3, 0.2], [0.2 + 0.5 * h, 0.3, 0.2]]), 3)
+    rng = np.random.default_rng(0)
+    pos = 0.2 + rng.uniform(-1.5 * h, 1.5 * h, (27, 3))
+    run_parity(sph, orc, p, tiny(sph, pos, rng.normal(0, 0.1, (27, 3))), 5)
+
+
+def test_coincident_pair_is_finite(sph, orc, gpu):
+    p = sph.default_params()
+    a = tiny(sph, [[0.2, 0.3, 0.2], [0.2, 0.3, 0.2], [0.2 + 0.3 * p.h, 0.3, 0.2]])
+    errs = run_parity(sph, orc, p, a, 2)
+    assert errs
+
+
+def test_reference_literal_scene(sph, orc, gpu):
+    """make_grid() start (0.25h lattice, ~180 neighbours) with the shaders' own constants."""
+    run_parity(sph, orc, sph.default_params(), sph.scene_reference_grid(), 5)
+
+
+def test_reference_scene_10k_200_steps(sph, orc, gpu):
+    """10,000 particles, 0.5h jittered lattice, g = -9.81, 200 steps, every step checked."""
+    sc = sph.reference_scene_10k(seed=1)
+    errs = run_parity(sph, orc, sc.params, sc.particles, sc.steps)
+    assert len(errs) == 200
+
+
+@pytest.mark.parametrize("launch", [(256, 1), (128, 2), (512, 1)])
+def test_dam_break_crop(sph, orc, gpu, launch):
+    sc = sph.dam_break(32, 64, 64, seed=4)
+    run_parity(sph, orc, sc.params, sc.particles, 6, launch=launch)
+
+
+def test_upload_download_roundtrip(sph, gpu):
+    sc = sph.reference_scene_10k(seed=2)
+    a = sc.particles.copy()
+    rng = np.random.default_rng(1)
+    a["vel"] = rng.normal(size=(len(a), 4)).astype(np.float32)
+    a["force"] = rng.normal(size=(len(a), 4)).astype(np.float32)
+    a["extras"] = rng.normal(size=(len(a), 4)).astype(np.float32)
+    with sph.Sim(sc.params, n_max=len(a) + 5) as sim:
+        sim.upload(a)
+        b = sim.download()
+        np.testing.assert_array_equal(a.view(np.uint8), b.view(np.uint8))
+        sim.step(3)
+        c = sim.download()
+        # untouched fields come back as uploaded
+        np.testing.assert_array_equal(c["pos"][:, 3], a["pos"][:, 3])
+        np.testing.assert_array_equal(c["vel"][:, 3], a["vel"][:, 3])
+        np.testing.assert_array_equal(c["extras"][:, 2:], a["extras"][:, 2:])
+        np.testing.assert_array_equal(c["force"], a["force"])  # KEEP_FORCE off
+
+
+def test_device_aos_buffers(sph, gpu):
+    import torch
+
+    sc = sph.reference_scene_10k(seed=3)
+    n = len(sc.particles)
+    dev = torch.from_numpy(sc.particles.view(np.uint8).copy()).to(gpu)
+    with sph.Sim(sc.params, n_max=n) as a, sph.Sim(sc.params, n_max=n) as b:
+        a.upload(sc.particles)
+        torch.cuda.synchronize()
+        b.upload_device(dev.data_ptr(), n)
+        a.step(4)
+        b.step(4)
+        b.download_device(dev.data_ptr(), n)
+        b.synchronize()
+        got = dev.cpu().numpy().view(sph.PARTICLE_DTYPE)
+        np.testing.assert_array_equal(got.view(np.uint8), a.download().view(np.uint8))
+
+
+def test_deterministic(sph, gpu):
+    sc = sph.dam_break(32, 64, 64, seed=6)
+    outs = []
+    for _ in range(2):
+        with sph.Sim(sc.params, n_max=len(sc.particles)) as sim:
+            sim.upload(sc.particles)
+            sim.step(20)
+            outs.append(sim.download())
+    np.testing.assert_array_equal(outs[0].view(np.uint8), outs[1].view(np.uint8))
+
+
+def test_batched_equals_single_scenes(sph, orc, gpu):
+    plist, counts, parts = sph.batched_scenes(12, seed=9, n_lo=500, n_hi=6000)
+    offs = np.concatenate([[0], np.cumsum(counts)])
+    with sph.Sim(plist, counts=counts) as bat:
+        bat.upload(parts)
+        bat.step(5)
+        got = bat.download()
+        diags = bat.reduce_scenes()
+    for i, p in enumerate(plist):
+        seg = parts[offs[i]:offs[i + 1]]
+        with sph.Sim(p, n_max=len(seg)) as one:
+            one.upload(seg)
+            one.step(5)
+            ref = one.download()
+            d1 = one.reduce()
+        np.testing.assert_array_equal(got[offs[i]:offs[i + 1]].view(np.uint8), ref.view(np.uint8))
+        assert diags[i].n == len(seg)
+        assert diags[i].mean_rho == pytest.approx(d1.mean_rho, rel=1e-12)
+
+
+def test_batched_parity_per_scene(sph, orc, gpu):
+    plist, counts, parts = sph.batched_scenes(6, seed=21, n_lo=1000, n_hi=4000)
+    plist = [p.copy() for p in plist]
+    for p in plist:
+        p.flags |= sph.FLAG_KEEP_FORCE
+    offs = np.concatenate([[0], np.cumsum(counts)])
+    with sph.Sim(plist, counts=counts) as bat:
+        bat.upload(parts)
+        state = bat.download()
+        for _ in range(3):
+            bat.step(1)
+            after = bat.download()
+            for i, p in enumerate(plist):
+                check_step(orc, p, state[offs[i]:offs[i + 1]], after[offs[i]:offs[i + 1]])
+            state = after
+
+
+def test_set_params_between_steps(sph, orc, gpu):
+    sc = sph.reference_scene_10k(seed=4)
+    p = sc.params.copy()
+    p.flags |= sph.FLAG_KEEP_FORCE
+    with sph.Sim(p, n_max=len(sc.particles)) as sim:
+        sim.upload(sc.particles)
+        sim.step(2)
+        p2 = p.copy()
+        p2.gas_const, p2.visc, p2.smoothing_coeff = 900.0, 1.5, 4.5
+        sim.set_params(p2)
+        before = sim.download()
+        sim.step(1)
+        check_step(orc, p2, before, sim.download())
+
+
+def test_reduce_matches_host_fp64(sph, gpu):
+    sc = sph.dam_break(32, 64, 64, seed=8)
+    with sph.Sim(sc.params, n_max=len(sc.particles)) as sim:
+        sim.upload(sc.particles)
+        sim.step(5)
+        d = sim.reduce()
+        a = sim.download()
+    m = float(np.float32(sc.params.mass))
+    v = a["vel"][:, :3].astype(np.float64)
+    rho = a["extras"][:, 0].astype(np.float64)
+    np.testing.assert_allclose(d.momentum, m * v.sum(0), rtol=1e-9, atol=1e-12)
+    assert d.kinetic_energy == pytest.approx(0.5 * m * (v * v).sum(), rel=1e-9)
+    assert d.mean_rho == pytest.approx(rho.mean(), rel=1e-12)
+    assert d.min_rho == rho.min() and d.max_rho == rho.max()
+    assert d.nonfinite == 0 and d.n == len(a) and d.step == 5
+
+
+def test_errors(sph, gpu):
+    p = sph.default_params()
+    with sph.Sim(p, n_max=100) as sim:
+        with pytest.raises(sph.SphError) as e:
+            sim.step(1)
+        assert e.value.code == sph.ERR_NOT_READY
+        with pytest.raises(sph.SphError) as e:
+            sim.upload(sph.empty_particles(101))
+        assert e.value.code == sph.ERR_CAPACITY
+        sim.upload(sph.empty_particles(10))
+        with pytest.raises(sph.SphError):
+            sim.download(sph.empty_particles(11))
+        with pytest.raises(sph.SphError):
+            sim.set_launch(100, 1)
+
+
+def test_timing_and_autotune(sph, orc, gpu):
+    sc = sph.dam_break(32, 64, 64, seed=10)
+    p = sc.params.copy()
+    p.flags |= sph.FLAG_KEEP_FORCE
+    with sph.Sim(p, n_max=len(sc.particles)) as sim:
+        sim.upload(sc.particles)
+        sim.enable_timing(True)
+        sim.step(2)
+        t = sim.pass_times()
+        assert all(x > 0 for x in t)
+        sim.enable_timing(False)
+        ms = sim.autotune(3)
+        assert ms > 0
+        blk, sten = sim.get_launch()
+        assert blk in (128, 256, 512) and sten in (1, 2)
+        assert sim.steps == 0  # state restored
+        before = sim.download()
+        np.testing.assert_array_equal(before["pos"], sc.particles["pos"])
+        sim.step(1)
+        check_step(orc, p, before, sim.download())

@@ -1,0 +1,197 @@
+"""Pins of the CPU oracle against the reference itself and against closed-form answers.
+
+The reference has no tests or golden data of its own. Its three compute shaders are
+compiled as C++ (oracle/ref_shader) and stepped on the CPU; tests/golden/make_golden.py
+stored sha256 digests and subsamples of their outputs. Here:
+  - the oracle's FP32 mirror reproduces the shaders bit for bit (1, 3 and 20 steps),
+  - the FP64 oracle agrees with them within FP32 rounding after one step,
+  - closed-form answers derived from the shader formulas hold
+    (rho_pres_comp.glsl:52,58; force_comp.glsl:59-66; integrate_comp.glsl:41-77).
+"""
+from __future__ import annotations
+
+import hashlib
+import math
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+GOLD = np.load(Path(__file__).resolve().parent / "golden" / "reference_shader.npz")
+SUB = slice(0, None, 20)
+PI = float(np.float32(3.141592741))  # the shaders' PI (rho_pres_comp.glsl:8)
+
+
+def sha(a) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def scene(sph, case):
+    if case == "literal":
+        return sph.scene_reference_grid()
+    return sph.reference_scene_10k(seed=1).particles
+
+
+def flat(a):
+    return np.ascontiguousarray(a).view(np.float32).reshape(-1, 16)
+
+
+@pytest.mark.parametrize("case", ["literal", "lattice"])
+def test_scene_generators_match_fixture(sph, case):
+    assert sha(scene(sph, case)) == str(GOLD[f"{case}_input_sha"])
+
+
+@pytest.mark.parametrize("case", ["literal", "lattice"])
+@pytest.mark.parametrize("steps", [1, 3, 20])
+def test_fp32_mirror_is_bit_exact_with_reference_shaders(sph, orc, case, steps):
+    p = sph.default_params()  # the shaders' own constants (G = -9806.65, k = 2000, dt = 1e-4)
+    out = orc.step_f32(p, scene(sph, case), steps, backend="brute", literal_nan=True)
+    np.testing.assert_array_equal(flat(out[SUB]), GOLD[f"{case}_s{steps}_sub"])
+    assert sha(out) == str(GOLD[f"{case}_s{steps}_sha"])
+
+
+@pytest.mark.parametrize("case", ["literal", "lattice"])
+def test_fp64_oracle_one_step_vs_reference_shaders(sph, orc, case):
+    p = sph.default_params()
+    parts = scene(sph, case)
+    o = orc.step_f64(p, parts, backend="brute")
+    g = GOLD[f"{case}_s1_sub"].astype(np.float64)
+    rho, pres, force = o["rho"][SUB], o["pres"][SUB], o["force"][SUB]
+    # The shaders sum in plain FP32; 1e-5 covers their rounding.
+    assert np.max(np.abs(g[:, 12] - rho) / rho) < 1e-5
+    assert np.max(np.abs(g[:, 13] - pres) / (p.gas_const * rho)) < 1e-5
+    ferr = np.linalg.norm(g[:, 8:11] - force, axis=1) / o["fscale"][SUB]
+    assert np.max(ferr) < 1e-5
+    vscale = np.abs(o["vel"][SUB]).max(axis=1) + p.dt * o["fscale"][SUB] / rho
+    assert np.max(np.abs(g[:, 4:7] - o["vel"][SUB]).max(axis=1) / vscale) < 1e-5
+    assert np.max(np.abs(g[:, 0:3] - o["pos"][SUB])) < 1e-6
+
+
+def test_live_reference_shaders_vs_fp32_mirror(sph, orc):
+    """Where the reference tree was present at build time: a fresh seed, stepped both ways."""
+    if not orc.ref_available():
+        pytest.skip("oracle/_ref not built here (the reference tree is absent)")
+    p = sph.default_params()
+    parts = sph.reference_scene_10k(seed=7).particles
+    parts["vel"][:, :3] = np.random.default_rng(7).uniform(-0.5, 0.5, (len(parts), 3)).astype(np.float32)
+    a = orc.ref_shader_step(parts, 2)
+    b = orc.step_f32(p, parts, 2, backend="brute", literal_nan=True)
+    assert sha(a) == sha(b)
+
+
+# ---- closed-form answers ----------------------------------------------------------------------
+
+def one(sph, positions, velocities=None, params=None):
+    a = sph.empty_particles(len(positions))
+    a["pos"][:, :3] = np.asarray(positions, dtype=np.float32)
+    a["pos"][:, 3] = 1.0
+    if velocities is not None:
+        a["vel"][:, :3] = np.asarray(velocities, dtype=np.float32)
+    return a, (params or sph.default_params())
+
+
+def w_poly6(p, r):
+    h = p.h
+    return p.mass * 315.0 * (h * h - r * r) ** 3 / (64.0 * PI * h ** 9)
+
+
+def test_isolated_particle(sph, orc):
+    a, p = one(sph, [[0.2, 0.3, 0.2]])
+    o = orc.step_f64(p, a)
+    h = p.h
+    rho = p.mass * 315.0 / (64.0 * PI * h ** 3)  # self term only
+    assert abs(rho - 3916.7) < 0.1
+    assert o["rho"][0] == pytest.approx(rho, rel=1e-12)
+    assert o["pres"][0] == pytest.approx(p.gas_const * (rho - p.resting_rho), rel=1e-12)
+    np.testing.assert_allclose(o["force"][0], rho * np.array(p.gravity[:]), rtol=1e-12)
+    # a = F / rho = G: v' = dt * G, x' = x + dt * v'
+    np.testing.assert_allclose(o["vel"][0], p.dt * np.array(p.gravity[:]), rtol=1e-12)
+    np.testing.assert_allclose(o["pos"][0], a["pos"][0, :3] + p.dt * o["vel"][0], rtol=1e-12, atol=1e-15)
+
+
+def test_two_particles_density_and_pressure_force(sph, orc):
+    p = sph.default_params()
+    h = p.h
+    r = 0.5 * h
+    a, _ = one(sph, [[0.2, 0.3, 0.2], [0.2 + r, 0.3, 0.2]], params=p)
+    o = orc.step_f64(p, a)
+    rr = float(np.float64(a["pos"][1, 0]) - np.float64(a["pos"][0, 0]))
+    rho = w_poly6(p, 0.0) + w_poly6(p, rr)
+    np.testing.assert_allclose(o["rho"], [rho, rho], rtol=1e-12)
+    pr = max(p.gas_const * (rho - p.resting_rho), 0.0)
+    spiky = -45.0 / (PI * h ** 6)
+    # force_comp.glsl:59 on particle 0: delta = x0 - x1 = (-rr, 0, 0), normalize = (-1, 0, 0)
+    fp = -p.mass * (pr + pr) / (2.0 * rho) * spiky * (h - rr) ** 2 * np.array([-1.0, 0.0, 0.0])
+    f0 = fp + rho * np.array(p.gravity[:])  # equal velocities: no viscosity
+    np.testing.assert_allclose(o["force"][0], f0, rtol=1e-10)
+    assert o["force"][0][0] < 0 and o["force"][1][0] > 0  # repulsion
+    np.testing.assert_allclose(o["force"][0][0], -o["force"][1][0], rtol=1e-12)
+
+
+def test_viscosity_vanishes_at_equal_velocities(sph, orc):
+    p = sph.default_params()
+    pos = [[0.2, 0.3, 0.2], [0.2 + 0.4 * p.h, 0.3, 0.2], [0.2, 0.3 + 0.3 * p.h, 0.2]]
+    a0, _ = one(sph, pos, params=p)
+    a1, _ = one(sph, pos, [[1.0, -2.0, 0.5]] * 3, params=p)
+    np.testing.assert_allclose(orc.step_f64(p, a1)["force"], orc.step_f64(p, a0)["force"], rtol=1e-12, atol=1e-9)
+
+
+def test_viscosity_pulls_towards_neighbour_velocity(sph, orc):
+    p = sph.default_params()
+    p.gravity[1] = 0.0
+    pos = [[0.2, 0.3, 0.2], [0.2, 0.3 + 0.5 * p.h, 0.2]]
+    a, _ = one(sph, pos, [[0.0, 0.0, 0.0], [1.0, 0.0, 0.0]], params=p)
+    o = orc.step_f64(p, a)
+    h, r = p.h, float(np.float64(a["pos"][1, 1]) - np.float64(a["pos"][0, 1]))
+    lap = 45.0 / (PI * h ** 6)
+    fv = p.visc * p.mass * (1.0 - 0.0) / o["rho"][1] * lap * (h - r)  # force_comp.glsl:60,63
+    assert o["force"][0][0] == pytest.approx(fv, rel=1e-10)
+    assert o["force"][1][0] == pytest.approx(-fv, rel=1e-10)
+
+
+def test_wall_clamp_reflects_with_damping(sph, orc):
+    p = sph.default_params()
+    p.gravity[1] = 0.0
+    a, _ = one(sph, [[p.lower[0] + 1e-4, 0.3, 0.2]], [[-5.0, 0.0, 0.0]], params=p)
+    o = orc.step_f64(p, a)
+    assert o["pos"][0][0] == pytest.approx(p.lower[0])
+    assert o["vel"][0][0] == pytest.approx(5.0 * 0.3, rel=1e-6)  # v *= -DAMPING
+    b, _ = one(sph, [[0.2, p.upper[1] - 1e-4, 0.2]], [[0.0, 7.0, 0.0]], params=p)
+    o = orc.step_f64(p, b)
+    assert o["pos"][0][1] == pytest.approx(p.upper[1])
+    assert o["vel"][0][1] == pytest.approx(-7.0 * 0.3, rel=1e-6)
+
+
+def test_symmetric_line_cancels_pressure_on_centre(sph, orc):
+    p = sph.default_params()
+    p.gravity[1] = 0.0
+    d = 0.4 * p.h
+    a, _ = one(sph, [[0.2 - d, 0.3, 0.2], [0.2, 0.3, 0.2], [0.2 + d, 0.3, 0.2]], params=p)
+    o = orc.step_f64(p, a)
+    assert np.all(np.abs(o["force"][1]) <= 1e-9 * o["fscale"][1])
+    assert o["force"][0][0] < 0 < o["force"][2][0]
+
+
+def test_coincident_pair_skips_pressure_instead_of_nan(sph, orc):
+    """Divergence from the shader: normalize(0) (force_comp.glsl:59) is NaN there; the oracle
+    (and the GPU step) skip that pair's pressure term. The FP32 mirror can reproduce either."""
+    p = sph.default_params()
+    a, _ = one(sph, [[0.2, 0.3, 0.2], [0.2, 0.3, 0.2]], params=p)
+    o = orc.step_f64(p, a)
+    assert np.all(np.isfinite(o["force"]))
+    np.testing.assert_allclose(o["force"][0], o["rho"][0] * np.array(p.gravity[:]), rtol=1e-12)
+    lit = orc.step_f32(p, a, 1, literal_nan=True)
+    assert np.isnan(lit["force"][0, 0])
+    ours = orc.step_f32(p, a, 1, literal_nan=False)
+    assert np.all(np.isfinite(ours["force"][:, :3]))
+
+
+def test_neighbour_predicate_is_strict(sph, orc):
+    """rho_pres_comp.glsl:50 `r < smoothing_length`: a pair at exactly r = h is not a neighbour."""
+    p = sph.default_params()
+    h = np.float32(p.h)
+    a, _ = one(sph, [[0.1, 0.3, 0.2], [np.float32(0.1) + h, 0.3, 0.2]], params=p)
+    dx = np.float32(a["pos"][1, 0]) - np.float32(a["pos"][0, 0])
+    cnt, _ = orc.neighbors(p, a, [0, 1], backend="brute")
+    expect = 2 if np.sqrt(np.float32(dx * dx)) < h else 1
+    assert list(cnt) == [expect, expect]
