@@ -147,7 +147,13 @@ sph_status capture_graph(sph_ctx* ctx) {
     enqueue_sort(ctx);
     enqueue_pairs(ctx);
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &ctx->graph);
-    if (e != cudaSuccess) return fail(ctx, SPH_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    cudaError_t launch_err = cudaGetLastError();  // also clears the thread's error state
+    if (e == cudaSuccess) e = launch_err;
+    if (e != cudaSuccess) {
+        if (ctx->graph) cudaGraphDestroy(ctx->graph);
+        ctx->graph = nullptr;
+        return fail(ctx, SPH_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    }
     CK(cudaGraphInstantiate(&ctx->gexec, ctx->graph, 0));
     ctx->graph_dirty = false;
     return SPH_OK;
@@ -223,6 +229,8 @@ sph_status create_impl(const sph_params* params, const uint32_t* counts, uint32_
     sph_status st = SPH_OK;
     auto bail = [&](sph_status s) { sph_destroy(ctx); return s; };
     if (cudaGetDevice(&ctx->device) != cudaSuccess) return bail(SPH_ERR_CUDA);
+    device_sm_count();  // cached before any stream capture
+    init_step_kernels();
     if (stream) {
         ctx->stream = (cudaStream_t)stream;
     } else {

@@ -119,33 +119,45 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(int* __restrict__ count, 
     const int tile_total = s_warp[kScanThreads / 32 - 1];
     const int thread_excl = warp_excl + incl - sum;
 
-    if (threadIdx.x == 0) {
+    // Look-back by warp 0: each probe reads the 32 nearest predecessors at once and
+    // sums back to the nearest one whose inclusive prefix is published.
+    if (warp == 0) {
         int excl = 0;
         if (tile == 0) {
-            st_volatile(&state[0], kFlagPrefix | (unsigned)tile_total);
+            if (lane == 0) st_volatile(&state[0], kFlagPrefix | (unsigned)tile_total);
         } else {
-            st_volatile(&state[tile], kFlagAgg | (unsigned)tile_total);
-            for (int t = tile - 1; t >= 0;) {
-                unsigned long long d = ld_volatile(&state[t]);
+            if (lane == 0) st_volatile(&state[tile], kFlagAgg | (unsigned)tile_total);
+            for (int t = tile - 1;; t -= 32) {
+                const int idx = t - lane;  // lane 0 = nearest predecessor
+                unsigned long long d = idx >= 0 ? ld_volatile(&state[idx]) : kFlagPrefix;
                 int spins = 0;
-                while ((d >> 62) == 0 && spins < kSpinLimit) {
-                    __nanosleep(64);
-                    d = ld_volatile(&state[t]);
-                    ++spins;
+                while (true) {
+                    const bool missing = (d >> 62) == 0;
+                    if (!__any_sync(0xffffffffu, missing) || ++spins > kSpinLimit) break;
+                    if (missing) {
+                        __nanosleep(64);
+                        d = ld_volatile(&state[idx]);
+                    }
                 }
-                if ((d >> 62) == 0) {  // gave up: flag it, continue with what we have
-                    raise_err(err, ERR_SCAN_SPIN);
+                if (__any_sync(0xffffffffu, (d >> 62) == 0)) {  // gave up: flag it, go on with what we have
+                    if (lane == 0) raise_err(err, ERR_SCAN_SPIN);
                     break;
                 }
-                excl += (int)(unsigned)(d & 0xffffffffull);
-                if ((d >> 62) == 2) break;
-                --t;
+                const unsigned pmask = __ballot_sync(0xffffffffu, (d >> 62) == 2);
+                const int first_p = pmask ? __ffs(pmask) - 1 : 32;
+                int val = lane <= first_p ? (int)(unsigned)(d & 0xffffffffull) : 0;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
+                excl += val;
+                if (pmask) break;
             }
-            st_volatile(&state[tile], kFlagPrefix | (unsigned)(excl + tile_total));
+            if (lane == 0) st_volatile(&state[tile], kFlagPrefix | (unsigned)(excl + tile_total));
         }
-        s_prefix = excl;
-        __threadfence();
-        s_last = (atomicAdd(&ticket[1], 1) == ntiles - 1);
+        if (lane == 0) {
+            s_prefix = excl;
+            __threadfence();
+            s_last = (atomicAdd(&ticket[1], 1) == ntiles - 1);
+        }
     }
     __syncthreads();
     int run = s_prefix + thread_excl;
@@ -213,6 +225,7 @@ __global__ void __launch_bounds__(kThreads) k_digest_grid(const float4* __restri
     int qi = (int)qids[q];
     if (qi < 0 || qi >= n) { cnt[q] = 0xffffffffu; dig[q] = 0; return; }
     int t = slot_of_id[qi];
+    if (t < 0 || t >= n) { cnt[q] = 0xffffffffu; dig[q] = 0; return; }
     float4 p = pos_s[t];
     int sc = 0;
     if constexpr (BATCHED) sc = min(max(scene_of(p), 0), nscene - 1);
@@ -257,8 +270,10 @@ __global__ void __launch_bounds__(kThreads) k_digest_brute(const float4* __restr
     float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
     int a = 0, b = 0;
     float cut = s0.cut_d2;
+    int slot = live ? slot_of_id[qi] : 0;
+    if (slot < 0 || slot >= n) live = false;
     if (live) {
-        p = pos_s[slot_of_id[qi]];
+        p = pos_s[slot];
         int sc = 0;
         if constexpr (BATCHED) sc = min(max(scene_of(p), 0), nscene - 1);
         const SceneDev& S = scene_params<BATCHED>(s0, scenes, sc);

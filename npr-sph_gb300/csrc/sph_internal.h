@@ -92,6 +92,8 @@ void launch_neighbor_digest(const Buffers& b, const SceneDev& s0, bool batched, 
                             const uint32_t* qids, int nq, int brute, uint32_t* cnt,
                             unsigned long long* dig, cudaStream_t st);
 // ---- launchers (sph_step.cu) ----
+// Kernel attributes (shared-memory opt-in); called once per process before any capture.
+void init_step_kernels();
 void launch_density(const Buffers& b, const SceneDev& s0, bool batched, const LaunchCfg& c,
                     cudaStream_t st);
 void launch_force_integrate(const Buffers& b, const SceneDev& s0, bool batched, const LaunchCfg& c,

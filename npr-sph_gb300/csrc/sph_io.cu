@@ -15,7 +15,7 @@ namespace sphgb {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kChunks = 64;  // reduction partials per scene
+constexpr int kMaxChunks = 512;  // reduction partials per scene (at most)
 
 __device__ __forceinline__ float4 ld4(const float* f) { return *reinterpret_cast<const float4*>(f); }
 __device__ __forceinline__ void st4(float* f, float4 v) { *reinterpret_cast<float4*>(f) = v; }
@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(kThreads) k_soa_to_aos(const float4* __restric
     }
 }
 
-// FP64 per-scene sums. Grid (kChunks, nscene); each CTA reduces a strided
+// FP64 per-scene sums. Grid (chunks, nscene); each CTA reduces a strided
 // share of its scene's slots in a fixed order (deterministic).
 __global__ void __launch_bounds__(kThreads) k_reduce_partial(const float4* __restrict__ pos, const float4* __restrict__ vel,
                                                              const float2* __restrict__ rhop,
@@ -113,17 +113,17 @@ __global__ void __launch_bounds__(kThreads) k_reduce_partial(const float4* __res
             }
             __syncthreads();
         }
-        if (threadIdx.x == 0) partials[((size_t)sc * kChunks + blockIdx.x) * kDiagFields + f] = sh[0];
+        if (threadIdx.x == 0) partials[((size_t)sc * gridDim.x + blockIdx.x) * kDiagFields + f] = sh[0];
         __syncthreads();
     }
 }
 
-__global__ void k_reduce_final(const double* __restrict__ partials, double* __restrict__ out) {
+__global__ void k_reduce_final(const double* __restrict__ partials, int chunks, double* __restrict__ out) {
     const int sc = blockIdx.x, f = threadIdx.x;
     if (f >= kDiagFields) return;
     double r = f == 6 ? INFINITY : (f == 7 ? -INFINITY : 0.0);
-    for (int c = 0; c < kChunks; ++c) {
-        double x = partials[((size_t)sc * kChunks + c) * kDiagFields + f];
+    for (int c = 0; c < chunks; ++c) {
+        double x = partials[((size_t)sc * chunks + c) * kDiagFields + f];
         r = f == 6 ? fmin(r, x) : (f == 7 ? fmax(r, x) : r + x);
     }
     out[(size_t)sc * kDiagFields + f] = r;
@@ -145,12 +145,18 @@ void launch_soa_to_aos(const Buffers& b, bool force_from_step, sph_particle* aos
                                               b.aux, b.n, aos_dev);
 }
 
-size_t reduce_partials_doubles(int nscene) { return (size_t)nscene * kChunks * kDiagFields; }
+static int reduce_chunks(int nscene) {
+    int c = 4 * device_sm_count() / (nscene > 0 ? nscene : 1);
+    return c < 1 ? 1 : (c > kMaxChunks ? kMaxChunks : c);
+}
+
+size_t reduce_partials_doubles(int nscene) { return (size_t)nscene * reduce_chunks(nscene) * kDiagFields; }
 
 void launch_reduce(const Buffers& b, const SceneDev*, int nscene, double* out_dev, cudaStream_t st) {
-    dim3 grid(kChunks, nscene);
+    const int chunks = reduce_chunks(nscene);
+    dim3 grid(chunks, nscene);
     k_reduce_partial<<<grid, kThreads, 0, st>>>(b.pos, b.vel, b.rhop, b.scenes, b.partials);
-    k_reduce_final<<<nscene, 32, 0, st>>>(b.partials, out_dev);
+    k_reduce_final<<<nscene, 32, 0, st>>>(b.partials, chunks, out_dev);
 }
 
 }  // namespace sphgb

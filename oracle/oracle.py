@@ -45,6 +45,8 @@ def lib() -> C.CDLL:
         L = C.CDLL(str(LIB))
         L.oracle_step_f64.restype = C.c_int
         L.oracle_step_f64.argtypes = [_P, _I64, _P, _P, C.c_int, C.c_int, _P, _P, _P, _P, _P, _P, _P]
+        L.oracle_force_f64.restype = C.c_int
+        L.oracle_force_f64.argtypes = [_P, _I64, _P, _P, _P, _P, C.c_int, C.c_int, _P, _P, _P, _P, _P]
         L.oracle_run_f64.restype = C.c_int
         L.oracle_run_f64.argtypes = [_P, _I64, _P, _P, _P, _P, C.c_int, C.c_int, C.c_int]
         L.oracle_step_f32_aos.restype = C.c_int
@@ -97,6 +99,25 @@ def step_f64(params, particles: np.ndarray, backend: str = "grid", nthreads: int
                                out["rho"].ctypes.data, out["pres"].ctypes.data, out["force"].ctypes.data,
                                out["fscale"].ctypes.data, out["pos"].ctypes.data, out["vel"].ctypes.data,
                                out["margin"].ctypes.data)
+    assert rc == 0
+    return out
+
+
+def force_f64(params, particles: np.ndarray, rho, pres, backend: str = "grid", nthreads: int = 0) -> dict:
+    """The force and integrate passes in FP64 from the state of `particles` and the given
+    densities/pressures (so a GPU force pass is checked on the very inputs it consumed)."""
+    n = len(particles)
+    pos = np.ascontiguousarray(particles["pos"][:, :3], dtype=np.float64)
+    vel = np.ascontiguousarray(particles["vel"][:, :3], dtype=np.float64)
+    rho = np.ascontiguousarray(rho, dtype=np.float64)
+    pres = np.ascontiguousarray(pres, dtype=np.float64)
+    out = {"rho": rho, "pres": pres, "fscale": np.zeros(n), "margin": np.zeros(n)}
+    for k in ("force", "pos", "vel"):
+        out[k] = np.zeros((n, 3))
+    rc = lib().oracle_force_f64(_pp(params), n, pos.ctypes.data, vel.ctypes.data, rho.ctypes.data,
+                                pres.ctypes.data, BACKENDS[backend], nthreads, out["force"].ctypes.data,
+                                out["fscale"].ctypes.data, out["pos"].ctypes.data, out["vel"].ctypes.data,
+                                out["margin"].ctypes.data)
     assert rc == 0
     return out
 

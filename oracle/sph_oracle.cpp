@@ -169,9 +169,12 @@ uint64_t oracle_mix64(uint64_t j) { return mix64(j); }
 //                    scale of the force error metric (pressure terms cancel inside).
 //   wall_margin[i] = distance of the unclamped new position to the nearest wall plane.
 //   backend: 0 brute force, 1 grid.
-int oracle_step_f64(const sph_params* P, int64_t n, const double* pos, const double* vel,
-                    int backend, int nthreads, double* rho, double* pres, double* force,
-                    double* fscale, double* pos_out, double* vel_out, double* wall_margin) {
+//   rho_given: 0 computes rho/pres (pass 1); 1 takes them as inputs and runs the force and
+//              integrate passes only (the check of a force pass fed the same densities).
+static int step_f64_impl(const sph_params* P, int64_t n, const double* pos, const double* vel,
+                         int backend, int nthreads, double* rho, double* pres, double* force,
+                         double* fscale, double* pos_out, double* vel_out, double* wall_margin,
+                         int rho_given) {
     if (!P || n < 0 || !pos || !vel || !rho || !pres || !pos_out || !vel_out) return -1;
     if (nthreads <= 0) nthreads = omp_get_max_threads();
     const float hf = P->smoothing_coeff * P->particle_radius;  // rho_pres_comp.glsl:40 (FP32)
@@ -191,7 +194,7 @@ int oracle_step_f64(const sph_params* P, int64_t n, const double* pos, const dou
 
     // Pass 1: density + pressure (rho_pres_comp.glsl:43-58).
 #pragma omp parallel for schedule(dynamic, 256) num_threads(nthreads)
-    for (int64_t i = 0; i < n; ++i) {
+    for (int64_t i = 0; i < (rho_given ? 0 : n); ++i) {
         double r_acc = 0.0;
         for_candidates(g, n, i, getpos, [&](int64_t j) {
             float d2f = canon_d2(pf[3*i], pf[3*i+1], pf[3*i+2], pf[3*j], pf[3*j+1], pf[3*j+2]);
@@ -255,6 +258,21 @@ int oracle_step_f64(const sph_params* P, int64_t n, const double* pos, const dou
         if (wall_margin) wall_margin[i] = margin;
     }
     return 0;
+}
+
+int oracle_step_f64(const sph_params* P, int64_t n, const double* pos, const double* vel,
+                    int backend, int nthreads, double* rho, double* pres, double* force,
+                    double* fscale, double* pos_out, double* vel_out, double* wall_margin) {
+    return step_f64_impl(P, n, pos, vel, backend, nthreads, rho, pres, force, fscale, pos_out, vel_out,
+                         wall_margin, 0);
+}
+
+// Force + integrate passes (force_comp.glsl, integrate_comp.glsl) from given rho/pres.
+int oracle_force_f64(const sph_params* P, int64_t n, const double* pos, const double* vel,
+                     const double* rho, const double* pres, int backend, int nthreads, double* force,
+                     double* fscale, double* pos_out, double* vel_out, double* wall_margin) {
+    return step_f64_impl(P, n, pos, vel, backend, nthreads, const_cast<double*>(rho),
+                         const_cast<double*>(pres), force, fscale, pos_out, vel_out, wall_margin, 1);
 }
 
 // n_steps FP64 steps in place (state in double). The CPU baseline.

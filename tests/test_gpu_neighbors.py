@@ -81,7 +81,7 @@ def test_edge_cases(sph, orc, gpu, stencil):
 
 def test_batched_neighbours(sph, orc, gpu):
     plist, counts, parts = sph.batched_scenes(8, seed=31, n_lo=2000, n_hi=8000)
-    offs = np.concatenate([[0], np.cumsum(counts)])
+    offs = np.concatenate([[0], np.cumsum(counts, dtype=np.int64)])
     q = np.arange(len(parts), dtype=np.uint32)
     with sph.Sim(plist, counts=counts) as sim:
         sim.upload(parts)

@@ -124,7 +124,7 @@ def test_deterministic(sph, gpu):
 
 def test_batched_equals_single_scenes(sph, orc, gpu):
     plist, counts, parts = sph.batched_scenes(12, seed=9, n_lo=500, n_hi=6000)
-    offs = np.concatenate([[0], np.cumsum(counts)])
+    offs = np.concatenate([[0], np.cumsum(counts, dtype=np.int64)])
     with sph.Sim(plist, counts=counts) as bat:
         bat.upload(parts)
         bat.step(5)
@@ -147,7 +147,7 @@ def test_batched_parity_per_scene(sph, orc, gpu):
     plist = [p.copy() for p in plist]
     for p in plist:
         p.flags |= sph.FLAG_KEEP_FORCE
-    offs = np.concatenate([[0], np.cumsum(counts)])
+    offs = np.concatenate([[0], np.cumsum(counts, dtype=np.int64)])
     with sph.Sim(plist, counts=counts) as bat:
         bat.upload(parts)
         state = bat.download()
@@ -218,12 +218,14 @@ def test_timing_and_autotune(sph, orc, gpu):
         t = sim.pass_times()
         assert all(x > 0 for x in t)
         sim.enable_timing(False)
+        start = sim.download()
         ms = sim.autotune(3)
         assert ms > 0
         blk, sten = sim.get_launch()
         assert blk in (128, 256, 512) and sten in (1, 2)
-        assert sim.steps == 0  # state restored
+        assert sim.steps == 2  # the state the autotuner started from is restored
         before = sim.download()
-        np.testing.assert_array_equal(before["pos"], sc.particles["pos"])
+        np.testing.assert_array_equal(before["pos"], start["pos"])
+        np.testing.assert_array_equal(before["vel"], start["vel"])
         sim.step(1)
         check_step(orc, p, before, sim.download())

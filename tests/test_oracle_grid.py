@@ -73,6 +73,14 @@ def test_fp64_step_grid_equals_brute(sph, orc):
     np.testing.assert_allclose(g["force"], b["force"], rtol=0, atol=1e-10 * b["fscale"].max())
 
 
+def test_force_pass_from_given_densities_matches_full_step(sph, orc):
+    sc = sph.reference_scene_10k(seed=6)
+    full = orc.step_f64(sc.params, sc.particles)
+    part = orc.force_f64(sc.params, sc.particles, full["rho"], full["pres"])
+    for k in ("force", "fscale", "pos", "vel", "margin"):
+        np.testing.assert_array_equal(part[k], full[k])
+
+
 def test_cutoff_threshold_is_exact(sph, orc):
     for h in [0.02, 0.01, 0.0199999996, 1.0, 3.3e-3, 7.77]:
         hf = np.float32(h)
