@@ -187,13 +187,18 @@ uint32_t sph_num_scenes(const sph_ctx* ctx);
 sph_status sph_reduce_scenes(sph_ctx* ctx, sph_diag* out, uint32_t n_scene);
 
 /* ---- launch shape and autotuner (new) ----------------------------------
- * threads_per_block of the pair passes (64..1024, multiple of 32) and
- * stencil (1: cell edge >= h, 27 cells; 2: cell edge >= h/2, 125 smaller cells).
+ * threads_per_block of the pair passes (128 or 256: the particles of one
+ * shared-memory tile) and stencil (1: cell edge >= h, 27 cells; 2: cell edge
+ * >= h/2, 125 smaller cells).
  * sph_autotune times `trial_steps` steps of every candidate shape on the
  * current state (restoring it afterwards) and keeps the fastest. */
 sph_status sph_set_launch(sph_ctx* ctx, int32_t threads_per_block, int32_t stencil);
 sph_status sph_get_launch(const sph_ctx* ctx, int32_t* threads_per_block, int32_t* stencil);
 sph_status sph_autotune(sph_ctx* ctx, int32_t trial_steps, float* best_ms_per_step);
+/* Chunks of the density (out[0]) and force (out[1]) passes, since creation,
+ * that did not fit a shared-memory tile and read their neighbours from global
+ * memory instead (heavy pile-ups). Synchronous. */
+sph_status sph_tile_stats(sph_ctx* ctx, uint32_t out[2]);
 
 /* ---- scene generators (host only; no GPU needed) ----------------------- */
 

@@ -90,11 +90,13 @@ void free_graph(sph_ctx* ctx) {
 // the cell arrays when needed. Leaves count zeroed and asks for a fresh hash.
 sph_status rebuild_geometry(sph_ctx* ctx) {
     std::vector<SceneDev> sc(ctx->params.size());
-    long long cell = 0, first = 0;
+    long long cell = 0, first = 0, rows = 0;
     const bool keep = (ctx->params[0].flags & SPH_FLAG_KEEP_FORCE) != 0;
     for (size_t i = 0; i < sc.size(); ++i) {
         sc[i] = make_scene_dev(ctx->params[i], ctx->cfg.stencil, (int)cell, (int)first, (int)ctx->counts[i], keep);
+        sc[i].row_base = (int)rows;
         cell += (long long)sc[i].dim[0] * sc[i].dim[1] * sc[i].dim[2];
+        rows += (long long)sc[i].dim[1] * sc[i].dim[2];
         first += ctx->counts[i];
         if (cell >= (1ll << 31) - 1) return fail(ctx, SPH_ERR_INVALID_ARG, "too many grid cells");
     }
@@ -242,11 +244,12 @@ sph_status create_impl(const sph_params* params, const uint32_t* counts, uint32_
     if (dalloc(&b.pos, n) || dalloc(&b.vel, n) || dalloc(&b.pos_s, n) || dalloc(&b.vel_s, n) ||
         dalloc(&b.rhop, n) || dalloc(&b.force_s, n) || dalloc(&b.force_up, n) || dalloc(&b.aux, n) ||
         dalloc(&b.key, n) || dalloc(&b.rank, n) || dalloc(&b.perm, n) || dalloc(&b.slot_of_id, n) ||
-        dalloc(&b.err, 1) || dalloc(&b.scan_ticket, 2) || dalloc(&b.scenes, nscene) ||
+        dalloc(&b.err, 1) || dalloc(&b.scan_ticket, 2) || dalloc(&b.scenes, nscene) || dalloc(&b.tile_stats, 2) ||
         dalloc(&b.partials, reduce_partials_doubles((int)nscene)) ||
         dalloc(&ctx->diag_dev, (size_t)nscene * kDiagFields) || dalloc(&ctx->scene_first_dev, nscene + 1))
         return bail(SPH_ERR_OUT_OF_MEMORY);
     if (cudaMemsetAsync(b.err, 0, sizeof(uint32_t), ctx->stream) ||
+        cudaMemsetAsync(b.tile_stats, 0, sizeof(uint32_t) * 2, ctx->stream) ||
         cudaMemsetAsync(b.scan_ticket, 0, sizeof(int) * 2, ctx->stream))
         return bail(SPH_ERR_CUDA);
     for (auto& e : ctx->ev)
@@ -366,7 +369,7 @@ sph_status sph_destroy(sph_ctx* ctx) {
     Buffers& b = ctx->b;
     void* ptrs[] = {b.pos, b.vel, b.pos_s, b.vel_s, b.rhop, b.force_s, b.force_up, b.aux, b.aos, b.key, b.rank,
                     b.perm, b.count, b.start, b.scan_state, b.scan_ticket, b.slot_of_id, b.err, b.partials,
-                    b.scenes, ctx->diag_dev, ctx->scene_first_dev, ctx->q_ids, ctx->q_cnt, ctx->q_dig};
+                    b.scenes, b.tile_stats, ctx->diag_dev, ctx->scene_first_dev, ctx->q_ids, ctx->q_cnt, ctx->q_dig};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (auto& e : ctx->ev)
@@ -511,8 +514,8 @@ sph_status sph_neighbor_digest(sph_ctx* ctx, const uint32_t* query_ids, uint32_t
 
 sph_status sph_set_launch(sph_ctx* ctx, int32_t tpb, int32_t stencil) {
     if (!ctx) return SPH_ERR_INVALID_ARG;
-    if (tpb < 64 || tpb > 1024 || (tpb % 32) || (stencil != 1 && stencil != 2))
-        return fail(ctx, SPH_ERR_INVALID_ARG, "threads_per_block in [64,1024] multiple of 32, stencil 1 or 2");
+    if ((tpb != 128 && tpb != 256) || (stencil != 1 && stencil != 2))
+        return fail(ctx, SPH_ERR_INVALID_ARG, "threads_per_block 128 or 256, stencil 1 or 2");
     GUARD_BEGIN
     CK(cudaSetDevice(ctx->device));
     bool geo = stencil != ctx->cfg.stencil;
@@ -522,6 +525,14 @@ sph_status sph_set_launch(sph_ctx* ctx, int32_t tpb, int32_t stencil) {
     free_graph(ctx);
     return SPH_OK;
     GUARD_END
+}
+
+sph_status sph_tile_stats(sph_ctx* ctx, uint32_t out[2]) {
+    if (!ctx || !out) return SPH_ERR_INVALID_ARG;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaMemcpyAsync(out, ctx->b.tile_stats, sizeof(uint32_t) * 2, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SPH_OK;
 }
 
 sph_status sph_get_launch(const sph_ctx* ctx, int32_t* tpb, int32_t* stencil) {
@@ -551,7 +562,7 @@ sph_status sph_autotune(sph_ctx* ctx, int32_t trial_steps, float* best_ms) {
     const uint64_t steps0 = ctx->steps;
     const bool stepped0 = ctx->stepped, timing0 = ctx->timing;
     ctx->timing = false;
-    const int blocks[] = {128, 256, 512};
+    const int blocks[] = {128, 256};
     const int stencils[] = {1, 2};
     float best = 1e30f;
     LaunchCfg best_cfg = ctx->cfg;

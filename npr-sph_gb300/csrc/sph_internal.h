@@ -39,7 +39,8 @@ struct SceneDev {
     float damp;       // DAMPING (integrate_comp.glsl:8)
     float mass;
     int keep_force;
-    int pad_[2];
+    int row_base;     // first cell row (y, z) of this scene in the global row numbering
+    int pad_;
 };
 
 // Device buffers of one engine (single scene or a batch of scenes).
@@ -69,6 +70,7 @@ struct Buffers {
     int n = 0;
     int ncell = 0;
     int nscene = 1;
+    uint32_t* tile_stats = nullptr;  // [0] chunks staged, [1] chunks on the global-memory path
 };
 
 // Launch shape chosen by the autotuner.

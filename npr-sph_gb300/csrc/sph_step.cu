@@ -8,30 +8,36 @@
 //                                               v *= -damping
 //                    + the cell hash of the new position for the next step's sort.
 //
-// One thread per particle in cell-sorted order: the threads of a warp walk the
-// same few cells, so their candidate loads hit L1. Each thread visits the
-// (2R+1)^2 rows of (2R+1) contiguous cells around its own cell (cell edge h/R).
+// Work decomposition: a CTA takes a chunk of BLOCK consecutive sorted slots
+// (one target particle per thread). Consecutive slots share a cell row
+// (y, z) -- or a few rows, or several small scenes. For every distinct row of
+// the chunk the CTA stages the (2R+1)^2 neighbour-row segments it needs (cells
+// x_first-R .. x_last+R of each neighbour row) into shared memory as SoA
+// x/y/z arrays, padded to even length with a sentinel that fails every test.
+// Each thread then scans the sub-range of each segment that covers its own
+// cells cx-R..cx+R, two candidates at a time: one 8-byte shared load per
+// coordinate and packed FP32x2 arithmetic (__fadd2_rn / __fmul2_rn, each lane
+// rounded on its own, so the neighbour predicate is the canonical FP32
+// expression bit for bit). Rounding a sub-range out to even bounds only adds
+// candidates from cells two cells away (never within h: cell edge >= h/R with
+// margin) or the sentinel.
 //
-// Two phases per thread, so that the warp never runs the interaction code for
-// a minority of lanes (with ~15% of candidates inside r < h, some lane almost
-// always would):
-//   1. candidate scan: the canonical FP32 predicate on every candidate; the
-//      passing ones are appended to a per-thread list in shared memory
-//      (density keeps d2, force keeps the slot j),
-//   2. interaction loop over the list, all lanes busy.
-// The list holds kNbCap entries; a longer neighbourhood is processed in chunks.
-// Neighbours are visited in candidate order either way, so results are
-// deterministic and independent of the chunking.
+// Passing candidates are appended to a per-thread list in shared memory
+// (density: d2; force: the staged index), then processed in a second loop in
+// which all lanes are busy: with ~15% of candidates inside r < h, testing and
+// interacting in one loop would run the interaction code for a minority of
+// lanes almost every iteration. Lists hold kNbCap* entries; longer
+// neighbourhoods are processed in chunks, in candidate order, so results are
+// deterministic either way.
 //
-// The (dx, dy) part of the predicate runs as one packed FP32x2 subtraction and
-// one packed multiplication (sub.rn.f32x2 / mul.rn.f32x2): each lane is
-// rounded on its own, exactly like __fsub_rn / __fmul_rn, so the neighbour
-// predicate stays bit-exact.
+// A chunk with more distinct rows or more staged candidates than the tile
+// holds (heavy pile-ups) takes a global-memory path with the same arithmetic.
 //
 // Numerics: the density sum is compensated (Kahan) in FP32; the force sums are
 // plain FP32 with contraction allowed (only the predicate is pinned bit-exact).
 // For i != j at r == 0 the pressure term is skipped (the shader's
 // normalize(0) is NaN, force_comp.glsl:59); the viscosity term is kept.
+#include <climits>
 #include <type_traits>
 
 #include "sph_device.cuh"
@@ -40,93 +46,282 @@ namespace sphgb {
 
 namespace {
 
-constexpr int kNbCap = 32;  // shared-memory neighbour list entries per thread
+// BLOCK threads per CTA = target particles per chunk (128 or 256, autotuned).
+template <int BLOCK> constexpr int stage_cap() { return 11 * BLOCK; }  // staged candidates per chunk
+constexpr int kNbCapDensity = 24;       // density list entries per thread (d2, float)
+constexpr int kNbCapForce = 40;         // force list entries per thread (staged index, u16)
+constexpr float kSentinel = 1e30f;      // staged padding: its distance to any particle is +inf
 
-// (px - ox, py - oy) and their squares, each lane rounded separately.
-__device__ __forceinline__ void sub_sq_xy(float px, float py, float ox, float oy, float& dx, float& dy, float& sx,
-                                          float& sy) {
-    asm("{\n\t.reg .b64 a, b, d, s;\n\t"
-        "mov.b64 a, {%4, %5};\n\t"
-        "mov.b64 b, {%6, %7};\n\t"
-        "sub.rn.f32x2 d, a, b;\n\t"
-        "mul.rn.f32x2 s, d, d;\n\t"
-        "mov.b64 {%0, %1}, d;\n\t"
-        "mov.b64 {%2, %3}, s;\n\t}"
-        : "=f"(dx), "=f"(dy), "=f"(sx), "=f"(sy)
-        : "f"(px), "f"(py), "f"(ox), "f"(oy));
-}
+template <int R>
+struct TileGeom {
+    static constexpr int kSide = 2 * R + 1;
+    static constexpr int kSegPerRow = kSide * kSide;
+    static constexpr int kMaxRows = R == 1 ? 32 : 16;
+    static constexpr int kMaxSeg = kMaxRows * kSegPerRow;
+};
 
-// canon_d2 (sph_device.cuh) with the x/y lanes packed.
-__device__ __forceinline__ float canon_d2_pk(float px, float py, float pz, float4 o, float& dx, float& dy, float& dz) {
-    float sx, sy;
-    sub_sq_xy(px, py, o.x, o.y, dx, dy, sx, sy);
-    dz = __fsub_rn(pz, o.z);
-    return __fadd_rn(__fadd_rn(sx, sy), __fmul_rn(dz, dz));
-}
+template <int R, int BLOCK>
+struct TileShared {
+    static constexpr int kWarps = BLOCK / 32;
+    int rowid[BLOCK];
+    int row_scene[TileGeom<R>::kMaxRows], row_y[TileGeom<R>::kMaxRows], row_z[TileGeom<R>::kMaxRows];
+    int row_xa[TileGeom<R>::kMaxRows], row_xb[TileGeom<R>::kMaxRows];
+    int seg_gbeg[TileGeom<R>::kMaxSeg], seg_len[TileGeom<R>::kMaxSeg], seg_nrow[TileGeom<R>::kMaxSeg];
+    int seg_off[TileGeom<R>::kMaxSeg + 1];
+    int warp_cnt[kWarps];
+};
 
-// Iterate the stencil rows around cell (cx, cy, cz): calls fn(a, b) with the
-// contiguous sorted-slot range [a, b) of cells cx-R..cx+R of each row.
-template <int R, class Fn>
-__device__ __forceinline__ void for_rows(const SceneDev& S, const int* __restrict__ start, int n, int cx, int cy,
-                                         int cz, Fn fn) {
-    const int x0 = max(cx - R, 0), x1 = min(cx + R, S.dim[0] - 1);
-    const int z0 = max(cz - R, 0), z1 = min(cz + R, S.dim[2] - 1);
-    const int y0 = max(cy - R, 0), y1 = min(cy + R, S.dim[1] - 1);
-    for (int z = z0; z <= z1; ++z) {
-        for (int y = y0; y <= y1; ++y) {
-            const int row = S.cell_base + S.dim[0] * (y + S.dim[1] * z);
-            const int a = max(__ldg(start + row + x0), 0);
-            const int b = min(__ldg(start + row + x1 + 1), n);
-            fn(a, b);
+struct Staged {
+    float* x;
+    float* y;
+    float* z;
+    int* slot;  // global slot of each staged candidate (force only)
+};
+
+// Plan and stage one chunk [c0, c0 + BLOCK). Every thread of the CTA calls it.
+// Returns false (for the whole CTA) when the chunk does not fit the tile.
+// On return each live thread has its position p, scene sc, cell cx and local row lrow.
+template <bool BATCHED, int R, int BLOCK>
+__device__ bool stage_chunk(TileShared<R, BLOCK>& T, const Staged& st, int c0, int n, const float4* __restrict__ pos_s,
+                            const int* __restrict__ start, const SceneDev& s0, const SceneDev* __restrict__ scenes,
+                            int nscene, float4& p, int& sc, int& cx, int& lrow) {
+    using G = TileGeom<R>;
+    constexpr int kWarps = BLOCK / 32;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int t = c0 + tid;
+    const bool live = t < n;
+    int cy = 0, cz = 0, rowid = INT_MAX;
+    sc = 0;
+    cx = 0;
+    if (live) {
+        p = pos_s[t];
+        if constexpr (BATCHED) sc = min(max(scene_of(p), 0), nscene - 1);
+        const SceneDev& S = scene_params<BATCHED>(s0, scenes, sc);
+        cx = cell_coord(p.x, S.lo[0], S.inv_edge, S.dim[0]);
+        cy = cell_coord(p.y, S.lo[1], S.inv_edge, S.dim[1]);
+        cz = cell_coord(p.z, S.lo[2], S.inv_edge, S.dim[2]);
+        rowid = S.row_base + cy + S.dim[1] * cz;
+    }
+    T.rowid[tid] = rowid;
+    __syncthreads();
+    const bool first = live && (tid == 0 || T.rowid[tid - 1] != rowid);
+    const bool last = live && (tid == BLOCK - 1 || T.rowid[tid + 1] != rowid);
+    const unsigned fb = __ballot_sync(0xffffffffu, first);
+    if (lane == 0) T.warp_cnt[warp] = __popc(fb);
+    __syncthreads();
+    int before = 0, nrows = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) {
+        const int c = T.warp_cnt[w];
+        before += w < warp ? c : 0;
+        nrows += c;
+    }
+    if (nrows > G::kMaxRows) return false;  // uniform
+    lrow = before + __popc(fb & ((1u << lane) - 1)) + (first ? 1 : 0) - 1;
+    if (first) {
+        T.row_scene[lrow] = sc;
+        T.row_y[lrow] = cy;
+        T.row_z[lrow] = cz;
+        T.row_xa[lrow] = cx;
+    }
+    if (last) T.row_xb[lrow] = cx;
+    __syncthreads();
+    const int nseg = nrows * G::kSegPerRow;
+    for (int s = tid; s < nseg; s += BLOCK) {
+        const int m = s / G::kSegPerRow, r = s % G::kSegPerRow;
+        const int dz = r / G::kSide - R, dy = r % G::kSide - R;
+        const SceneDev& S = scene_params<BATCHED>(s0, scenes, T.row_scene[m]);
+        const int yy = T.row_y[m] + dy, zz = T.row_z[m] + dz;
+        int gbeg = 0, len = 0, nrow = 0;
+        if (yy >= 0 && yy < S.dim[1] && zz >= 0 && zz < S.dim[2]) {
+            nrow = S.cell_base + S.dim[0] * (yy + S.dim[1] * zz);
+            const int xa = max(T.row_xa[m] - R, 0), xb = min(T.row_xb[m] + R, S.dim[0] - 1);
+            gbeg = min(max(__ldg(start + nrow + xa), 0), n);
+            const int gend = min(max(__ldg(start + nrow + xb + 1), 0), n);
+            len = max(gend - gbeg, 0);
+        }
+        T.seg_gbeg[s] = gbeg;
+        T.seg_len[s] = len;
+        T.seg_nrow[s] = nrow;
+    }
+    __syncthreads();
+    if (warp == 0) {  // exclusive scan of the even-padded segment lengths
+        const int per = (nseg + 31) / 32, lo = lane * per, hi = min(lo + per, nseg);
+        int local = 0;
+        for (int i = lo; i < hi; ++i) local += (T.seg_len[i] + 1) & ~1;
+        int incl = local;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        int run = incl - local;
+        for (int i = lo; i < hi; ++i) {
+            T.seg_off[i] = run;
+            run += (T.seg_len[i] + 1) & ~1;
+        }
+        if (lane == 31) T.seg_off[nseg] = incl;
+    }
+    __syncthreads();
+    if (T.seg_off[nseg] > stage_cap<BLOCK>()) return false;  // uniform
+    for (int s = warp; s < nseg; s += kWarps) {
+        const int gbeg = T.seg_gbeg[s], len = T.seg_len[s], off = T.seg_off[s];
+        const int plen = (len + 1) & ~1;
+        for (int k = lane; k < plen; k += 32) {
+            float x = kSentinel, y = kSentinel, z = kSentinel;
+            if (k < len) {
+                const float4 o = __ldg(pos_s + gbeg + k);
+                x = o.x; y = o.y; z = o.z;
+            }
+            st.x[off + k] = x;
+            st.y[off + k] = y;
+            st.z[off + k] = z;
+            if (st.slot) st.slot[off + k] = k < len ? gbeg + k : 0;
         }
     }
+    __syncthreads();
+    return true;
 }
+
+// Staged sub-range of segment s that covers cells cx-R..cx+R of its row, rounded out to even.
+template <int R, int BLOCK>
+__device__ __forceinline__ void seg_range(const TileShared<R, BLOCK>& T, int s, int cx, int dimx,
+                                          const int* __restrict__ start, int& a, int& b) {
+    const int len = T.seg_len[s];
+    if (len == 0) { a = b = 0; return; }
+    const int nrow = T.seg_nrow[s], gbeg = T.seg_gbeg[s], off = T.seg_off[s];
+    const int ga = __ldg(start + nrow + max(cx - R, 0));
+    const int gb = __ldg(start + nrow + min(cx + R, dimx - 1) + 1);
+    a = off + min(max(ga - gbeg, 0), len);
+    b = off + min(max(gb - gbeg, 0), len);
+    a &= ~1;
+}
+
+// d2 of two staged candidates j, j+1 against (px, py, pz), given as npx = (-px, -px) etc.:
+// (x_j - px)^2 + ... is the canonical d2 (the sign of a difference does not change its square).
+__device__ __forceinline__ float2 pair_d2(const Staged& st, int j, float2 npx, float2 npy, float2 npz) {
+    const float2 X = *reinterpret_cast<const float2*>(st.x + j);
+    const float2 Y = *reinterpret_cast<const float2*>(st.y + j);
+    const float2 Z = *reinterpret_cast<const float2*>(st.z + j);
+    const float2 dx = __fadd2_rn(X, npx), dy = __fadd2_rn(Y, npy), dz = __fadd2_rn(Z, npz);
+    return __fadd2_rn(__fadd2_rn(__fmul2_rn(dx, dx), __fmul2_rn(dy, dy)), __fmul2_rn(dz, dz));
+}
+
+// Stencil rows around cell (cx, cy, cz) over global memory (the fallback path).
+template <int R, class Fn>
+__device__ __forceinline__ void for_rows_global(const SceneDev& S, const int* __restrict__ start, int n, int cx, int cy,
+                                                int cz, Fn fn) {
+    const int x0 = max(cx - R, 0), x1 = min(cx + R, S.dim[0] - 1);
+    for (int z = max(cz - R, 0); z <= min(cz + R, S.dim[2] - 1); ++z)
+        for (int y = max(cy - R, 0); y <= min(cy + R, S.dim[1] - 1); ++y) {
+            const int row = S.cell_base + S.dim[0] * (y + S.dim[1] * z);
+            fn(max(__ldg(start + row + x0), 0), min(__ldg(start + row + x1 + 1), n));
+        }
+}
+
+__device__ __forceinline__ void kahan_add(float& sum, float& comp, float x) {
+    const float y = x - comp;
+    const float t = sum + y;
+    comp = (t - sum) - y;
+    sum = t;
+}
+
+template <int BLOCK>
+constexpr size_t density_smem() { return (size_t)3 * stage_cap<BLOCK>() * 4 + (size_t)kNbCapDensity * BLOCK * 4; }
+template <int BLOCK>
+constexpr size_t force_smem() { return (size_t)4 * stage_cap<BLOCK>() * 4 + (size_t)kNbCapForce * BLOCK * 2; }
+static_assert(stage_cap<256>() < 65536, "staged indices are 16-bit");
 
 template <bool BATCHED, int R, int BLOCK>
 __global__ void __launch_bounds__(BLOCK) k_density(const float4* __restrict__ pos_s, const int* __restrict__ start,
                                                    SceneDev s0, const SceneDev* __restrict__ scenes, int nscene,
-                                                   float2* __restrict__ rhop, int n) {
-    extern __shared__ float s_d2[];  // [kNbCap][BLOCK]
-    float* lst = s_d2 + threadIdx.x;
-    for (int t = blockIdx.x * BLOCK + threadIdx.x; t < n; t += gridDim.x * BLOCK) {
-        const float4 p = pos_s[t];
-        int sc = 0;
-        if constexpr (BATCHED) sc = min(max(scene_of(p), 0), nscene - 1);
-        const SceneDev& S = scene_params<BATCHED>(s0, scenes, sc);
-        const float cut = S.cut_d2, h2 = S.h2;
-        const int cx = cell_coord(p.x, S.lo[0], S.inv_edge, S.dim[0]);
-        const int cy = cell_coord(p.y, S.lo[1], S.inv_edge, S.dim[1]);
-        const int cz = cell_coord(p.z, S.lo[2], S.inv_edge, S.dim[2]);
-        float sum = 0.0f, comp = 0.0f;
-        int cnt = 0;
-        auto flush = [&]() {
-            for (int k = 0; k < cnt; ++k) {
-                const float w = h2 - lst[k * BLOCK];
-                const float yk = w * w * w - comp;  // Kahan step
-                const float tk = sum + yk;
-                comp = (tk - sum) - yk;
-                sum = tk;
-            }
-            cnt = 0;
-        };
-        for_rows<R>(S, start, n, cx, cy, cz, [&](int a, int b) {
-#pragma unroll 4
-            for (int j = a; j < b; ++j) {
-                const float4 o = __ldg(pos_s + j);
-                float dx, dy, dz;
-                const float d2 = canon_d2_pk(p.x, p.y, p.z, o, dx, dy, dz);
-                if (d2 < cut) {
-                    lst[cnt * BLOCK] = d2;
-                    if (++cnt == kNbCap) flush();
+                                                   float2* __restrict__ rhop, int n, uint32_t* __restrict__ stats) {
+    using G = TileGeom<R>;
+    constexpr int kCap = stage_cap<BLOCK>();
+    __shared__ TileShared<R, BLOCK> T;
+    extern __shared__ float4 dyn_d[];
+    float* base = reinterpret_cast<float*>(dyn_d);
+    const Staged st{base, base + kCap, base + 2 * kCap, nullptr};
+    float* lst = base + 3 * kCap + threadIdx.x;  // [kNbCapDensity][BLOCK]
+    for (int c0 = blockIdx.x * BLOCK; c0 < n; c0 += gridDim.x * BLOCK) {
+        float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+        int sc = 0, cx = 0, lrow = 0;
+        const bool tiled =
+            stage_chunk<BATCHED, R, BLOCK>(T, st, c0, n, pos_s, start, s0, scenes, nscene, p, sc, cx, lrow);
+        const int t = c0 + threadIdx.x;
+        if (t < n) {
+            if (!tiled) p = pos_s[t];
+            if constexpr (BATCHED) sc = min(max(scene_of(p), 0), nscene - 1);
+            const SceneDev& S = scene_params<BATCHED>(s0, scenes, sc);
+            const float cut = S.cut_d2, h2 = S.h2;
+            float sum = 0.0f, comp = 0.0f;
+            if (tiled) {
+                int cnt = 0;
+                const float2 npx = make_float2(-p.x, -p.x), npy = make_float2(-p.y, -p.y);
+                const float2 npz = make_float2(-p.z, -p.z);
+#pragma unroll 1
+                for (int r = 0; r < G::kSegPerRow; ++r) {
+                    int a, b;
+                    seg_range<R, BLOCK>(T, lrow * G::kSegPerRow + r, cx, S.dim[0], start, a, b);
+#pragma unroll 2
+                    for (int j = a; j < b; j += 2) {
+                        const float2 d2 = pair_d2(st, j, npx, npy, npz);
+                        if (d2.x < cut) lst[BLOCK * cnt++] = d2.x;
+                        if (d2.y < cut) lst[BLOCK * cnt++] = d2.y;
+                        if (cnt > kNbCapDensity - 2) {
+                            for (int k = 0; k < cnt; ++k) {
+                                const float w = h2 - lst[BLOCK * k];
+                                kahan_add(sum, comp, w * w * w);
+                            }
+                            cnt = 0;
+                        }
+                    }
                 }
+                for (int k = 0; k < cnt; ++k) {
+                    const float w = h2 - lst[BLOCK * k];
+                    kahan_add(sum, comp, w * w * w);
+                }
+            } else {
+                const int gx = cell_coord(p.x, S.lo[0], S.inv_edge, S.dim[0]);
+                const int gy = cell_coord(p.y, S.lo[1], S.inv_edge, S.dim[1]);
+                const int gz = cell_coord(p.z, S.lo[2], S.inv_edge, S.dim[2]);
+                for_rows_global<R>(S, start, n, gx, gy, gz, [&](int a, int b) {
+                    for (int j = a; j < b; ++j) {
+                        const float4 o = __ldg(pos_s + j);
+                        float dx, dy, dz;
+                        const float d2 = canon_d2(p.x, p.y, p.z, o.x, o.y, o.z, dx, dy, dz);
+                        if (d2 < cut) {
+                            const float w = h2 - d2;
+                            kahan_add(sum, comp, w * w * w);
+                        }
+                    }
+                });
             }
-        });
-        flush();
-        const float rho = S.poly6c * sum;
-        const float pr = S.gas_k * (rho - S.rho0);
-        rhop[t] = make_float2(rho, pr < 0.0f ? 0.0f : pr);  // GLSL max(x, 0): NaN stays NaN
+            const float rho = S.poly6c * sum;
+            const float pr = S.gas_k * (rho - S.rho0);
+            rhop[t] = make_float2(rho, pr < 0.0f ? 0.0f : pr);  // GLSL max(x, 0): NaN stays NaN
+        }
+        if (!tiled && threadIdx.x == 0 && stats) atomicAdd(&stats[0], 1u);
+        __syncthreads();  // the next chunk reuses the tile
     }
 }
+
+struct ForceAcc {
+    float fpx = 0.f, fpy = 0.f, fpz = 0.f, fvx = 0.f, fvy = 0.f, fvz = 0.f;
+    // force_comp.glsl:59-60 for one neighbour j at offset (dx, dy, dz) = x_i - x_j.
+    __device__ __forceinline__ void add(float dx, float dy, float dz, float h, float pi, float4 v, float2 rj,
+                                        float4 vj) {
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        const float irho = __fdividef(1.0f, rj.x);
+        const float inv_r = rsqrtf(d2);
+        const float r = d2 > 0.0f ? d2 * inv_r : 0.0f;
+        const float hr = h - r;
+        const float s = d2 > 0.0f ? (pi + rj.y) * irho * hr * hr * inv_r : 0.0f;  // spiky gradient
+        fpx += s * dx; fpy += s * dy; fpz += s * dz;
+        const float c = irho * hr;                                                // Laplacian
+        fvx += c * (vj.x - v.x); fvy += c * (vj.y - v.y); fvz += c * (vj.z - v.z);
+    }
+};
 
 template <bool BATCHED, int R, int BLOCK>
 __global__ void __launch_bounds__(BLOCK) k_force_integrate(const float4* __restrict__ pos_s, const float4* __restrict__ vel_s,
@@ -134,74 +329,94 @@ __global__ void __launch_bounds__(BLOCK) k_force_integrate(const float4* __restr
                                                            SceneDev s0, const SceneDev* __restrict__ scenes, int nscene,
                                                            float4* __restrict__ pos_out, float4* __restrict__ vel_out,
                                                            float4* __restrict__ force_out, int* __restrict__ key_out,
-                                                           int* __restrict__ rank_out, int* __restrict__ count, int n) {
-    extern __shared__ int s_nb[];  // [kNbCap][BLOCK]
-    int* lst = s_nb + threadIdx.x;
-    for (int t = blockIdx.x * BLOCK + threadIdx.x; t < n; t += gridDim.x * BLOCK) {
-        const float4 p = pos_s[t];
-        const float4 v = vel_s[t];
-        const float2 rp = rhop[t];
-        int sc = 0;
-        if constexpr (BATCHED) sc = min(max(scene_of(p), 0), nscene - 1);
-        const SceneDev& S = scene_params<BATCHED>(s0, scenes, sc);
-        const float cut = S.cut_d2, h = S.h;
-        const int cx = cell_coord(p.x, S.lo[0], S.inv_edge, S.dim[0]);
-        const int cy = cell_coord(p.y, S.lo[1], S.inv_edge, S.dim[1]);
-        const int cz = cell_coord(p.z, S.lo[2], S.inv_edge, S.dim[2]);
-        float fpx = 0.f, fpy = 0.f, fpz = 0.f, fvx = 0.f, fvy = 0.f, fvz = 0.f;
-        int cnt = 0;
-        auto flush = [&]() {
-            for (int k = 0; k < cnt; ++k) {
-                const int j = lst[k * BLOCK];
-                const float4 o = __ldg(pos_s + j);
-                const float2 rj = __ldg(rhop + j);
-                const float4 vj = __ldg(vel_s + j);
-                const float dx = p.x - o.x, dy = p.y - o.y, dz = p.z - o.z;
-                const float d2 = dx * dx + dy * dy + dz * dz;
-                const float irho = __fdividef(1.0f, rj.x);
-                const float inv_r = rsqrtf(d2);
-                const float r = d2 > 0.0f ? d2 * inv_r : 0.0f;
-                const float hr = h - r;
-                const float s = d2 > 0.0f ? (rp.y + rj.y) * irho * hr * hr * inv_r : 0.0f;  // :59 spiky gradient
-                fpx += s * dx; fpy += s * dy; fpz += s * dz;
-                const float c = irho * hr;                                                // :60 Laplacian
-                fvx += c * (vj.x - v.x); fvy += c * (vj.y - v.y); fvz += c * (vj.z - v.z);
-            }
-            cnt = 0;
-        };
-        for_rows<R>(S, start, n, cx, cy, cz, [&](int a, int b) {
-#pragma unroll 4
-            for (int j = a; j < b; ++j) {
-                const float4 o = __ldg(pos_s + j);
-                float dx, dy, dz;
-                const float d2 = canon_d2_pk(p.x, p.y, p.z, o, dx, dy, dz);
-                if (d2 < cut && j != t) {  // force_comp.glsl:50-57
-                    lst[cnt * BLOCK] = j;
-                    if (++cnt == kNbCap) flush();
+                                                           int* __restrict__ rank_out, int* __restrict__ count, int n,
+                                                           uint32_t* __restrict__ stats) {
+    using G = TileGeom<R>;
+    constexpr int kCap = stage_cap<BLOCK>();
+    __shared__ TileShared<R, BLOCK> T;
+    extern __shared__ float4 dyn_f[];
+    float* base = reinterpret_cast<float*>(dyn_f);
+    const Staged st{base, base + kCap, base + 2 * kCap, reinterpret_cast<int*>(base + 3 * kCap)};
+    unsigned short* lst = reinterpret_cast<unsigned short*>(base + 4 * kCap) + threadIdx.x;  // [kNbCapForce][BLOCK]
+    for (int c0 = blockIdx.x * BLOCK; c0 < n; c0 += gridDim.x * BLOCK) {
+        float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+        int sc = 0, cx = 0, lrow = 0;
+        const bool tiled =
+            stage_chunk<BATCHED, R, BLOCK>(T, st, c0, n, pos_s, start, s0, scenes, nscene, p, sc, cx, lrow);
+        const int t = c0 + threadIdx.x;
+        if (t < n) {
+            if (!tiled) p = pos_s[t];
+            if constexpr (BATCHED) sc = min(max(scene_of(p), 0), nscene - 1);
+            const SceneDev& S = scene_params<BATCHED>(s0, scenes, sc);
+            const float4 v = vel_s[t];
+            const float2 rp = rhop[t];
+            const float cut = S.cut_d2, h = S.h;
+            ForceAcc acc;
+            if (tiled) {
+                // the target's own staged index: it lies in the centre segment of its row
+                const int cs = lrow * G::kSegPerRow + G::kSegPerRow / 2;
+                const int self = T.seg_off[cs] + (t - T.seg_gbeg[cs]);
+                int cnt = 0;
+                auto flush = [&]() {
+                    for (int k = 0; k < cnt; ++k) {
+                        const int j = lst[BLOCK * k];
+                        const int g = st.slot[j];
+                        acc.add(p.x - st.x[j], p.y - st.y[j], p.z - st.z[j], h, rp.y, v, __ldg(rhop + g),
+                                __ldg(vel_s + g));
+                    }
+                    cnt = 0;
+                };
+                const float2 npx = make_float2(-p.x, -p.x), npy = make_float2(-p.y, -p.y);
+                const float2 npz = make_float2(-p.z, -p.z);
+#pragma unroll 1
+                for (int r = 0; r < G::kSegPerRow; ++r) {
+                    int a, b;
+                    seg_range<R, BLOCK>(T, lrow * G::kSegPerRow + r, cx, S.dim[0], start, a, b);
+#pragma unroll 2
+                    for (int j = a; j < b; j += 2) {
+                        const float2 d2 = pair_d2(st, j, npx, npy, npz);
+                        if (d2.x < cut && j != self) lst[BLOCK * cnt++] = (unsigned short)j;  // :50-57
+                        if (d2.y < cut && j + 1 != self) lst[BLOCK * cnt++] = (unsigned short)(j + 1);
+                        if (cnt > kNbCapForce - 2) flush();
+                    }
                 }
+                flush();
+            } else {
+                const int gx = cell_coord(p.x, S.lo[0], S.inv_edge, S.dim[0]);
+                const int gy = cell_coord(p.y, S.lo[1], S.inv_edge, S.dim[1]);
+                const int gz = cell_coord(p.z, S.lo[2], S.inv_edge, S.dim[2]);
+                for_rows_global<R>(S, start, n, gx, gy, gz, [&](int a, int b) {
+                    for (int j = a; j < b; ++j) {
+                        const float4 o = __ldg(pos_s + j);
+                        float dx, dy, dz;
+                        const float d2 = canon_d2(p.x, p.y, p.z, o.x, o.y, o.z, dx, dy, dz);
+                        if (d2 < cut && j != t) acc.add(dx, dy, dz, h, rp.y, v, __ldg(rhop + j), __ldg(vel_s + j));
+                    }
+                });
             }
-        });
-        flush();
-        // :63-66 F = f_p + mu*f_v + rho_i*G (constants folded into pres_c, visc_c)
-        const float Fx = S.pres_c * fpx + S.visc_c * fvx + rp.x * S.g[0];
-        const float Fy = S.pres_c * fpy + S.visc_c * fvy + rp.x * S.g[1];
-        const float Fz = S.pres_c * fpz + S.visc_c * fvz + rp.x * S.g[2];
-        // integrate_comp.glsl:41-77
-        const float ir = 1.0f / rp.x;
-        float nv[3] = {v.x + S.dt * (Fx * ir), v.y + S.dt * (Fy * ir), v.z + S.dt * (Fz * ir)};
-        float np[3] = {p.x + S.dt * nv[0], p.y + S.dt * nv[1], p.z + S.dt * nv[2]};
+            // :63-66 F = f_p + mu*f_v + rho_i*G (constants folded into pres_c, visc_c)
+            const float Fx = S.pres_c * acc.fpx + S.visc_c * acc.fvx + rp.x * S.g[0];
+            const float Fy = S.pres_c * acc.fpy + S.visc_c * acc.fvy + rp.x * S.g[1];
+            const float Fz = S.pres_c * acc.fpz + S.visc_c * acc.fvz + rp.x * S.g[2];
+            // integrate_comp.glsl:41-77
+            const float ir = 1.0f / rp.x;
+            float nv[3] = {v.x + S.dt * (Fx * ir), v.y + S.dt * (Fy * ir), v.z + S.dt * (Fz * ir)};
+            float np[3] = {p.x + S.dt * nv[0], p.y + S.dt * nv[1], p.z + S.dt * nv[2]};
 #pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            if (np[a] < S.lo[a]) { np[a] = S.lo[a]; nv[a] *= -S.damp; }
-            else if (np[a] > S.up[a]) { np[a] = S.up[a]; nv[a] *= -S.damp; }
+            for (int a = 0; a < 3; ++a) {
+                if (np[a] < S.lo[a]) { np[a] = S.lo[a]; nv[a] *= -S.damp; }
+                else if (np[a] > S.up[a]) { np[a] = S.up[a]; nv[a] *= -S.damp; }
+            }
+            pos_out[t] = make_float4(np[0], np[1], np[2], p.w);
+            vel_out[t] = make_float4(nv[0], nv[1], nv[2], v.w);
+            if (force_out) force_out[t] = make_float4(Fx, Fy, Fz, 0.0f);
+            // Hash of the new position: the next step's sort starts from here.
+            const int c = cell_key(S, np[0], np[1], np[2]);
+            key_out[t] = c;
+            rank_out[t] = atomicAdd(&count[c], 1);
         }
-        pos_out[t] = make_float4(np[0], np[1], np[2], p.w);
-        vel_out[t] = make_float4(nv[0], nv[1], nv[2], v.w);
-        if (force_out) force_out[t] = make_float4(Fx, Fy, Fz, 0.0f);
-        // Hash of the new position: the next step's sort starts from here.
-        const int c = cell_key(S, np[0], np[1], np[2]);
-        key_out[t] = c;
-        rank_out[t] = atomicAdd(&count[c], 1);
+        if (!tiled && threadIdx.x == 0 && stats) atomicAdd(&stats[1], 1u);
+        __syncthreads();  // the next chunk reuses the tile
     }
 }
 
@@ -215,29 +430,29 @@ int grid_size(K kernel, int block, size_t smem, int n) {
     return (int)(need < cap ? (need < 1 ? 1 : need) : cap);
 }
 
-template <int BLOCK>
-constexpr size_t list_bytes() { return (size_t)kNbCap * BLOCK * 4; }
-
 template <bool B, int R, int BLOCK>
 void density_impl(const Buffers& b, const SceneDev& s0, cudaStream_t st) {
     auto k = k_density<B, R, BLOCK>;
-    const size_t sm = list_bytes<BLOCK>();
-    k<<<grid_size(k, BLOCK, sm, b.n), BLOCK, sm, st>>>(b.pos_s, b.start, s0, b.scenes, b.nscene, b.rhop, b.n);
+    constexpr size_t sm = density_smem<BLOCK>();
+    k<<<grid_size(k, BLOCK, sm, b.n), BLOCK, sm, st>>>(b.pos_s, b.start, s0, b.scenes, b.nscene, b.rhop, b.n,
+                                                       b.tile_stats);
 }
 
 template <bool B, int R, int BLOCK>
 void force_impl(const Buffers& b, const SceneDev& s0, float4* force_out, cudaStream_t st) {
     auto k = k_force_integrate<B, R, BLOCK>;
-    const size_t sm = list_bytes<BLOCK>();
+    constexpr size_t sm = force_smem<BLOCK>();
     k<<<grid_size(k, BLOCK, sm, b.n), BLOCK, sm, st>>>(b.pos_s, b.vel_s, b.rhop, b.start, s0, b.scenes, b.nscene,
-                                                       b.pos, b.vel, force_out, b.key, b.rank, b.count, b.n);
+                                                       b.pos, b.vel, force_out, b.key, b.rank, b.count, b.n,
+                                                       b.tile_stats);
 }
 
-template <bool B, int R>
+template <bool B, int R, int BLOCK>
 void set_attrs() {
-    cudaFuncSetAttribute(k_density<B, R, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)list_bytes<512>());
-    cudaFuncSetAttribute(k_force_integrate<B, R, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)list_bytes<512>());
+    cudaFuncSetAttribute(k_density<B, R, BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)density_smem<BLOCK>());
+    cudaFuncSetAttribute(k_force_integrate<B, R, BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)force_smem<BLOCK>());
 }
 
 // Calls f(integral_constant<R>, integral_constant<BLOCK>) for the runtime (block, stencil).
@@ -245,7 +460,6 @@ template <class F>
 void dispatch(int block, int stencil, F f) {
     auto by_block = [&](auto rc) {
         if (block == 128) f(rc, std::integral_constant<int, 128>{});
-        else if (block == 512) f(rc, std::integral_constant<int, 512>{});
         else f(rc, std::integral_constant<int, 256>{});
     };
     if (stencil == 2) by_block(std::integral_constant<int, 2>{});
@@ -255,10 +469,14 @@ void dispatch(int block, int stencil, F f) {
 }  // namespace
 
 void init_step_kernels() {
-    set_attrs<false, 1>();
-    set_attrs<false, 2>();
-    set_attrs<true, 1>();
-    set_attrs<true, 2>();
+    set_attrs<false, 1, 128>();
+    set_attrs<false, 1, 256>();
+    set_attrs<false, 2, 128>();
+    set_attrs<false, 2, 256>();
+    set_attrs<true, 1, 128>();
+    set_attrs<true, 1, 256>();
+    set_attrs<true, 2, 128>();
+    set_attrs<true, 2, 256>();
 }
 
 void launch_density(const Buffers& b, const SceneDev& s0, bool batched, const LaunchCfg& c, cudaStream_t st) {

@@ -95,6 +95,7 @@ _SIGS = {
     "sph_set_launch": (C.c_int32, [_P, C.c_int32, C.c_int32]),
     "sph_get_launch": (C.c_int32, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "sph_autotune": (C.c_int32, [_P, C.c_int32, C.POINTER(C.c_float)]),
+    "sph_tile_stats": (C.c_int32, [_P, C.POINTER(C.c_uint32)]),
     "sph_scene_reference_grid": (C.c_int32, [_P, C.c_uint32, C.c_float]),
     "sph_scene_fill": (C.c_int32, [_P, C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_float,
                                    C.c_float, C.c_uint64]),
@@ -271,6 +272,12 @@ class Sim:
         a, b = C.c_int32(), C.c_int32()
         _check(lib.sph_get_launch(self._ctx, C.byref(a), C.byref(b)), self._ctx)
         return a.value, b.value
+
+    def tile_stats(self) -> tuple[int, int]:
+        """(density, force) chunks that fell back to the global-memory path since creation."""
+        a = (C.c_uint32 * 2)()
+        _check(lib.sph_tile_stats(self._ctx, a), self._ctx)
+        return a[0], a[1]
 
     def autotune(self, trial_steps: int = 5) -> float:
         ms = C.c_float()

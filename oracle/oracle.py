@@ -47,6 +47,8 @@ def lib() -> C.CDLL:
         L.oracle_step_f64.argtypes = [_P, _I64, _P, _P, C.c_int, C.c_int, _P, _P, _P, _P, _P, _P, _P]
         L.oracle_force_f64.restype = C.c_int
         L.oracle_force_f64.argtypes = [_P, _I64, _P, _P, _P, _P, C.c_int, C.c_int, _P, _P, _P, _P, _P]
+        L.oracle_force_cond_f64.restype = C.c_int
+        L.oracle_force_cond_f64.argtypes = [_P, _I64, _P, _P, _P, _P, C.c_int, C.c_int, _P]
         L.oracle_run_f64.restype = C.c_int
         L.oracle_run_f64.argtypes = [_P, _I64, _P, _P, _P, _P, C.c_int, C.c_int, C.c_int]
         L.oracle_step_f32_aos.restype = C.c_int
@@ -119,6 +121,11 @@ def force_f64(params, particles: np.ndarray, rho, pres, backend: str = "grid", n
                                 out["fscale"].ctypes.data, out["pos"].ctypes.data, out["vel"].ctypes.data,
                                 out["margin"].ctypes.data)
     assert rc == 0
+    cond = np.zeros(n)
+    rc = lib().oracle_force_cond_f64(_pp(params), n, pos.ctypes.data, vel.ctypes.data, rho.ctypes.data,
+                                     pres.ctypes.data, BACKENDS[backend], nthreads, cond.ctypes.data)
+    assert rc == 0
+    out["fcond"] = cond
     return out
 
 

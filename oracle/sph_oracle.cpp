@@ -275,6 +275,46 @@ int oracle_force_f64(const sph_params* P, int64_t n, const double* pos, const do
                          const_cast<double*>(pres), force, fscale, pos_out, vel_out, wall_margin, 1);
 }
 
+// Conditioning of the force pass: fcond[i] = sum_j |f_ij(p)| * 2r/(h-r) + mu*|f_ij(v)| * r/(h-r),
+// the first-order change of F_i under a relative perturbation of every pair distance r
+// (d ln (h-r)^2 / d ln r = -2r/(h-r); d ln (h-r) / d ln r = -r/(h-r)). Any FP32 evaluation of
+// force_comp.glsl:59-60 from FP32 positions (the shader itself included) rounds r by a few
+// 2^-24, so its force error is bounded by a few 2^-24 * fcond on top of the usual scale.
+int oracle_force_cond_f64(const sph_params* P, int64_t n, const double* pos, const double* vel,
+                          const double* rho, const double* pres, int backend, int nthreads, double* fcond) {
+    if (!P || n < 0 || !pos || !vel || !rho || !pres || !fcond) return -1;
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+    const float hf = P->smoothing_coeff * P->particle_radius;
+    const double h = hf, m = P->mass, PI = kPiF, mu = P->visc;
+    const double lap = 45.0 / (PI * std::pow(h, 6));
+    std::vector<float> pf(3 * n);
+    for (int64_t t = 0; t < 3 * n; ++t) pf[t] = (float)pos[t];
+    auto getpos = [&](int64_t i, float* p) { p[0] = pf[3 * i]; p[1] = pf[3 * i + 1]; p[2] = pf[3 * i + 2]; };
+    Grid grid;
+    const Grid* g = nullptr;
+    if (backend == 1) { build_grid(grid, P, hf, n, getpos); g = &grid; }
+#pragma omp parallel for schedule(dynamic, 256) num_threads(nthreads)
+    for (int64_t i = 0; i < n; ++i) {
+        double cond = 0.0;
+        for_candidates(g, n, i, getpos, [&](int64_t j) {
+            if (j == i) return;
+            float d2f = canon_d2(pf[3*i], pf[3*i+1], pf[3*i+2], pf[3*j], pf[3*j+1], pf[3*j+2]);
+            if (!canon_pred(d2f, hf)) return;
+            double d[3] = {pos[3*i] - pos[3*j], pos[3*i+1] - pos[3*j+1], pos[3*i+2] - pos[3*j+2]};
+            double r = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+            double hr = h - r;
+            if (!(hr > 0.0)) hr = 1e-300;
+            double fp = std::fabs(m * (pres[i] + pres[j]) / (2.0 * rho[j]) * lap * hr * hr);
+            double vn = 0.0;
+            for (int a = 0; a < 3; ++a) { double dv = vel[3*j+a] - vel[3*i+a]; vn += dv * dv; }
+            double fv = mu * std::fabs(m / rho[j] * lap * hr) * std::sqrt(vn);
+            cond += fp * 2.0 * r / hr + fv * r / hr;
+        });
+        fcond[i] = cond;
+    }
+    return 0;
+}
+
 // n_steps FP64 steps in place (state in double). The CPU baseline.
 int oracle_run_f64(const sph_params* P, int64_t n, double* pos, double* vel, double* rho,
                    double* pres, int n_steps, int backend, int nthreads) {
