@@ -227,6 +227,7 @@ def run_ours(args) -> None:
     local_s = sum(step_ms) / 1e3
     total_s = max_over_ranks(local_s, world)
     diag = sim.reduce()
+    fallback = sim.tile_stats()
 
     # Per-pass device times over the same trajectory (events between passes, eager launches).
     sim.upload(sc.particles)
@@ -283,7 +284,9 @@ def run_ours(args) -> None:
                                "against the x=0 wall of a 5.12x1.28x1.28 box, g=-9.81, dt=1e-4, plain SPH",
                    "particles": n, "timed_steps": [args.warmup, args.warmup + args.steps],
                    "l2": "flushed between steps (256 MiB write outside the timed events)",
-                   "launch": {"threads_per_block": blk, "stencil": sten}, "parallelism": f"replicas x{world}"},
+                   "launch": {"threads_per_block": blk, "stencil": sten}, "parallelism": f"replicas x{world}",
+                   "global_path_chunks": {"density": fallback[0], "force": fallback[1],
+                                          "of": (args.warmup + args.steps) * ((n + blk - 1) // blk)}},
         "roofline": {"bound": "hbm", "kernel": "force_integrate", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic, "peak_source": f"{src} hbm_gbs",
                      "bytes_per_particle": B_ALG["force_integrate"],

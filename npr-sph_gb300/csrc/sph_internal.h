@@ -75,13 +75,13 @@ struct Buffers {
 
 // Launch shape chosen by the autotuner.
 struct LaunchCfg {
-    int block = 256;     // threads per CTA of the pair kernels
+    int block = 128;     // threads per CTA of the pair kernels (particles per shared-memory tile)
     int stencil = 1;     // cell edge = h/stencil, (2*stencil+1)^3 cells visited
     int grid_cap = 0;    // persistent grid size (CTAs); 0 = one thread per particle
 };
 
 constexpr int kScanThreads = 256;
-constexpr int kScanItems = 16;
+constexpr int kScanItems = 32;  // 8192 cells per tile: a 1M-cell grid is 128 tiles
 constexpr int kScanTile = kScanThreads * kScanItems;
 
 // ---- launchers (sph_grid.cu) ----

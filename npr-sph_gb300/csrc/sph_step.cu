@@ -22,13 +22,14 @@
 // candidates from cells two cells away (never within h: cell edge >= h/R with
 // margin) or the sentinel.
 //
-// Passing candidates are appended to a per-thread list in shared memory
-// (density: d2; force: the staged index), then processed in a second loop in
-// which all lanes are busy: with ~15% of candidates inside r < h, testing and
-// interacting in one loop would run the interaction code for a minority of
-// lanes almost every iteration. Lists hold kNbCap* entries; longer
-// neighbourhoods are processed in chunks, in candidate order, so results are
-// deterministic either way.
+// Density accumulates every candidate branch-free (its weight is zero outside
+// r < h). Force appends passing candidates to a per-thread list in shared
+// memory (the staged index) and processes the list in a second loop in which
+// all lanes are busy: with ~15% of candidates inside r < h, testing and
+// interacting in one loop would run the ~35-instruction interaction for a
+// minority of lanes almost every iteration. The list holds kNbCapForce
+// entries; a longer neighbourhood is processed in chunks, in candidate order,
+// so results are deterministic either way.
 //
 // A chunk with more distinct rows or more staged candidates than the tile
 // holds (heavy pile-ups) takes a global-memory path with the same arithmetic.
@@ -47,9 +48,11 @@ namespace sphgb {
 namespace {
 
 // BLOCK threads per CTA = target particles per chunk (128 or 256, autotuned).
-template <int BLOCK> constexpr int stage_cap() { return 11 * BLOCK; }  // staged candidates per chunk
-constexpr int kNbCapDensity = 24;       // density list entries per thread (d2, float)
-constexpr int kNbCapForce = 40;         // force list entries per thread (staged index, u16)
+// A chunk stages about (2R+1)^2 * (BLOCK + 2R * cell occupancy * rows in the chunk)
+// candidates: ~9.7 * BLOCK for a lattice at 0.5h spacing; 16 * BLOCK leaves room for
+// compression and for chunks that straddle rows.
+template <int BLOCK> constexpr int stage_cap() { return 16 * BLOCK; }
+constexpr int kNbCapForce = 64;         // force list entries per thread (staged index, u16)
 constexpr float kSentinel = 1e30f;      // staged padding: its distance to any particle is +inf
 
 template <int R>
@@ -227,7 +230,7 @@ __device__ __forceinline__ void kahan_add(float& sum, float& comp, float x) {
 }
 
 template <int BLOCK>
-constexpr size_t density_smem() { return (size_t)3 * stage_cap<BLOCK>() * 4 + (size_t)kNbCapDensity * BLOCK * 4; }
+constexpr size_t density_smem() { return (size_t)3 * stage_cap<BLOCK>() * 4; }
 template <int BLOCK>
 constexpr size_t force_smem() { return (size_t)4 * stage_cap<BLOCK>() * 4 + (size_t)kNbCapForce * BLOCK * 2; }
 static_assert(stage_cap<256>() < 65536, "staged indices are 16-bit");
@@ -242,7 +245,6 @@ __global__ void __launch_bounds__(BLOCK) k_density(const float4* __restrict__ po
     extern __shared__ float4 dyn_d[];
     float* base = reinterpret_cast<float*>(dyn_d);
     const Staged st{base, base + kCap, base + 2 * kCap, nullptr};
-    float* lst = base + 3 * kCap + threadIdx.x;  // [kNbCapDensity][BLOCK]
     for (int c0 = blockIdx.x * BLOCK; c0 < n; c0 += gridDim.x * BLOCK) {
         float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
         int sc = 0, cx = 0, lrow = 0;
@@ -256,9 +258,14 @@ __global__ void __launch_bounds__(BLOCK) k_density(const float4* __restrict__ po
             const float cut = S.cut_d2, h2 = S.h2;
             float sum = 0.0f, comp = 0.0f;
             if (tiled) {
-                int cnt = 0;
+                // Branch-free: every candidate adds max(h^2 - d2, 0)^3, two per step in
+                // packed lanes, each lane its own Kahan sum. The weight differs from the
+                // strict-predicate one (d2 < cut) only for d2 within an ulp of h^2, where it
+                // is below 1e-30 * h^6: invisible in an FP32 sum of terms of order h^6.
                 const float2 npx = make_float2(-p.x, -p.x), npy = make_float2(-p.y, -p.y);
                 const float2 npz = make_float2(-p.z, -p.z);
+                const float2 h2v = make_float2(h2, h2);
+                float2 s2 = make_float2(0.f, 0.f), c2 = make_float2(0.f, 0.f);
 #pragma unroll 1
                 for (int r = 0; r < G::kSegPerRow; ++r) {
                     int a, b;
@@ -266,21 +273,22 @@ __global__ void __launch_bounds__(BLOCK) k_density(const float4* __restrict__ po
 #pragma unroll 2
                     for (int j = a; j < b; j += 2) {
                         const float2 d2 = pair_d2(st, j, npx, npy, npz);
-                        if (d2.x < cut) lst[BLOCK * cnt++] = d2.x;
-                        if (d2.y < cut) lst[BLOCK * cnt++] = d2.y;
-                        if (cnt > kNbCapDensity - 2) {
-                            for (int k = 0; k < cnt; ++k) {
-                                const float w = h2 - lst[BLOCK * k];
-                                kahan_add(sum, comp, w * w * w);
-                            }
-                            cnt = 0;
-                        }
+                        float2 w = __fadd2_rn(h2v, make_float2(-d2.x, -d2.y));
+                        w.x = fmaxf(w.x, 0.0f);
+                        w.y = fmaxf(w.y, 0.0f);
+                        const float2 term = __fmul2_rn(__fmul2_rn(w, w), w);
+                        const float2 y = __fadd2_rn(term, make_float2(-c2.x, -c2.y));  // Kahan, per lane
+                        const float2 tt = __fadd2_rn(s2, y);
+                        const float2 lost = __fadd2_rn(tt, make_float2(-s2.x, -s2.y));
+                        c2 = __fadd2_rn(lost, make_float2(-y.x, -y.y));
+                        s2 = tt;
                     }
                 }
-                for (int k = 0; k < cnt; ++k) {
-                    const float w = h2 - lst[BLOCK * k];
-                    kahan_add(sum, comp, w * w * w);
-                }
+                // combine the two lanes: (s.x - c.x) + (s.y - c.y) with a compensated add
+                kahan_add(sum, comp, s2.x);
+                kahan_add(sum, comp, -c2.x);
+                kahan_add(sum, comp, s2.y);
+                kahan_add(sum, comp, -c2.y);
             } else {
                 const int gx = cell_coord(p.x, S.lo[0], S.inv_edge, S.dim[0]);
                 const int gy = cell_coord(p.y, S.lo[1], S.inv_edge, S.dim[1]);
