@@ -200,6 +200,34 @@ sph_status sph_autotune(sph_ctx* ctx, int32_t trial_steps, float* best_ms_per_st
  * memory instead (heavy pile-ups). Synchronous. */
 sph_status sph_tile_stats(sph_ctx* ctx, uint32_t out[2]);
 
+/* ---- diagnostics without allocation -------------------------------------
+ * No counterpart in the reference.
+ *
+ * sph_reduce_aos_noalloc: the FP64 sums behind sph_diag for n particle
+ * records in the CALLER's device buffer, written to the caller's device
+ * buffer dev_sums[12]:
+ *   0-2 sum m v, 3 sum 1/2 m |v|^2, 4 sum -m G.x, 5 sum rho (extras[0]),
+ *   6 min rho, 7 max rho, 8 sum |rho - rho0| / rho0, 9 non-finite records,
+ *   10 finite records, 11 sum rho^2
+ * (records with a NaN/Inf in pos, vel or rho are counted in 9 and left out of
+ * every other field). Uses mass, resting_rho and gravity of *p.
+ *
+ * It exists for callers that cannot allocate device memory at the point they
+ * need it: a render or game loop that reserves its GPU memory up front and
+ * must not allocate per frame, a plugin host that owns every buffer, code that
+ * records its work into a CUDA graph (where cudaMalloc would break the
+ * capture). It calls no cudaMalloc/cudaFree: its scratch is a fixed 96 KiB
+ * array in device memory, which every GPU that loads this library holds until
+ * the process exits.
+ *   - n <= 4,194,304 records; larger n returns SPH_ERR_CAPACITY.
+ *   - Asynchronous on `stream` (cudaStream_t, NULL = legacy default stream).
+ *   - The first call on each device looks up the scratch array's device
+ *     address; make that first call before any stream capture.
+ *   - All calls share the scratch: calls that overlap on the GPU (different
+ *     streams without ordering between them) race and give wrong sums. */
+sph_status sph_reduce_aos_noalloc(const sph_particle* dev_particles, uint32_t n, const sph_params* p,
+                                  double* dev_sums, void* stream);
+
 /* ---- scene generators (host only; no GPU needed) ----------------------- */
 
 /* The reference's make_grid()+init_particles() (Main.cpp:488-539): 10x100x10

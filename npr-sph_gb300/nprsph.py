@@ -96,6 +96,7 @@ _SIGS = {
     "sph_get_launch": (C.c_int32, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "sph_autotune": (C.c_int32, [_P, C.c_int32, C.POINTER(C.c_float)]),
     "sph_tile_stats": (C.c_int32, [_P, C.POINTER(C.c_uint32)]),
+    "sph_reduce_aos_noalloc": (C.c_int32, [_P, C.c_uint32, C.POINTER(Params), _P, _P]),
     "sph_scene_reference_grid": (C.c_int32, [_P, C.c_uint32, C.c_float]),
     "sph_scene_fill": (C.c_int32, [_P, C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_float,
                                    C.c_float, C.c_uint64]),
