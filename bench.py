@@ -186,6 +186,51 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def timed_steps(sim, stream, steps: int, warmup: int) -> float:
+    """Seconds of `steps` sph_step calls after `warmup`, by CUDA events on the simulation stream."""
+    import torch
+
+    sim.step(warmup)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(stream)
+    sim.step(steps)
+    b.record(stream)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / 1e3
+
+
+def extra_workloads(args, stream) -> dict:
+    """The other two plain configurations, measured the same way (no L2 flush: the batched
+    state, ~4.7M particles, is larger than L2; the 10k scene is launch-bound)."""
+    import nprsph as S
+
+    out = {}
+    plist, counts, parts = S.batched_scenes(256, seed=3)
+    n = int(counts.sum())
+    with S.Sim(plist, counts=counts, stream=stream.cuda_stream) as sim:
+        sim.upload(parts)
+        ms = sim.autotune(3) if args.autotune else None
+        sim.upload(parts)
+        sec = timed_steps(sim, stream, args.extra_steps, 5)
+        fb = sim.tile_stats()
+        out["batched_256_scenes"] = {
+            "value": n * args.extra_steps / sec, "unit": UNIT, "particles": n, "scenes": 256, "steps": args.extra_steps,
+            "ms_per_step": 1e3 * sec / args.extra_steps, "launch": list(sim.get_launch()),
+            "global_path_chunks": list(fb), "autotune_ms": ms,
+            "workload": "256 boxes, counts log-uniform in [2000, 65536], k ~ U[500,3000], mu ~ U[0.1,2], lattice "
+                        "or sphere drop; one launch per pass over all scenes, replayed from a CUDA graph"}
+    sc = S.reference_scene_10k(seed=1)
+    with S.Sim(sc.params, n_max=len(sc.particles), stream=stream.cuda_stream) as sim:
+        sim.upload(sc.particles)
+        sec = timed_steps(sim, stream, args.extra_steps, 5)
+        out["reference_scene_10k"] = {
+            "value": len(sc.particles) * args.extra_steps / sec, "unit": UNIT, "particles": len(sc.particles),
+            "steps": args.extra_steps, "ms_per_step": 1e3 * sec / args.extra_steps,
+            "workload": "10,000 particles, 0.5h lattice in the lower-corner quarter of the reference box"}
+    return out
+
+
 def run_ours(args) -> None:
     import torch
     import nprsph as S
@@ -265,6 +310,7 @@ def run_ours(args) -> None:
 
     if rank != 0:
         return
+    extra = extra_workloads(args, stream) if args.extra_steps > 0 else {}
     peaks, src = measured_peaks()
     hbm = float(peaks["hbm_gbs"])
     value = world * n * args.steps / total_s
@@ -300,6 +346,7 @@ def run_ours(args) -> None:
         "gpu_launches": KERNELS_PER_STEP * args.steps,
         "clocks": clk.summary(),
         "final_state": {"mean_rho": diag.mean_rho, "nonfinite": int(diag.nonfinite), "step": int(diag.step)},
+        "other_configs": extra,
     }
     print(json.dumps(line), flush=True)
     if world > 1:
@@ -315,7 +362,10 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample length (0: skip)")
-    ap.add_argument("--autotune", action="store_true", help="pick the launch shape by timing before the run")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="keep the default launch shape instead of timing the candidates first")
+    ap.add_argument("--extra-steps", type=int, default=100,
+                    help="steps of the batched-scenes and 10k reference-scene measurements (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

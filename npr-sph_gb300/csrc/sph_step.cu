@@ -51,7 +51,8 @@ namespace {
 // A chunk stages about (2R+1)^2 * (BLOCK + 2R * cell occupancy * rows in the chunk)
 // candidates: ~9.7 * BLOCK for a lattice at 0.5h spacing; 16 * BLOCK leaves room for
 // compression and for chunks that straddle rows.
-template <int BLOCK> constexpr int stage_cap() { return 16 * BLOCK; }
+// With R = 2 (cells of h/2, 25 neighbour rows) a chunk stages ~26 * BLOCK.
+template <int R, int BLOCK> constexpr int stage_cap() { return (R == 1 ? 16 : 30) * BLOCK; }
 constexpr int kNbCapForce = 64;         // force list entries per thread (staged index, u16)
 constexpr float kSentinel = 1e30f;      // staged padding: its distance to any particle is +inf
 
@@ -166,7 +167,7 @@ __device__ bool stage_chunk(TileShared<R, BLOCK>& T, const Staged& st, int c0, i
         if (lane == 31) T.seg_off[nseg] = incl;
     }
     __syncthreads();
-    if (T.seg_off[nseg] > stage_cap<BLOCK>()) return false;  // uniform
+    if (T.seg_off[nseg] > stage_cap<R, BLOCK>()) return false;  // uniform
     for (int s = warp; s < nseg; s += kWarps) {
         const int gbeg = T.seg_gbeg[s], len = T.seg_len[s], off = T.seg_off[s];
         const int plen = (len + 1) & ~1;
@@ -229,18 +230,18 @@ __device__ __forceinline__ void kahan_add(float& sum, float& comp, float x) {
     sum = t;
 }
 
-template <int BLOCK>
-constexpr size_t density_smem() { return (size_t)3 * stage_cap<BLOCK>() * 4; }
-template <int BLOCK>
-constexpr size_t force_smem() { return (size_t)4 * stage_cap<BLOCK>() * 4 + (size_t)kNbCapForce * BLOCK * 2; }
-static_assert(stage_cap<256>() < 65536, "staged indices are 16-bit");
+template <int R, int BLOCK>
+constexpr size_t density_smem() { return (size_t)3 * stage_cap<R, BLOCK>() * 4; }
+template <int R, int BLOCK>
+constexpr size_t force_smem() { return (size_t)4 * stage_cap<R, BLOCK>() * 4 + (size_t)kNbCapForce * BLOCK * 2; }
+static_assert(stage_cap<2, 256>() < 65536, "staged indices are 16-bit");
 
 template <bool BATCHED, int R, int BLOCK>
 __global__ void __launch_bounds__(BLOCK) k_density(const float4* __restrict__ pos_s, const int* __restrict__ start,
                                                    SceneDev s0, const SceneDev* __restrict__ scenes, int nscene,
                                                    float2* __restrict__ rhop, int n, uint32_t* __restrict__ stats) {
     using G = TileGeom<R>;
-    constexpr int kCap = stage_cap<BLOCK>();
+    constexpr int kCap = stage_cap<R, BLOCK>();
     __shared__ TileShared<R, BLOCK> T;
     extern __shared__ float4 dyn_d[];
     float* base = reinterpret_cast<float*>(dyn_d);
@@ -315,8 +316,10 @@ __global__ void __launch_bounds__(BLOCK) k_density(const float4* __restrict__ po
 }
 
 struct ForceAcc {
-    float fpx = 0.f, fpy = 0.f, fpz = 0.f, fvx = 0.f, fvy = 0.f, fvz = 0.f;
-    // force_comp.glsl:59-60 for one neighbour j at offset (dx, dy, dz) = x_i - x_j.
+    float2 fp_xy = make_float2(0.f, 0.f), fv_xy = make_float2(0.f, 0.f);
+    float fpz = 0.f, fvz = 0.f;
+    // force_comp.glsl:59-60 for one neighbour j at offset (dx, dy, dz) = x_i - x_j; the x/y
+    // lanes of the two vector sums run as packed FP32x2 operations.
     __device__ __forceinline__ void add(float dx, float dy, float dz, float h, float pi, float4 v, float2 rj,
                                         float4 vj) {
         const float d2 = dx * dx + dy * dy + dz * dz;
@@ -325,9 +328,12 @@ struct ForceAcc {
         const float r = d2 > 0.0f ? d2 * inv_r : 0.0f;
         const float hr = h - r;
         const float s = d2 > 0.0f ? (pi + rj.y) * irho * hr * hr * inv_r : 0.0f;  // spiky gradient
-        fpx += s * dx; fpy += s * dy; fpz += s * dz;
+        fp_xy = __ffma2_rn(make_float2(s, s), make_float2(dx, dy), fp_xy);
+        fpz = fmaf(s, dz, fpz);
         const float c = irho * hr;                                                // Laplacian
-        fvx += c * (vj.x - v.x); fvy += c * (vj.y - v.y); fvz += c * (vj.z - v.z);
+        const float2 dv = __fadd2_rn(make_float2(vj.x, vj.y), make_float2(-v.x, -v.y));
+        fv_xy = __ffma2_rn(make_float2(c, c), dv, fv_xy);
+        fvz = fmaf(c, vj.z - v.z, fvz);
     }
 };
 
@@ -340,7 +346,7 @@ __global__ void __launch_bounds__(BLOCK) k_force_integrate(const float4* __restr
                                                            int* __restrict__ rank_out, int* __restrict__ count, int n,
                                                            uint32_t* __restrict__ stats) {
     using G = TileGeom<R>;
-    constexpr int kCap = stage_cap<BLOCK>();
+    constexpr int kCap = stage_cap<R, BLOCK>();
     __shared__ TileShared<R, BLOCK> T;
     extern __shared__ float4 dyn_f[];
     float* base = reinterpret_cast<float*>(dyn_f);
@@ -361,9 +367,9 @@ __global__ void __launch_bounds__(BLOCK) k_force_integrate(const float4* __restr
             const float cut = S.cut_d2, h = S.h;
             ForceAcc acc;
             if (tiled) {
-                // the target's own staged index: it lies in the centre segment of its row
-                const int cs = lrow * G::kSegPerRow + G::kSegPerRow / 2;
-                const int self = T.seg_off[cs] + (t - T.seg_gbeg[cs]);
+                // The list keeps the particle itself too (force_comp.glsl:50-53 skips j == i):
+                // its offset and relative velocity are exactly zero, so its pressure term is
+                // skipped (d2 == 0) and its viscosity term adds exact zeros.
                 int cnt = 0;
                 auto flush = [&]() {
                     for (int k = 0; k < cnt; ++k) {
@@ -383,8 +389,8 @@ __global__ void __launch_bounds__(BLOCK) k_force_integrate(const float4* __restr
 #pragma unroll 2
                     for (int j = a; j < b; j += 2) {
                         const float2 d2 = pair_d2(st, j, npx, npy, npz);
-                        if (d2.x < cut && j != self) lst[BLOCK * cnt++] = (unsigned short)j;  // :50-57
-                        if (d2.y < cut && j + 1 != self) lst[BLOCK * cnt++] = (unsigned short)(j + 1);
+                        if (d2.x < cut) lst[BLOCK * cnt++] = (unsigned short)j;  // :57
+                        if (d2.y < cut) lst[BLOCK * cnt++] = (unsigned short)(j + 1);
                         if (cnt > kNbCapForce - 2) flush();
                     }
                 }
@@ -403,8 +409,8 @@ __global__ void __launch_bounds__(BLOCK) k_force_integrate(const float4* __restr
                 });
             }
             // :63-66 F = f_p + mu*f_v + rho_i*G (constants folded into pres_c, visc_c)
-            const float Fx = S.pres_c * acc.fpx + S.visc_c * acc.fvx + rp.x * S.g[0];
-            const float Fy = S.pres_c * acc.fpy + S.visc_c * acc.fvy + rp.x * S.g[1];
+            const float Fx = S.pres_c * acc.fp_xy.x + S.visc_c * acc.fv_xy.x + rp.x * S.g[0];
+            const float Fy = S.pres_c * acc.fp_xy.y + S.visc_c * acc.fv_xy.y + rp.x * S.g[1];
             const float Fz = S.pres_c * acc.fpz + S.visc_c * acc.fvz + rp.x * S.g[2];
             // integrate_comp.glsl:41-77
             const float ir = 1.0f / rp.x;
@@ -441,7 +447,7 @@ int grid_size(K kernel, int block, size_t smem, int n) {
 template <bool B, int R, int BLOCK>
 void density_impl(const Buffers& b, const SceneDev& s0, cudaStream_t st) {
     auto k = k_density<B, R, BLOCK>;
-    constexpr size_t sm = density_smem<BLOCK>();
+    constexpr size_t sm = density_smem<R, BLOCK>();
     k<<<grid_size(k, BLOCK, sm, b.n), BLOCK, sm, st>>>(b.pos_s, b.start, s0, b.scenes, b.nscene, b.rhop, b.n,
                                                        b.tile_stats);
 }
@@ -449,7 +455,7 @@ void density_impl(const Buffers& b, const SceneDev& s0, cudaStream_t st) {
 template <bool B, int R, int BLOCK>
 void force_impl(const Buffers& b, const SceneDev& s0, float4* force_out, cudaStream_t st) {
     auto k = k_force_integrate<B, R, BLOCK>;
-    constexpr size_t sm = force_smem<BLOCK>();
+    constexpr size_t sm = force_smem<R, BLOCK>();
     k<<<grid_size(k, BLOCK, sm, b.n), BLOCK, sm, st>>>(b.pos_s, b.vel_s, b.rhop, b.start, s0, b.scenes, b.nscene,
                                                        b.pos, b.vel, force_out, b.key, b.rank, b.count, b.n,
                                                        b.tile_stats);
@@ -458,9 +464,9 @@ void force_impl(const Buffers& b, const SceneDev& s0, float4* force_out, cudaStr
 template <bool B, int R, int BLOCK>
 void set_attrs() {
     cudaFuncSetAttribute(k_density<B, R, BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)density_smem<BLOCK>());
+                         (int)density_smem<R, BLOCK>());
     cudaFuncSetAttribute(k_force_integrate<B, R, BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)force_smem<BLOCK>());
+                         (int)force_smem<R, BLOCK>());
 }
 
 // Calls f(integral_constant<R>, integral_constant<BLOCK>) for the runtime (block, stencil).
