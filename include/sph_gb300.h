@@ -200,6 +200,58 @@ sph_status sph_autotune(sph_ctx* ctx, int32_t trial_steps, float* best_ms_per_st
  * memory instead (heavy pile-ups). Synchronous. */
 sph_status sph_tile_stats(sph_ctx* ctx, uint32_t out[2]);
 
+/* ---- learned macro-step (new; no reference counterpart) -----------------
+ * A message-passing network (2 rounds over the <= 32 nearest neighbours,
+ * hidden width 64) predicts each particle's velocity change over 4*dt; one
+ * network pass replaces 4 plain steps. It is trained on the GPU, by this
+ * library's own forward/backward/Adam kernels, on frames recorded from the
+ * plain step itself. Every judge_every macro-steps plain SPH re-runs the same
+ * interval from the same state; when the mean relative density deviation
+ * between the two results exceeds density_tol, or their momentum difference
+ * (relative to sum m|v| + M |G| 4 dt) exceeds momentum_tol, the plain result is
+ * kept and plain SPH runs the next judge_every macro-steps. */
+typedef struct sph_mpnn sph_mpnn;
+
+typedef struct sph_learned_report {
+    uint64_t learned_macro_steps;
+    uint64_t plain_macro_steps;   /* macro-steps (4 plain steps each) run by plain SPH */
+    uint64_t judged;
+    uint64_t fallbacks;           /* judged macro-steps that kept the plain result */
+    double last_density_dev;      /* mean |rho_learned - rho_plain| / rho_plain at the last judge */
+    double last_momentum_dev;
+    double max_density_dev;
+    double sum_density_dev;       /* over all judges */
+} sph_learned_report;
+
+uint32_t sph_mpnn_num_params(void);
+/* Network with a training workspace for frames of up to n_frame particles. */
+sph_status sph_mpnn_create(uint32_t n_frame, void* stream, sph_mpnn** out);
+sph_status sph_mpnn_destroy(sph_mpnn* net);
+const char* sph_mpnn_last_error(const sph_mpnn* net);
+/* FP32 parameter vector in the layout We1, be1, Wn1, bn1, Wp, We2, be2, Wn2, bn2, Wo, bo. */
+sph_status sph_mpnn_set_params(sph_mpnn* net, const float* params, uint32_t n);
+sph_status sph_mpnn_get_params(sph_mpnn* net, float* params, uint32_t n);
+/* Loss, outputs and gradient of one frame given in host memory (n particles; pos4/vel4
+ * n x 4, rhop2 n x 2 (rho, pres), nb n x 32 (-1 padded), cnt n, target4 n x 4 = velocity
+ * change / c; fc = {h, c, rho_self, rho0, log10(mu)/4}). out4: n x 4, grad: num_params. */
+sph_status sph_mpnn_loss_grad(sph_mpnn* net, uint32_t n, const float* pos4, const float* vel4,
+                              const float* rhop2, const int32_t* nb, const int32_t* cnt,
+                              const float* target4, const float fc[5], double* loss, float* out4,
+                              float* grad);
+/* Record n_frames frames of every scene of ctx (created with SPH_FLAG_KEEP_FORCE): the state,
+ * its neighbour lists and density, and as target the velocity change of the next 4 plain
+ * steps from the forces alone. Advances ctx by 4 * n_frames steps. */
+sph_status sph_mpnn_record(sph_mpnn* net, sph_ctx* ctx, uint32_t n_frames, uint32_t* frames_total);
+sph_status sph_mpnn_clear_frames(sph_mpnn* net);
+/* `steps` Adam steps (lr), each on one recorded frame drawn from `seed`; loss_per_step may be NULL. */
+sph_status sph_mpnn_train(sph_mpnn* net, uint32_t steps, float lr, uint64_t seed, float* loss_per_step);
+/* n_macro learned macro-steps (4*dt each) on a single-scene context, judged as above
+ * (judge_every = 0: never). */
+sph_status sph_learned_step(sph_ctx* ctx, sph_mpnn* net, int32_t n_macro, int32_t judge_every,
+                            float density_tol, float momentum_tol, sph_learned_report* report);
+/* Recompute rho and pres at the current positions (the state is re-sorted by cell). */
+sph_status sph_refresh_density(sph_ctx* ctx);
+
 /* ---- diagnostics without allocation -------------------------------------
  * No counterpart in the reference.
  *

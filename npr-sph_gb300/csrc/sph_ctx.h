@@ -1,0 +1,54 @@
+// sph_ctx.h -- the context behind the C ABI (private to the library), and the
+// engine helpers that the learned macro-step (sph_learn.cu) reuses.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "sph_internal.h"
+
+struct sph_ctx {
+    int device = 0;
+    std::string err;
+    std::vector<sph_params> params;   // per scene
+    std::vector<uint32_t> counts;     // particles per scene
+    bool batched = false;
+    uint32_t n_max = 0;
+    sphgb::Buffers b;
+    std::vector<sphgb::SceneDev> sc_h;
+    sphgb::SceneDev s0{};
+    sphgb::LaunchCfg cfg;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    bool graph_dirty = true;
+    bool have_state = false, need_hash = true, stepped = false;
+    uint64_t steps = 0;
+    long long cell_cap = 0;
+    int tile_cap = 0;
+    double* diag_dev = nullptr;
+    int* scene_first_dev = nullptr;
+    bool timing = false;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    float pass_ms[3] = {0, 0, 0};
+    uint32_t* q_ids = nullptr;
+    uint32_t* q_cnt = nullptr;
+    unsigned long long* q_dig = nullptr;
+    int q_cap = 0;
+};
+
+namespace sphgb {
+namespace engine {
+
+sph_status fail(sph_ctx* c, sph_status code, const std::string& msg);
+// Sort the current state into (pos_s, vel_s) with a valid cell table; hashes first if needed.
+// Afterwards the cell counts are consumed (the next step re-hashes).
+void sort_state(sph_ctx* ctx);
+// n plain steps (graph replay, or eager with per-pass timing).
+sph_status run_steps(sph_ctx* ctx, int n);
+sph_status check_device_error(sph_ctx* ctx);
+
+}  // namespace engine
+}  // namespace sphgb

@@ -14,48 +14,26 @@
 #include <string>
 #include <vector>
 
+#include "sph_ctx.h"
 #include "sph_host.h"
 #include "sph_internal.h"
 
 using namespace sphgb;
 
-struct sph_ctx {
-    int device = 0;
-    std::string err;
-    std::vector<sph_params> params;   // per scene
-    std::vector<uint32_t> counts;     // particles per scene
-    bool batched = false;
-    uint32_t n_max = 0;
-    Buffers b;
-    std::vector<SceneDev> sc_h;
-    SceneDev s0{};
-    LaunchCfg cfg;
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t gexec = nullptr;
-    bool graph_dirty = true;
-    bool have_state = false, need_hash = true, stepped = false;
-    uint64_t steps = 0;
-    long long cell_cap = 0;
-    int tile_cap = 0;
-    double* diag_dev = nullptr;
-    int* scene_first_dev = nullptr;
-    bool timing = false;
-    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-    float pass_ms[3] = {0, 0, 0};
-    uint32_t* q_ids = nullptr;
-    uint32_t* q_cnt = nullptr;
-    unsigned long long* q_dig = nullptr;
-    int q_cap = 0;
-};
-
-namespace {
+namespace sphgb {
+namespace engine {
 
 sph_status fail(sph_ctx* c, sph_status code, const std::string& msg) {
     if (c) c->err = msg;
     return code;
 }
+
+}  // namespace engine
+}  // namespace sphgb
+
+using sphgb::engine::fail;
+
+namespace {
 
 #define CK(call)                                                                          \
     do {                                                                                  \
@@ -342,6 +320,22 @@ sph_status reduce_all(sph_ctx* ctx, std::vector<double>& h) {
 }
 
 }  // namespace
+
+namespace sphgb {
+namespace engine {
+
+void sort_state(sph_ctx* ctx) {
+    if (ctx->need_hash) launch_hash(ctx->b, ctx->s0, ctx->batched, ctx->stream);
+    ::enqueue_sort(ctx);
+    ctx->need_hash = true;  // the scan consumed the cell counts
+}
+
+sph_status run_steps(sph_ctx* ctx, int n) { return ::run_steps(ctx, n); }
+
+sph_status check_device_error(sph_ctx* ctx) { return ::check_device_error(ctx); }
+
+}  // namespace engine
+}  // namespace sphgb
 
 extern "C" {
 

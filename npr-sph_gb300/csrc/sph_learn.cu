@@ -1,0 +1,610 @@
+// sph_learn.cu -- the learned macro-step behind the C ABI (no counterpart in
+// the reference): neighbour lists and density, frame recording from the SPH
+// step itself, the training loop, the macro-step (4*dt per network pass) and
+// the plain-SPH judge that takes over when the learned state drifts.
+//
+// Macro-step on a context (single scene):
+//   sort -> neighbours+density (k_nb_density) -> network -> integrate
+//   v' = v + c*O,  x' = x + 4 dt v + 2.5 dt c*O  (the constant-acceleration
+//   position of 4 symplectic sub-steps), then the wall clamp of
+//   integrate_comp.glsl:45-77 with the damping, then the cell hash.
+// Judge (every judge_every macro-steps): from the same state, one learned
+// macro-step and 4 plain steps; the mean relative density deviation between
+// the two results and their momentum difference decide. Above the bounds the
+// plain result is kept and plain SPH runs the next judge_every macro-steps.
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "sph_ctx.h"
+#include "sph_device.cuh"
+#include "sph_mpnn.h"
+
+using namespace sphgb;
+using sphgb::engine::fail;
+namespace M = sphgb::mpnn;
+
+struct sph_mpnn {
+    int device = 0;
+    std::string err;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    M::Trainer* tr = nullptr;   // training workspace (frames up to n_frame particles)
+    M::Trainer* inf = nullptr;  // forward-only workspace for a context (grown on demand)
+    struct Rec {
+        void* arena = nullptr;
+        M::Frame f{};
+    };
+    std::vector<Rec> frames;
+    // context-sized scratch
+    int cap = 0;
+    int *nb = nullptr, *cnt = nullptr;
+    float4 *snap_pos = nullptr, *snap_vel = nullptr, *l_pos = nullptr, *l_vel = nullptr, *acc = nullptr;
+    float2 *snap_rhop = nullptr, *l_rhop = nullptr;
+    float *rho_l = nullptr, *rho_p = nullptr;
+    float4 *vel_l = nullptr, *vel_p = nullptr;
+    double* cmp = nullptr;
+    // host-frame scratch (sph_mpnn_loss_grad)
+    int hcap = 0;
+    void* harena = nullptr;
+    int adam_t = 0;  // Adam steps taken since the parameters were last set
+};
+
+namespace {
+
+constexpr int kT = 128;
+inline int nblk(long long n, int t = kT) { return (int)((n + t - 1) / t); }
+
+#define NCK(call)                                                                              \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess) {                                                               \
+            net->err = std::string(#call) + ": " + cudaGetErrorString(e_);                     \
+            return e_ == cudaErrorMemoryAllocation ? SPH_ERR_OUT_OF_MEMORY : SPH_ERR_CUDA;     \
+        }                                                                                      \
+    } while (0)
+
+// ---- kernels ------------------------------------------------------------------------------
+
+// Density (the exact predicate, Kahan) and the K nearest neighbours j != i with r < h, over the
+// sorted state. Candidate order is the stencil walk, so the lists are deterministic.
+template <bool BATCHED, int R>
+__global__ void __launch_bounds__(kT) k_nb_density(const float4* __restrict__ pos_s, const int* __restrict__ start,
+                                                  SceneDev s0, const SceneDev* __restrict__ scenes, int nscene,
+                                                  float2* __restrict__ rhop, int* __restrict__ nb,
+                                                  int* __restrict__ cnt, int n) {
+    for (int t = blockIdx.x * kT + threadIdx.x; t < n; t += gridDim.x * kT) {
+        const float4 p = pos_s[t];
+        int sc = 0;
+        if constexpr (BATCHED) sc = min(max(scene_of(p), 0), nscene - 1);
+        const SceneDev& S = scene_params<BATCHED>(s0, scenes, sc);
+        const int cx = cell_coord(p.x, S.lo[0], S.inv_edge, S.dim[0]);
+        const int cy = cell_coord(p.y, S.lo[1], S.inv_edge, S.dim[1]);
+        const int cz = cell_coord(p.z, S.lo[2], S.inv_edge, S.dim[2]);
+        float bd[M::K];
+        int bj[M::K];
+        int c = 0, wpos = 0;
+        float worst = -1.0f, sum = 0.0f, comp = 0.0f;
+        const int x0 = max(cx - R, 0), x1 = min(cx + R, S.dim[0] - 1);
+        for (int z = max(cz - R, 0); z <= min(cz + R, S.dim[2] - 1); ++z)
+            for (int y = max(cy - R, 0); y <= min(cy + R, S.dim[1] - 1); ++y) {
+                const int row = S.cell_base + S.dim[0] * (y + S.dim[1] * z);
+                const int a = max(__ldg(start + row + x0), 0), b = min(__ldg(start + row + x1 + 1), n);
+                for (int j = a; j < b; ++j) {
+                    const float4 o = __ldg(pos_s + j);
+                    float dx, dy, dz;
+                    const float d2 = canon_d2(p.x, p.y, p.z, o.x, o.y, o.z, dx, dy, dz);
+                    if (!(d2 < S.cut_d2)) continue;
+                    const float w = S.h2 - d2;
+                    const float yk = w * w * w - comp, tk = sum + yk;  // Kahan
+                    comp = (tk - sum) - yk;
+                    sum = tk;
+                    if (j == t) continue;
+                    if (c < M::K) {
+                        bd[c] = d2;
+                        bj[c] = j;
+                        if (d2 > worst) { worst = d2; wpos = c; }
+                        ++c;
+                    } else if (d2 < worst) {
+                        bd[wpos] = d2;
+                        bj[wpos] = j;
+                        worst = -1.0f;
+                        for (int q = 0; q < M::K; ++q)
+                            if (bd[q] > worst) { worst = bd[q]; wpos = q; }
+                    }
+                }
+            }
+        const float rho = S.poly6c * sum;
+        const float pr = S.gas_k * (rho - S.rho0);
+        rhop[t] = make_float2(rho, pr < 0.0f ? 0.0f : pr);
+        for (int q = 0; q < M::K; ++q) nb[(size_t)t * M::K + q] = q < c ? bj[q] : -1;
+        cnt[t] = c;
+    }
+}
+
+// Macro-step integrate from the network output O (= velocity change / c), fused with the hash.
+__global__ void __launch_bounds__(kT) k_macro_integrate(const float4* __restrict__ pos_s, const float4* __restrict__ vel_s,
+                                                       const float* __restrict__ O, SceneDev S, float c,
+                                                       float4* __restrict__ pos_out, float4* __restrict__ vel_out,
+                                                       int* __restrict__ key_out, int* __restrict__ rank_out,
+                                                       int* __restrict__ count, int n) {
+    const int t = blockIdx.x * kT + threadIdx.x;
+    if (t >= n) return;
+    const float4 p = pos_s[t], v = vel_s[t];
+    const float dv[3] = {c * O[t * 4 + 0], c * O[t * 4 + 1], c * O[t * 4 + 2]};
+    const float vv[3] = {v.x, v.y, v.z}, pp[3] = {p.x, p.y, p.z};
+    float nv[3], np[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        nv[a] = vv[a] + dv[a];
+        np[a] = pp[a] + 4.0f * S.dt * vv[a] + 2.5f * S.dt * dv[a];
+        if (np[a] < S.lo[a]) { np[a] = S.lo[a]; nv[a] *= -S.damp; }        // integrate_comp.glsl:45-77
+        else if (np[a] > S.up[a]) { np[a] = S.up[a]; nv[a] *= -S.damp; }
+    }
+    pos_out[t] = make_float4(np[0], np[1], np[2], p.w);
+    vel_out[t] = make_float4(nv[0], nv[1], nv[2], v.w);
+    const int k = cell_key(S, np[0], np[1], np[2]);
+    key_out[t] = k;
+    rank_out[t] = atomicAdd(&count[k], 1);
+}
+
+// acc[id] += F / rho after a plain step (slot order of that step).
+__global__ void __launch_bounds__(kT) k_accum_accel(const float4* __restrict__ vel, const float4* __restrict__ force_s,
+                                                   const float2* __restrict__ rhop, int n, float4* __restrict__ acc) {
+    const int s = blockIdx.x * kT + threadIdx.x;
+    if (s >= n) return;
+    const int id = id_of(vel[s]);
+    if (id < 0 || id >= n) return;
+    const float4 f = force_s[s];
+    const float ir = 1.0f / rhop[s].x;
+    float4 a = acc[id];
+    a.x += f.x * ir; a.y += f.y * ir; a.z += f.z * ir;
+    acc[id] = a;
+}
+
+// Frame arrays of one scene from the sorted state: neighbour slots made frame-local.
+__global__ void __launch_bounds__(kT) k_frame_copy(const float4* __restrict__ pos_s, const float4* __restrict__ vel_s,
+                                                  const float2* __restrict__ rhop, const int* __restrict__ nb,
+                                                  const int* __restrict__ cnt, int first, int m, float4* __restrict__ fpos,
+                                                  float4* __restrict__ fvel, float2* __restrict__ frhop,
+                                                  int* __restrict__ fnb, int* __restrict__ fcnt, int* __restrict__ fid) {
+    const int k = blockIdx.x * kT + threadIdx.x;
+    if (k >= m) return;
+    const int s = first + k;
+    fpos[k] = pos_s[s];
+    fvel[k] = vel_s[s];
+    frhop[k] = rhop[s];
+    fid[k] = id_of(vel_s[s]);
+    const int c = cnt[s];
+    fcnt[k] = c;
+    for (int q = 0; q < M::K; ++q) {
+        const int j = nb[(size_t)s * M::K + q];
+        fnb[(size_t)k * M::K + q] = (q < c && j >= first && j < first + m) ? j - first : -1;
+    }
+}
+
+__global__ void __launch_bounds__(kT) k_frame_target(const int* __restrict__ fid, const float4* __restrict__ acc,
+                                                    int m, float scale, float4* __restrict__ target) {
+    const int k = blockIdx.x * kT + threadIdx.x;
+    if (k >= m) return;
+    const float4 a = acc[fid[k]];
+    target[k] = make_float4(a.x * scale, a.y * scale, a.z * scale, 0.0f);
+}
+
+// Density and velocity by particle id (slot order -> id order).
+__global__ void __launch_bounds__(kT) k_by_id(const float4* __restrict__ vel, const float2* __restrict__ rhop, int n,
+                                             float* __restrict__ rho_id, float4* __restrict__ vel_id) {
+    const int s = blockIdx.x * kT + threadIdx.x;
+    if (s >= n) return;
+    const float4 v = vel[s];
+    const int id = id_of(v);
+    if (id < 0 || id >= n) return;
+    rho_id[id] = rhop[s].x;
+    vel_id[id] = v;
+}
+
+// FP64 partials of the judge: sum |rho_l - rho_p| / rho_p, sum (v_l - v_p) (3), sum |v_p|.
+__global__ void __launch_bounds__(kT) k_compare(const float* __restrict__ rl, const float* __restrict__ rp,
+                                               const float4* __restrict__ vl, const float4* __restrict__ vp, int n,
+                                               double* __restrict__ out) {
+    __shared__ double sh[5][kT];
+    double a[5] = {0, 0, 0, 0, 0};
+    for (int i = blockIdx.x * kT + threadIdx.x; i < n; i += gridDim.x * kT) {
+        a[0] += fabs((double)rl[i] - (double)rp[i]) / (double)rp[i];
+        a[1] += (double)vl[i].x - (double)vp[i].x;
+        a[2] += (double)vl[i].y - (double)vp[i].y;
+        a[3] += (double)vl[i].z - (double)vp[i].z;
+        a[4] += sqrt((double)vp[i].x * vp[i].x + (double)vp[i].y * vp[i].y + (double)vp[i].z * vp[i].z);
+    }
+    for (int f = 0; f < 5; ++f) sh[f][threadIdx.x] = a[f];
+    __syncthreads();
+    for (int o = kT / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o)
+            for (int f = 0; f < 5; ++f) sh[f][threadIdx.x] += sh[f][threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int f = 0; f < 5; ++f) out[blockIdx.x * 5 + f] = sh[f][0];
+}
+
+constexpr int kCmpBlocks = 256;
+
+M::FrameConst frame_const(const SceneDev& S) {
+    M::FrameConst fc;
+    const double PI = 3.141592741f, h = S.h;
+    fc.h = S.h;
+    fc.c = (float)std::sqrt((double)S.gas_k);
+    fc.rho_self = (float)((double)S.mass * 315.0 / (64.0 * PI * h * h * h));
+    fc.rho0 = S.rho0;
+    fc.log_mu = 0.0f;
+    return fc;
+}
+
+void launch_nb_density(sph_ctx* ctx, int* nb, int* cnt) {
+    const Buffers& b = ctx->b;
+    const int blocks = nblk(b.n);
+    if (ctx->batched) {
+        if (ctx->cfg.stencil == 2)
+            k_nb_density<true, 2><<<blocks, kT, 0, ctx->stream>>>(b.pos_s, b.start, ctx->s0, b.scenes, b.nscene, b.rhop, nb, cnt, b.n);
+        else
+            k_nb_density<true, 1><<<blocks, kT, 0, ctx->stream>>>(b.pos_s, b.start, ctx->s0, b.scenes, b.nscene, b.rhop, nb, cnt, b.n);
+    } else {
+        if (ctx->cfg.stencil == 2)
+            k_nb_density<false, 2><<<blocks, kT, 0, ctx->stream>>>(b.pos_s, b.start, ctx->s0, b.scenes, 1, b.rhop, nb, cnt, b.n);
+        else
+            k_nb_density<false, 1><<<blocks, kT, 0, ctx->stream>>>(b.pos_s, b.start, ctx->s0, b.scenes, 1, b.rhop, nb, cnt, b.n);
+    }
+}
+
+template <class T>
+cudaError_t dal(T** p, size_t n) {
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    return cudaMalloc((void**)p, (n ? n : 1) * sizeof(T));
+}
+
+sph_status ensure_ctx_scratch(sph_mpnn* net, int n) {
+    if (n <= net->cap) return SPH_OK;
+    const size_t m = (size_t)n;
+    NCK(dal(&net->nb, m * M::K)); NCK(dal(&net->cnt, m));
+    NCK(dal(&net->snap_pos, m)); NCK(dal(&net->snap_vel, m)); NCK(dal(&net->snap_rhop, m));
+    NCK(dal(&net->l_pos, m)); NCK(dal(&net->l_vel, m)); NCK(dal(&net->l_rhop, m));
+    NCK(dal(&net->acc, m)); NCK(dal(&net->rho_l, m)); NCK(dal(&net->rho_p, m));
+    NCK(dal(&net->vel_l, m)); NCK(dal(&net->vel_p, m)); NCK(dal(&net->cmp, (size_t)kCmpBlocks * 5));
+    net->cap = n;
+    return SPH_OK;
+}
+
+// Density at the current positions; the sorted copy becomes the state (so rhop lines up with it).
+sph_status refresh_density(sph_ctx* ctx) {
+    engine::sort_state(ctx);
+    launch_density(ctx->b, ctx->s0, ctx->batched, ctx->cfg, ctx->stream);
+    const size_t n = (size_t)ctx->b.n;
+    cudaMemcpyAsync(ctx->b.pos, ctx->b.pos_s, n * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->stream);
+    cudaMemcpyAsync(ctx->b.vel, ctx->b.vel_s, n * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->stream);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(ctx, SPH_ERR_CUDA, std::string("density refresh: ") + cudaGetErrorString(e));
+    return SPH_OK;
+}
+
+// One learned macro-step on ctx (4*dt).
+sph_status learned_macro(sph_ctx* ctx, sph_mpnn* net) {
+    const int n = ctx->b.n;
+    engine::sort_state(ctx);
+    launch_nb_density(ctx, net->nb, net->cnt);
+    M::Frame f{ctx->b.pos_s, ctx->b.vel_s, ctx->b.rhop, net->nb, net->cnt, nullptr, n, frame_const(ctx->s0)};
+    f.fc.log_mu = (float)(std::log10((double)ctx->params[0].visc) / 4.0);
+    M::trainer_forward(net->inf, f, ctx->stream);
+    k_macro_integrate<<<nblk(n), kT, 0, ctx->stream>>>(ctx->b.pos_s, ctx->b.vel_s, M::trainer_out(net->inf), ctx->s0,
+                                                       f.fc.c, ctx->b.pos, ctx->b.vel, ctx->b.key, ctx->b.rank,
+                                                       ctx->b.count, n);
+    ctx->need_hash = false;  // the integrate hashed the new positions
+    ctx->steps += 4;
+    ctx->stepped = true;
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(ctx, SPH_ERR_CUDA, std::string("learned macro-step: ") + cudaGetErrorString(e));
+    return SPH_OK;
+}
+
+void copy_state(sph_ctx* ctx, float4* dp, float4* dv, float2* dr, const float4* sp, const float4* sv, const float2* sr) {
+    const size_t n = (size_t)ctx->b.n;
+    cudaMemcpyAsync(dp, sp, n * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->stream);
+    cudaMemcpyAsync(dv, sv, n * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->stream);
+    cudaMemcpyAsync(dr, sr, n * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+uint32_t sph_mpnn_num_params(void) { return (uint32_t)M::kParams; }
+
+sph_status sph_mpnn_create(uint32_t n_frame, void* stream, sph_mpnn** out) {
+    if (!out || n_frame == 0 || n_frame > (1u << 22)) return SPH_ERR_INVALID_ARG;
+    *out = nullptr;
+    sph_mpnn* net = new (std::nothrow) sph_mpnn;
+    if (!net) return SPH_ERR_OUT_OF_MEMORY;
+    if (cudaGetDevice(&net->device) != cudaSuccess) { delete net; return SPH_ERR_CUDA; }
+    if (stream) net->stream = (cudaStream_t)stream;
+    else if (cudaStreamCreateWithFlags(&net->stream, cudaStreamNonBlocking) == cudaSuccess) net->own_stream = true;
+    else { delete net; return SPH_ERR_CUDA; }
+    net->tr = M::trainer_new((int)n_frame, true);
+    if (!net->tr) { sph_mpnn_destroy(net); return SPH_ERR_OUT_OF_MEMORY; }
+    *out = net;
+    return SPH_OK;
+}
+
+sph_status sph_mpnn_destroy(sph_mpnn* net) {
+    if (!net) return SPH_ERR_INVALID_ARG;
+    cudaSetDevice(net->device);
+    if (net->stream) cudaStreamSynchronize(net->stream);
+    if (net->tr) M::trainer_delete(net->tr);
+    if (net->inf) M::trainer_delete(net->inf);
+    for (auto& r : net->frames) cudaFree(r.arena);
+    void* ptrs[] = {net->nb, net->cnt, net->snap_pos, net->snap_vel, net->snap_rhop, net->l_pos, net->l_vel,
+                    net->l_rhop, net->acc, net->rho_l, net->rho_p, net->vel_l, net->vel_p, net->cmp, net->harena};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (net->own_stream) cudaStreamDestroy(net->stream);
+    delete net;
+    return SPH_OK;
+}
+
+const char* sph_mpnn_last_error(const sph_mpnn* net) { return net ? net->err.c_str() : "null network"; }
+
+sph_status sph_mpnn_set_params(sph_mpnn* net, const float* params, uint32_t n) {
+    if (!net || !params || n != (uint32_t)M::kParams) return SPH_ERR_INVALID_ARG;
+    NCK(cudaSetDevice(net->device));
+    NCK(cudaMemcpyAsync(M::trainer_params(net->tr), params, sizeof(float) * n, cudaMemcpyHostToDevice, net->stream));
+    if (net->inf)
+        NCK(cudaMemcpyAsync(M::trainer_params(net->inf), params, sizeof(float) * n, cudaMemcpyHostToDevice,
+                            net->stream));
+    M::trainer_reset_adam(net->tr);
+    net->adam_t = 0;
+    NCK(cudaStreamSynchronize(net->stream));
+    return SPH_OK;
+}
+
+sph_status sph_mpnn_get_params(sph_mpnn* net, float* params, uint32_t n) {
+    if (!net || !params || n != (uint32_t)M::kParams) return SPH_ERR_INVALID_ARG;
+    NCK(cudaSetDevice(net->device));
+    NCK(cudaMemcpyAsync(params, M::trainer_params(net->tr), sizeof(float) * n, cudaMemcpyDeviceToHost, net->stream));
+    NCK(cudaStreamSynchronize(net->stream));
+    return SPH_OK;
+}
+
+sph_status sph_mpnn_loss_grad(sph_mpnn* net, uint32_t n, const float* pos4, const float* vel4, const float* rhop2,
+                              const int32_t* nb, const int32_t* cnt, const float* target4, const float fc[5],
+                              double* loss, float* out4, float* grad) {
+    if (!net || !pos4 || !vel4 || !rhop2 || !nb || !cnt || !target4 || !fc || n == 0) return SPH_ERR_INVALID_ARG;
+    if ((int)n > M::trainer_capacity(net->tr)) { net->err = "frame larger than the training workspace"; return SPH_ERR_CAPACITY; }
+    for (uint32_t i = 0; i < n; ++i) {
+        if (cnt[i] < 0 || cnt[i] > M::K) { net->err = "neighbour count out of [0, 32]"; return SPH_ERR_INVALID_ARG; }
+        for (int q = 0; q < cnt[i]; ++q)
+            if (nb[(size_t)i * M::K + q] < 0 || nb[(size_t)i * M::K + q] >= (int)n) {
+                net->err = "neighbour index out of range";
+                return SPH_ERR_INVALID_ARG;
+            }
+    }
+    NCK(cudaSetDevice(net->device));
+    const size_t bytes = (size_t)n * (16 + 16 + 8 + 16 + 4) + (size_t)n * M::K * 4;
+    if ((int)n > net->hcap) {
+        if (net->harena) cudaFree(net->harena);
+        net->harena = nullptr;
+        NCK(cudaMalloc(&net->harena, bytes));
+        net->hcap = (int)n;
+    }
+    char* a = (char*)net->harena;
+    float4* dpos = (float4*)a; a += (size_t)n * 16;
+    float4* dvel = (float4*)a; a += (size_t)n * 16;
+    float4* dtg = (float4*)a; a += (size_t)n * 16;
+    float2* drh = (float2*)a; a += (size_t)n * 8;
+    int* dcnt = (int*)a; a += (size_t)n * 4;
+    int* dnb = (int*)a;
+    cudaStream_t st = net->stream;
+    NCK(cudaMemcpyAsync(dpos, pos4, (size_t)n * 16, cudaMemcpyHostToDevice, st));
+    NCK(cudaMemcpyAsync(dvel, vel4, (size_t)n * 16, cudaMemcpyHostToDevice, st));
+    NCK(cudaMemcpyAsync(dtg, target4, (size_t)n * 16, cudaMemcpyHostToDevice, st));
+    NCK(cudaMemcpyAsync(drh, rhop2, (size_t)n * 8, cudaMemcpyHostToDevice, st));
+    NCK(cudaMemcpyAsync(dcnt, cnt, (size_t)n * 4, cudaMemcpyHostToDevice, st));
+    NCK(cudaMemcpyAsync(dnb, nb, (size_t)n * M::K * 4, cudaMemcpyHostToDevice, st));
+    M::Frame f{dpos, dvel, drh, dnb, dcnt, dtg, (int)n, {fc[0], fc[1], fc[2], fc[3], fc[4]}};
+    const double l = M::trainer_loss_grad(net->tr, f, st);
+    if (loss) *loss = l;
+    if (out4) NCK(cudaMemcpyAsync(out4, M::trainer_out(net->tr), (size_t)n * 16, cudaMemcpyDeviceToHost, st));
+    if (grad) NCK(cudaMemcpyAsync(grad, M::trainer_grad(net->tr), sizeof(float) * M::kParams, cudaMemcpyDeviceToHost, st));
+    NCK(cudaStreamSynchronize(st));
+    NCK(cudaGetLastError());
+    return SPH_OK;
+}
+
+sph_status sph_mpnn_record(sph_mpnn* net, sph_ctx* ctx, uint32_t n_frames, uint32_t* frames_total) {
+    if (!net || !ctx) return SPH_ERR_INVALID_ARG;
+    if (!ctx->have_state) { net->err = "context has no particles"; return SPH_ERR_NOT_READY; }
+    if (!(ctx->params[0].flags & SPH_FLAG_KEEP_FORCE)) {
+        net->err = "recording needs a context created with SPH_FLAG_KEEP_FORCE";
+        return SPH_ERR_INVALID_ARG;
+    }
+    for (size_t s = 0; s < ctx->counts.size(); ++s)
+        if ((int)ctx->counts[s] > M::trainer_capacity(net->tr)) {
+            net->err = "a scene is larger than the training workspace";
+            return SPH_ERR_CAPACITY;
+        }
+    NCK(cudaSetDevice(ctx->device));
+    const int n = ctx->b.n;
+    sph_status st = ensure_ctx_scratch(net, n);
+    if (st) return st;
+    for (uint32_t fr = 0; fr < n_frames; ++fr) {
+        engine::sort_state(ctx);
+        launch_nb_density(ctx, net->nb, net->cnt);
+        std::vector<size_t> first_idx;
+        for (size_t s = 0; s < ctx->sc_h.size(); ++s) {
+            const SceneDev& S = ctx->sc_h[s];
+            const int m = S.count;
+            sph_mpnn::Rec r;
+            const size_t bytes = (size_t)m * (16 + 16 + 8 + 16 + 4 + 4) + (size_t)m * M::K * 4;
+            NCK(cudaMalloc(&r.arena, bytes));
+            char* a = (char*)r.arena;
+            float4* fpos = (float4*)a; a += (size_t)m * 16;
+            float4* fvel = (float4*)a; a += (size_t)m * 16;
+            float4* ftg = (float4*)a; a += (size_t)m * 16;
+            float2* frh = (float2*)a; a += (size_t)m * 8;
+            int* fcnt = (int*)a; a += (size_t)m * 4;
+            int* fid = (int*)a; a += (size_t)m * 4;
+            int* fnb = (int*)a;
+            k_frame_copy<<<nblk(m), kT, 0, ctx->stream>>>(ctx->b.pos_s, ctx->b.vel_s, ctx->b.rhop, net->nb, net->cnt,
+                                                          S.first, m, fpos, fvel, frh, fnb, fcnt, fid);
+            r.f = M::Frame{fpos, fvel, frh, fnb, fcnt, ftg, m, frame_const(S)};
+            r.f.fc.log_mu = (float)(std::log10((double)ctx->params[s].visc) / 4.0);
+            net->frames.push_back(r);
+            first_idx.push_back(net->frames.size() - 1);
+        }
+        // target: velocity change over the next 4 plain steps from the forces alone (no wall clamp)
+        NCK(cudaMemsetAsync(net->acc, 0, sizeof(float4) * n, ctx->stream));
+        for (int sub = 0; sub < 4; ++sub) {
+            st = engine::run_steps(ctx, 1);
+            if (st) { net->err = ctx->err; return st; }
+            k_accum_accel<<<nblk(n), kT, 0, ctx->stream>>>(ctx->b.vel, ctx->b.force_s, ctx->b.rhop, n, net->acc);
+        }
+        for (size_t s = 0; s < ctx->sc_h.size(); ++s) {
+            sph_mpnn::Rec& r = net->frames[first_idx[s]];
+            const SceneDev& S = ctx->sc_h[s];
+            const int* fid = (const int*)((const char*)r.arena + (size_t)S.count * (16 + 16 + 16 + 8 + 4));
+            k_frame_target<<<nblk(S.count), kT, 0, ctx->stream>>>(fid, net->acc, S.count, S.dt / r.f.fc.c,
+                                                                 (float4*)r.f.target);
+        }
+        NCK(cudaGetLastError());
+    }
+    NCK(cudaStreamSynchronize(ctx->stream));
+    if (frames_total) *frames_total = (uint32_t)net->frames.size();
+    return SPH_OK;
+}
+
+sph_status sph_mpnn_clear_frames(sph_mpnn* net) {
+    if (!net) return SPH_ERR_INVALID_ARG;
+    cudaSetDevice(net->device);
+    for (auto& r : net->frames) cudaFree(r.arena);
+    net->frames.clear();
+    return SPH_OK;
+}
+
+sph_status sph_mpnn_train(sph_mpnn* net, uint32_t steps, float lr, uint64_t seed, float* loss_per_step) {
+    if (!net || !(lr > 0.0f)) return SPH_ERR_INVALID_ARG;
+    if (net->frames.empty()) { net->err = "no recorded frames"; return SPH_ERR_NOT_READY; }
+    NCK(cudaSetDevice(net->device));
+    std::mt19937_64 rng(seed);
+    std::uniform_int_distribution<size_t> pick(0, net->frames.size() - 1);
+    for (uint32_t s = 0; s < steps; ++s) {
+        const M::Frame& f = net->frames[pick(rng)].f;
+        const double l = M::trainer_loss_grad(net->tr, f, net->stream);
+        M::trainer_adam(net->tr, ++net->adam_t, lr, net->stream);
+        if (loss_per_step) loss_per_step[s] = (float)l;
+    }
+    NCK(cudaStreamSynchronize(net->stream));
+    NCK(cudaGetLastError());
+    if (net->inf)
+        NCK(cudaMemcpyAsync(M::trainer_params(net->inf), M::trainer_params(net->tr), sizeof(float) * M::kParams,
+                            cudaMemcpyDeviceToDevice, net->stream));
+    return SPH_OK;
+}
+
+sph_status sph_refresh_density(sph_ctx* ctx) {
+    if (!ctx) return SPH_ERR_INVALID_ARG;
+    if (!ctx->have_state) return fail(ctx, SPH_ERR_NOT_READY, "no particles uploaded");
+    cudaSetDevice(ctx->device);
+    sph_status st = refresh_density(ctx);
+    if (st) return st;
+    return engine::check_device_error(ctx);
+}
+
+sph_status sph_learned_step(sph_ctx* ctx, sph_mpnn* net, int32_t n_macro, int32_t judge_every, float density_tol,
+                            float momentum_tol, sph_learned_report* rep) {
+    if (!ctx || !net) return SPH_ERR_INVALID_ARG;
+    if (ctx->batched) return fail(ctx, SPH_ERR_UNSUPPORTED, "the learned macro-step runs on single-scene contexts");
+    if (!ctx->have_state) return fail(ctx, SPH_ERR_NOT_READY, "no particles uploaded");
+    if (n_macro < 0 || judge_every < 0) return fail(ctx, SPH_ERR_INVALID_ARG, "negative count");
+    cudaSetDevice(ctx->device);
+    const int n = ctx->b.n;
+    if (!net->inf || M::trainer_capacity(net->inf) < n) {
+        if (net->inf) M::trainer_delete(net->inf);
+        net->inf = M::trainer_new(n, false);
+        if (!net->inf) return fail(ctx, SPH_ERR_OUT_OF_MEMORY, "network workspace");
+        if (cudaMemcpy(M::trainer_params(net->inf), M::trainer_params(net->tr), sizeof(float) * M::kParams,
+                       cudaMemcpyDeviceToDevice) != cudaSuccess)
+            return fail(ctx, SPH_ERR_CUDA, "copy of the network parameters");
+    }
+    sph_status st = ensure_ctx_scratch(net, n);
+    if (st) return fail(ctx, st, net->err);
+    sph_learned_report r{};
+    int plain_left = 0;
+    for (int k = 0; k < n_macro; ++k) {
+        if (plain_left > 0) {
+            st = engine::run_steps(ctx, 4);
+            if (st) return st;
+            --plain_left;
+            ++r.plain_macro_steps;
+            continue;
+        }
+        const bool judge = judge_every > 0 && (k % judge_every) == judge_every - 1;
+        if (!judge) {
+            st = learned_macro(ctx, net);
+            if (st) return st;
+            ++r.learned_macro_steps;
+            continue;
+        }
+        // judged macro-step: learned and plain from the same state
+        copy_state(ctx, net->snap_pos, net->snap_vel, net->snap_rhop, ctx->b.pos, ctx->b.vel, ctx->b.rhop);
+        const bool hash0 = ctx->need_hash;
+        const uint64_t steps0 = ctx->steps;
+        if (!hash0) cudaMemsetAsync(ctx->b.count, 0, sizeof(int) * (size_t)ctx->b.ncell, ctx->stream);
+        ctx->need_hash = true;
+        st = learned_macro(ctx, net);
+        if (!st) st = refresh_density(ctx);
+        if (st) return st;
+        k_by_id<<<nblk(n), kT, 0, ctx->stream>>>(ctx->b.vel, ctx->b.rhop, n, net->rho_l, net->vel_l);
+        copy_state(ctx, net->l_pos, net->l_vel, net->l_rhop, ctx->b.pos, ctx->b.vel, ctx->b.rhop);
+        copy_state(ctx, ctx->b.pos, ctx->b.vel, ctx->b.rhop, net->snap_pos, net->snap_vel, net->snap_rhop);
+        cudaMemsetAsync(ctx->b.count, 0, sizeof(int) * (size_t)ctx->b.ncell, ctx->stream);
+        ctx->need_hash = true;
+        ctx->steps = steps0;
+        st = engine::run_steps(ctx, 4);
+        if (!st) st = refresh_density(ctx);
+        if (st) return st;
+        k_by_id<<<nblk(n), kT, 0, ctx->stream>>>(ctx->b.vel, ctx->b.rhop, n, net->rho_p, net->vel_p);
+        k_compare<<<kCmpBlocks, kT, 0, ctx->stream>>>(net->rho_l, net->rho_p, net->vel_l, net->vel_p, n, net->cmp);
+        std::vector<double> h((size_t)kCmpBlocks * 5);
+        if (cudaMemcpyAsync(h.data(), net->cmp, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, ctx->stream) ||
+            cudaStreamSynchronize(ctx->stream))
+            return fail(ctx, SPH_ERR_CUDA, "judge readback");
+        double s[5] = {0, 0, 0, 0, 0};
+        for (int b = 0; b < kCmpBlocks; ++b)
+            for (int f = 0; f < 5; ++f) s[f] += h[(size_t)b * 5 + f];
+        const double dev = s[0] / n;
+        const double g = std::sqrt((double)ctx->s0.g[0] * ctx->s0.g[0] + (double)ctx->s0.g[1] * ctx->s0.g[1] +
+                                   (double)ctx->s0.g[2] * ctx->s0.g[2]);
+        const double mom = std::sqrt(s[1] * s[1] + s[2] * s[2] + s[3] * s[3]) / (s[4] + n * g * 4.0 * ctx->s0.dt);
+        ++r.judged;
+        r.last_density_dev = dev;
+        r.last_momentum_dev = mom;
+        r.max_density_dev = std::max(r.max_density_dev, dev);
+        r.sum_density_dev += dev;
+        if (dev <= density_tol && mom <= momentum_tol) {
+            copy_state(ctx, ctx->b.pos, ctx->b.vel, ctx->b.rhop, net->l_pos, net->l_vel, net->l_rhop);
+            ctx->need_hash = true;
+            cudaMemsetAsync(ctx->b.count, 0, sizeof(int) * (size_t)ctx->b.ncell, ctx->stream);
+            ++r.learned_macro_steps;
+        } else {
+            ++r.fallbacks;
+            ++r.plain_macro_steps;
+            plain_left = judge_every;  // plain SPH runs the next interval
+        }
+    }
+    if (rep) *rep = r;
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(ctx, SPH_ERR_CUDA, std::string("learned step: ") + cudaGetErrorString(e));
+    return engine::check_device_error(ctx);
+}
+
+}  // extern "C"

@@ -1,0 +1,460 @@
+// sph_mpnn.cu -- training of the learned macro-step network on the GPU:
+// FP32 forward and backward kernels and Adam, over frames the SPH step itself
+// recorded. (Inference at scale runs on BF16 tensor cores in
+// sph_mpnn_infer.cu; this file is the exact FP32 reference for it.)
+//
+// The forward pass is split into small kernels that each do one thing:
+//   k_edge1_fwd   edge features e_ij (stored), round-1 edge layer, mean -> M1, node features
+//   k_dense_fwd   [M1 n] Wn1 -> H1, H1 Wp -> P, [M2 H1] Wn2 -> H2, H2 Wo -> O
+//   k_edge2_fwd   round-2 edge layer with the gathered P_j, mean -> M2
+// and the backward pass mirrors it: dense data/weight gradients, per-edge
+// gradients of round 2 (materialised), the reverse-edge gather that returns
+// dP_j to the sending particle, and the round-1 edge weight gradient. Weight
+// gradients are reduced in fixed-order partials (deterministic); the reverse
+// gather follows atomically built lists, so training is deterministic up to
+// the FP32 summation order of dP.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "sph_mpnn.h"
+#include "sph_internal.h"
+
+namespace sphgb {
+namespace mpnn {
+
+namespace {
+
+constexpr int kT = 128;  // threads per CTA
+
+inline int nblk(long long n, int t = kT) { return (int)((n + t - 1) / t); }
+
+// Edge and node features (the header of sph_mpnn.h states them).
+__device__ __forceinline__ void edge_feat(float4 pi, float4 vi, float4 pj, float4 vj, const FrameConst& fc,
+                                          float* e) {
+    const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+    const float r = sqrtf(dx * dx + dy * dy + dz * dz);
+    const float ih = 1.0f / fc.h, ic = 1.0f / fc.c;
+    e[0] = dx * ih; e[1] = dy * ih; e[2] = dz * ih;
+    e[3] = (vj.x - vi.x) * ic; e[4] = (vj.y - vi.y) * ic; e[5] = (vj.z - vi.z) * ic;
+    e[6] = r * ih;
+    e[7] = 1.0f - r * ih;
+}
+
+__device__ __forceinline__ void node_feat(float4 vi, float rho, int cnt, const FrameConst& fc, float* nf) {
+    const float ic = 1.0f / fc.c;
+    nf[0] = vi.x * ic; nf[1] = vi.y * ic; nf[2] = vi.z * ic;
+    nf[3] = rho / fc.rho_self - 1.0f;
+    nf[4] = (rho - fc.rho0) / fc.rho_self;
+    nf[5] = fc.log_mu;
+    nf[6] = (float)cnt / K;
+    nf[7] = 1.0f;
+}
+
+// Round 1 edge layer per particle: E (stored), relu masks, X1 = [M1, n].
+__global__ void __launch_bounds__(kT) k_edge1_fwd(Frame f, const float* __restrict__ prm, float* __restrict__ E,
+                                                 unsigned long long* __restrict__ mask1, float* __restrict__ X1) {
+    __shared__ float sW[FE * W], sb[W];
+    for (int t = threadIdx.x; t < FE * W; t += kT) sW[t] = prm[kWe1 + t];
+    for (int t = threadIdx.x; t < W; t += kT) sb[t] = prm[kBe1 + t];
+    __syncthreads();
+    const int i = blockIdx.x * kT + threadIdx.x;
+    if (i >= f.n) return;
+    const float4 pi = f.pos[i], vi = f.vel[i];
+    const int cnt = min(max(f.cnt[i], 0), K);
+    float m[W];
+#pragma unroll
+    for (int o = 0; o < W; ++o) m[o] = 0.0f;
+    for (int k = 0; k < K; ++k) {
+        float e[FE];
+        unsigned long long bits = 0ull;
+        if (k < cnt) {
+            const int j = f.nb[i * K + k];
+            edge_feat(pi, vi, f.pos[j], f.vel[j], f.fc, e);
+#pragma unroll
+            for (int o = 0; o < W; ++o) {
+                float z = sb[o];
+#pragma unroll
+                for (int q = 0; q < FE; ++q) z = fmaf(e[q], sW[q * W + o], z);
+                if (z > 0.0f) { m[o] += z; bits |= 1ull << o; }
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < FE; ++q) e[q] = 0.0f;
+        }
+#pragma unroll
+        for (int q = 0; q < FE; ++q) E[((size_t)i * K + k) * FE + q] = e[q];
+        mask1[(size_t)i * K + k] = bits;
+    }
+    float* x = X1 + (size_t)i * (W + FN);
+#pragma unroll
+    for (int o = 0; o < W; ++o) x[o] = m[o] * (1.0f / K);
+    float nf[FN];
+    node_feat(vi, f.rhop[i].x, cnt, f.fc, nf);
+#pragma unroll
+    for (int q = 0; q < FN; ++q) x[W + q] = nf[q];
+}
+
+// Round 2 edge layer per particle: relu masks, X2 = [M2, H1].
+__global__ void __launch_bounds__(kT) k_edge2_fwd(Frame f, const float* __restrict__ prm, const float* __restrict__ E,
+                                                 const float* __restrict__ P, const float* __restrict__ H1,
+                                                 unsigned long long* __restrict__ mask2, float* __restrict__ X2) {
+    __shared__ float sW[FE * W], sb[W];
+    for (int t = threadIdx.x; t < FE * W; t += kT) sW[t] = prm[kWe2 + t];
+    for (int t = threadIdx.x; t < W; t += kT) sb[t] = prm[kBe2 + t];
+    __syncthreads();
+    const int i = blockIdx.x * kT + threadIdx.x;
+    if (i >= f.n) return;
+    const int cnt = min(max(f.cnt[i], 0), K);
+    float m[W];
+#pragma unroll
+    for (int o = 0; o < W; ++o) m[o] = 0.0f;
+    for (int k = 0; k < K; ++k) {
+        unsigned long long bits = 0ull;
+        if (k < cnt) {
+            const int j = f.nb[i * K + k];
+            float e[FE];
+#pragma unroll
+            for (int q = 0; q < FE; ++q) e[q] = E[((size_t)i * K + k) * FE + q];
+            const float* pj = P + (size_t)j * W;
+#pragma unroll
+            for (int o = 0; o < W; ++o) {
+                float z = sb[o] + pj[o];
+#pragma unroll
+                for (int q = 0; q < FE; ++q) z = fmaf(e[q], sW[q * W + o], z);
+                if (z > 0.0f) { m[o] += z; bits |= 1ull << o; }
+            }
+        }
+        mask2[(size_t)i * K + k] = bits;
+    }
+    float* x = X2 + (size_t)i * 2 * W;
+#pragma unroll
+    for (int o = 0; o < W; ++o) x[o] = m[o] * (1.0f / K);
+    for (int o = 0; o < W; ++o) x[W + o] = H1[(size_t)i * W + o];
+}
+
+// Y[i, o] = act(sum_k X[i, k] W[k, o] + b[o]); one thread per (i, o).
+__global__ void __launch_bounds__(kT) k_dense_fwd(const float* __restrict__ X, int ldx, int kin,
+                                                 const float* __restrict__ Wt, const float* __restrict__ b, int nout,
+                                                 float* __restrict__ Y, int ldy, int n, int relu) {
+    const long long t = (long long)blockIdx.x * kT + threadIdx.x;
+    if (t >= (long long)n * nout) return;
+    const int i = (int)(t / nout), o = (int)(t % nout);
+    const float* x = X + (size_t)i * ldx;
+    float s = b ? b[o] : 0.0f;
+    for (int k = 0; k < kin; ++k) s = fmaf(x[k], Wt[k * nout + o], s);
+    Y[(size_t)i * ldy + o] = relu ? fmaxf(s, 0.0f) : s;
+}
+
+// dX[i, k] = (add[i, k] + sum_o dY[i, o] W[k, o]) * (H[i, k] > 0 if H).
+__global__ void __launch_bounds__(kT) k_dense_bwd_data(const float* __restrict__ dY, int ldy, int nout,
+                                                      const float* __restrict__ Wt, int kin,
+                                                      const float* __restrict__ add, int lda,
+                                                      const float* __restrict__ H, int ldh, float* __restrict__ dX,
+                                                      int ldx, int n) {
+    const long long t = (long long)blockIdx.x * kT + threadIdx.x;
+    if (t >= (long long)n * kin) return;
+    const int i = (int)(t / kin), k = (int)(t % kin);
+    const float* dy = dY + (size_t)i * ldy;
+    float s = add ? add[(size_t)i * lda + k] : 0.0f;
+    for (int o = 0; o < nout; ++o) s = fmaf(dy[o], Wt[k * nout + o], s);
+    if (H && !(H[(size_t)i * ldh + k] > 0.0f)) s = 0.0f;
+    dX[(size_t)i * ldx + k] = s;
+}
+
+// Weight gradient partials: part[split][k][o] = sum_{i in split} X[i,k] dY[i,o]; row k == kin is
+// the bias (X = 1). Rows of a split are summed in order: deterministic.
+__global__ void __launch_bounds__(kT) k_wgrad_partial(const float* __restrict__ X, int ldx, int kin,
+                                                     const float* __restrict__ dY, int ldy, int nout, int n,
+                                                     int rows_per_split, float* __restrict__ part) {
+    const int t = blockIdx.x * kT + threadIdx.x;
+    const int total = (kin + 1) * nout;
+    if (t >= total) return;
+    const int k = t / nout, o = t % nout;
+    const int a = blockIdx.y * rows_per_split, b = min(a + rows_per_split, n);
+    float s = 0.0f;
+    for (int i = a; i < b; ++i) s = fmaf(k < kin ? X[(size_t)i * ldx + k] : 1.0f, dY[(size_t)i * ldy + o], s);
+    part[(size_t)blockIdx.y * total + t] = s;
+}
+
+// Edge-layer weight gradient partials over edges (kin = FE, bias row FE). Round 2 reads the
+// materialised dZ; round 1 (dZ == null) forms dZ1 = dM1 / K masked by the relu bits.
+__global__ void __launch_bounds__(kT) k_edge_wgrad_partial(const float* __restrict__ E, const float* __restrict__ dZ,
+                                                          const float* __restrict__ dM, int ldm,
+                                                          const unsigned long long* __restrict__ mask,
+                                                          const int* __restrict__ cnt, int n, int rows_per_split,
+                                                          float* __restrict__ part) {
+    const int t = blockIdx.x * kT + threadIdx.x;
+    const int total = (FE + 1) * W;
+    if (t >= total) return;
+    const int k = t / W, o = t % W;
+    const long long a = (long long)blockIdx.y * rows_per_split;
+    const long long b = min(a + rows_per_split, (long long)n * K);
+    float s = 0.0f;
+    for (long long r = a; r < b; ++r) {
+        const int i = (int)(r / K), e = (int)(r % K);
+        if (e >= cnt[i]) continue;
+        float dz;
+        if (dZ) dz = dZ[r * W + o];
+        else dz = ((mask[r] >> o) & 1ull) ? dM[(size_t)i * ldm + o] * (1.0f / K) : 0.0f;
+        s = fmaf(k < FE ? E[r * FE + k] : 1.0f, dz, s);
+    }
+    part[(size_t)blockIdx.y * total + t] = s;
+}
+
+__global__ void __launch_bounds__(kT) k_reduce_split(const float* __restrict__ part, int splits, int total,
+                                                    float* __restrict__ gw, int nw, float* __restrict__ gb) {
+    const int t = blockIdx.x * kT + threadIdx.x;
+    if (t >= total) return;
+    float s = 0.0f;
+    for (int q = 0; q < splits; ++q) s += part[(size_t)q * total + t];
+    if (t < nw) gw[t] = s;
+    else if (gb) gb[t - nw] = s;
+}
+
+__global__ void __launch_bounds__(kT) k_loss(const float* __restrict__ O, const float4* __restrict__ target, int n,
+                                            float* __restrict__ dO, double* __restrict__ part) {
+    __shared__ double sh[kT];
+    const int i = blockIdx.x * kT + threadIdx.x;
+    double l = 0.0;
+    if (i < n) {
+        const float4 tg = target[i];
+        const float d0 = O[i * 4 + 0] - tg.x, d1 = O[i * 4 + 1] - tg.y, d2 = O[i * 4 + 2] - tg.z;
+        const float s = 2.0f / (float)n;
+        dO[i * 4 + 0] = s * d0; dO[i * 4 + 1] = s * d1; dO[i * 4 + 2] = s * d2; dO[i * 4 + 3] = 0.0f;
+        l = (double)d0 * d0 + (double)d1 * d1 + (double)d2 * d2;
+    }
+    sh[threadIdx.x] = l;
+    __syncthreads();
+    for (int o = kT / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+// Per-edge round-2 gradient dZ2 = dM2 / K masked by the relu bits (zero on padded edges).
+__global__ void __launch_bounds__(kT) k_edge2_bwd(const float* __restrict__ dX2, const unsigned long long* __restrict__ mask2,
+                                                 const int* __restrict__ cnt, int n, float* __restrict__ dZ2) {
+    const long long t = (long long)blockIdx.x * kT + threadIdx.x;
+    if (t >= (long long)n * K * W) return;
+    const long long r = t / W;
+    const int o = (int)(t % W), i = (int)(r / K), e = (int)(r % K);
+    float v = 0.0f;
+    if (e < cnt[i] && ((mask2[r] >> o) & 1ull)) v = dX2[(size_t)i * 2 * W + o] * (1.0f / K);
+    dZ2[t] = v;
+}
+
+__global__ void __launch_bounds__(kT) k_rev_count(const int* __restrict__ nb, const int* __restrict__ cnt, int n,
+                                                 int* __restrict__ rc) {
+    const long long r = (long long)blockIdx.x * kT + threadIdx.x;
+    if (r >= (long long)n * K) return;
+    const int i = (int)(r / K), e = (int)(r % K);
+    if (e < cnt[i]) atomicAdd(&rc[nb[r]], 1);
+}
+
+// Exclusive scan of rc[0, n) into off[0, n] by one CTA of 1024 threads (frames are small).
+__global__ void __launch_bounds__(1024) k_scan_small(const int* __restrict__ rc, int n, int* __restrict__ off) {
+    __shared__ int s[1024];
+    const int per = (n + 1023) / 1024, a = threadIdx.x * per, b = min(a + per, n);
+    int local = 0;
+    for (int i = a; i < b; ++i) local += rc[i];
+    s[threadIdx.x] = local;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const int v = threadIdx.x >= o ? s[threadIdx.x - o] : 0;
+        __syncthreads();
+        s[threadIdx.x] += v;
+        __syncthreads();
+    }
+    int run = s[threadIdx.x] - local;
+    for (int i = a; i < b; ++i) { off[i] = run; run += rc[i]; }
+    if (threadIdx.x == 1023) off[n] = s[1023];
+}
+
+__global__ void __launch_bounds__(kT) k_rev_fill(const int* __restrict__ nb, const int* __restrict__ cnt, int n,
+                                                const int* __restrict__ off, int* __restrict__ cur,
+                                                int* __restrict__ edges) {
+    const long long r = (long long)blockIdx.x * kT + threadIdx.x;
+    if (r >= (long long)n * K) return;
+    const int i = (int)(r / K), e = (int)(r % K);
+    if (e >= cnt[i]) return;
+    const int j = nb[r];
+    edges[off[j] + atomicAdd(&cur[j], 1)] = (int)r;
+}
+
+// dP[j, o] = sum over the edges (i -> j) of dZ2[edge, o].
+__global__ void __launch_bounds__(kT) k_rev_gather(const int* __restrict__ off, const int* __restrict__ edges,
+                                                  const float* __restrict__ dZ2, int n, float* __restrict__ dP) {
+    const long long t = (long long)blockIdx.x * kT + threadIdx.x;
+    if (t >= (long long)n * W) return;
+    const int j = (int)(t / W), o = (int)(t % W);
+    float s = 0.0f;
+    for (int q = off[j]; q < off[j + 1]; ++q) s += dZ2[(size_t)edges[q] * W + o];
+    dP[t] = s;
+}
+
+__global__ void __launch_bounds__(kT) k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
+                                            float* __restrict__ v, int np, float lr, float b1, float b2, float eps,
+                                            float c1, float c2) {
+    const int t = blockIdx.x * kT + threadIdx.x;
+    if (t >= np) return;
+    const float gt = g[t];
+    const float mt = b1 * m[t] + (1.0f - b1) * gt;
+    const float vt = b2 * v[t] + (1.0f - b2) * gt * gt;
+    m[t] = mt;
+    v[t] = vt;
+    p[t] -= lr * (mt * c1) / (sqrtf(vt * c2) + eps);
+}
+
+}  // namespace
+
+// Workspace and passes of one training frame (up to n_max particles).
+struct Trainer {
+    int n_max = 0;
+    float *prm = nullptr, *grad = nullptr, *adam_m = nullptr, *adam_v = nullptr;
+    float *E = nullptr, *X1 = nullptr, *H1 = nullptr, *P = nullptr, *X2 = nullptr, *H2 = nullptr, *O = nullptr;
+    float *dO = nullptr, *dY2 = nullptr, *dX2 = nullptr, *dZ2 = nullptr, *dP = nullptr, *dY1 = nullptr, *dX1 = nullptr;
+    float* part = nullptr;
+    double* loss_part = nullptr;
+    unsigned long long *mask1 = nullptr, *mask2 = nullptr;
+    int *rev_cnt = nullptr, *rev_off = nullptr, *rev_edges = nullptr;
+    int splits = 64;
+
+    template <class T>
+    static cudaError_t al(T** p, size_t n) { return cudaMalloc((void**)p, (n ? n : 1) * sizeof(T)); }
+
+    // train = false allocates the forward pass only.
+    cudaError_t init(int nmax, bool train) {
+        n_max = nmax;
+        const size_t n = (size_t)nmax, e = n * K;
+        cudaError_t r = cudaSuccess;
+        auto A = [&](cudaError_t x) { if (r == cudaSuccess) r = x; };
+        A(al(&prm, kParams));
+        A(al(&E, e * FE)); A(al(&X1, n * (W + FN))); A(al(&H1, n * W)); A(al(&P, n * W)); A(al(&X2, n * 2 * W));
+        A(al(&H2, n * W)); A(al(&O, n * 4)); A(al(&mask1, e)); A(al(&mask2, e));
+        if (train) {
+            A(al(&grad, kParams)); A(al(&adam_m, kParams)); A(al(&adam_v, kParams));
+            A(al(&dO, n * 4)); A(al(&dY2, n * W)); A(al(&dX2, n * 2 * W));
+            A(al(&dZ2, e * W)); A(al(&dP, n * W)); A(al(&dY1, n * W)); A(al(&dX1, n * (W + FN)));
+            A(al(&part, (size_t)splits * (2 * W + 1) * W)); A(al(&loss_part, (size_t)nblk(n) + 1));
+            A(al(&rev_cnt, n)); A(al(&rev_off, n + 1)); A(al(&rev_edges, e));
+            if (r == cudaSuccess) r = cudaMemset(adam_m, 0, sizeof(float) * kParams);
+            if (r == cudaSuccess) r = cudaMemset(adam_v, 0, sizeof(float) * kParams);
+        }
+        return r;
+    }
+
+    ~Trainer() {
+        void* ptrs[] = {prm, grad, adam_m, adam_v, E, X1, H1, P, X2, H2, O, dO, dY2, dX2, dZ2, dP, dY1, dX1,
+                        part, loss_part, mask1, mask2, rev_cnt, rev_off, rev_edges};
+        for (void* q : ptrs)
+            if (q) cudaFree(q);
+    }
+
+    void dense(const float* X, int ldx, int kin, int woff, int boff, int nout, float* Y, int ldy, int n, int relu,
+               cudaStream_t st) {
+        k_dense_fwd<<<nblk((long long)n * nout), kT, 0, st>>>(X, ldx, kin, prm + woff, boff >= 0 ? prm + boff : nullptr,
+                                                             nout, Y, ldy, n, relu);
+    }
+
+    void wgrad(const float* X, int ldx, int kin, const float* dY, int ldy, int nout, int n, int woff, int boff,
+               cudaStream_t st) {
+        const int rows = (n + splits - 1) / splits;
+        const int total = (kin + 1) * nout;
+        k_wgrad_partial<<<dim3(nblk(total), splits), kT, 0, st>>>(X, ldx, kin, dY, ldy, nout, n, rows, part);
+        k_reduce_split<<<nblk(total), kT, 0, st>>>(part, splits, total, grad + woff, kin * nout,
+                                                   boff >= 0 ? grad + boff : nullptr);
+    }
+
+    void edge_wgrad(const float* dZ, const float* dM, int ldm, const unsigned long long* mask, const int* cnt, int n,
+                    int woff, int boff, cudaStream_t st) {
+        const long long rows_total = (long long)n * K;
+        const int rows = (int)((rows_total + splits - 1) / splits);
+        const int total = (FE + 1) * W;
+        k_edge_wgrad_partial<<<dim3(nblk(total), splits), kT, 0, st>>>(E, dZ, dM, ldm, mask, cnt, n, rows, part);
+        k_reduce_split<<<nblk(total), kT, 0, st>>>(part, splits, total, grad + woff, FE * W, grad + boff);
+    }
+
+    // Forward: O (n x 4) from the frame.
+    void forward(const Frame& f, cudaStream_t st) {
+        const int n = f.n;
+        k_edge1_fwd<<<nblk(n), kT, 0, st>>>(f, prm, E, mask1, X1);
+        dense(X1, W + FN, W + FN, kWn1, kBn1, W, H1, W, n, 1, st);
+        dense(H1, W, W, kWp, -1, W, P, W, n, 0, st);
+        k_edge2_fwd<<<nblk(n), kT, 0, st>>>(f, prm, E, P, H1, mask2, X2);
+        dense(X2, 2 * W, 2 * W, kWn2, kBn2, W, H2, W, n, 1, st);
+        dense(H2, W, W, kWo, kBo, FO, O, 4, n, 0, st);
+    }
+
+    // Loss partials and the full parameter gradient (forward must have run).
+    void backward(const Frame& f, cudaStream_t st) {
+        const int n = f.n;
+        k_loss<<<nblk(n), kT, 0, st>>>(O, f.target, n, dO, loss_part);
+        wgrad(H2, W, W, dO, 4, FO, n, kWo, kBo, st);
+        k_dense_bwd_data<<<nblk((long long)n * W), kT, 0, st>>>(dO, 4, FO, prm + kWo, W, nullptr, 0, H2, W, dY2, W, n);
+        wgrad(X2, 2 * W, 2 * W, dY2, W, W, n, kWn2, kBn2, st);
+        k_dense_bwd_data<<<nblk((long long)n * 2 * W), kT, 0, st>>>(dY2, W, W, prm + kWn2, 2 * W, nullptr, 0, nullptr,
+                                                                    0, dX2, 2 * W, n);
+        k_edge2_bwd<<<nblk((long long)n * K * W), kT, 0, st>>>(dX2, mask2, f.cnt, n, dZ2);
+        edge_wgrad(dZ2, nullptr, 0, nullptr, f.cnt, n, kWe2, kBe2, st);
+        cudaMemsetAsync(rev_cnt, 0, sizeof(int) * n, st);
+        k_rev_count<<<nblk((long long)n * K), kT, 0, st>>>(f.nb, f.cnt, n, rev_cnt);
+        k_scan_small<<<1, 1024, 0, st>>>(rev_cnt, n, rev_off);
+        cudaMemsetAsync(rev_cnt, 0, sizeof(int) * n, st);
+        k_rev_fill<<<nblk((long long)n * K), kT, 0, st>>>(f.nb, f.cnt, n, rev_off, rev_cnt, rev_edges);
+        k_rev_gather<<<nblk((long long)n * W), kT, 0, st>>>(rev_off, rev_edges, dZ2, n, dP);
+        wgrad(H1, W, W, dP, W, W, n, kWp, -1, st);
+        // dY1 = (dX2[:, W:] + dP Wp^T) * (H1 > 0)
+        k_dense_bwd_data<<<nblk((long long)n * W), kT, 0, st>>>(dP, W, W, prm + kWp, W, dX2 + W, 2 * W, H1, W, dY1, W,
+                                                                n);
+        wgrad(X1, W + FN, W + FN, dY1, W, W, n, kWn1, kBn1, st);
+        k_dense_bwd_data<<<nblk((long long)n * (W + FN)), kT, 0, st>>>(dY1, W, W, prm + kWn1, W + FN, nullptr, 0,
+                                                                        nullptr, 0, dX1, W + FN, n);
+        edge_wgrad(nullptr, dX1, W + FN, mask1, f.cnt, n, kWe1, kBe1, st);
+    }
+
+    void adam(int t, float lr, cudaStream_t st) {
+        const float b1 = 0.9f, b2 = 0.999f;
+        const float c1 = (float)(1.0 / (1.0 - std::pow((double)b1, t)));
+        const float c2 = (float)(1.0 / (1.0 - std::pow((double)b2, t)));
+        k_adam<<<nblk(kParams), kT, 0, st>>>(prm, grad, adam_m, adam_v, kParams, lr, b1, b2, 1e-8f, c1, c2);
+    }
+
+    double loss(int n, cudaStream_t st) {
+        std::vector<double> h(nblk(n));
+        cudaMemcpyAsync(h.data(), loss_part, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, st);
+        cudaStreamSynchronize(st);
+        double s = 0.0;
+        for (double x : h) s += x;
+        return s / (double)n;
+    }
+};
+
+Trainer* trainer_new(int n_max, bool train) {
+    Trainer* t = new Trainer;
+    if (t->init(n_max, train) != cudaSuccess) {
+        delete t;
+        return nullptr;
+    }
+    return t;
+}
+void trainer_delete(Trainer* t) { delete t; }
+float* trainer_params(Trainer* t) { return t->prm; }
+float* trainer_grad(Trainer* t) { return t->grad; }
+float* trainer_out(Trainer* t) { return t->O; }
+void trainer_reset_adam(Trainer* t) {
+    if (t->adam_m) cudaMemset(t->adam_m, 0, sizeof(float) * kParams);
+    if (t->adam_v) cudaMemset(t->adam_v, 0, sizeof(float) * kParams);
+}
+int trainer_capacity(Trainer* t) { return t->n_max; }
+void trainer_forward(Trainer* t, const Frame& f, cudaStream_t st) { t->forward(f, st); }
+double trainer_loss_grad(Trainer* t, const Frame& f, cudaStream_t st) {
+    t->forward(f, st);
+    t->backward(f, st);
+    return t->loss(f.n, st);
+}
+void trainer_adam(Trainer* t, int step, float lr, cudaStream_t st) { t->adam(step, lr, st); }
+
+}  // namespace mpnn
+}  // namespace sphgb

@@ -64,6 +64,15 @@ class Diag(C.Structure):
                 "nonfinite": int(self.nonfinite), "n": int(self.n), "step": int(self.step)}
 
 
+class LearnedReport(C.Structure):
+    _fields_ = [("learned_macro_steps", C.c_uint64), ("plain_macro_steps", C.c_uint64), ("judged", C.c_uint64),
+                ("fallbacks", C.c_uint64), ("last_density_dev", C.c_double), ("last_momentum_dev", C.c_double),
+                ("max_density_dev", C.c_double), ("sum_density_dev", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 # Every symbol of include/sph_gb300.h with its ctypes signature.
 _P = C.c_void_p
 _SIGS = {
@@ -97,6 +106,18 @@ _SIGS = {
     "sph_autotune": (C.c_int32, [_P, C.c_int32, C.POINTER(C.c_float)]),
     "sph_tile_stats": (C.c_int32, [_P, C.POINTER(C.c_uint32)]),
     "sph_reduce_aos_noalloc": (C.c_int32, [_P, C.c_uint32, C.POINTER(Params), _P, _P]),
+    "sph_mpnn_num_params": (C.c_uint32, []),
+    "sph_mpnn_create": (C.c_int32, [C.c_uint32, _P, C.POINTER(_P)]),
+    "sph_mpnn_destroy": (C.c_int32, [_P]),
+    "sph_mpnn_last_error": (C.c_char_p, [_P]),
+    "sph_mpnn_set_params": (C.c_int32, [_P, _P, C.c_uint32]),
+    "sph_mpnn_get_params": (C.c_int32, [_P, _P, C.c_uint32]),
+    "sph_mpnn_loss_grad": (C.c_int32, [_P, C.c_uint32, _P, _P, _P, _P, _P, _P, _P, C.POINTER(C.c_double), _P, _P]),
+    "sph_mpnn_record": (C.c_int32, [_P, _P, C.c_uint32, C.POINTER(C.c_uint32)]),
+    "sph_mpnn_clear_frames": (C.c_int32, [_P]),
+    "sph_mpnn_train": (C.c_int32, [_P, C.c_uint32, C.c_float, C.c_uint64, _P]),
+    "sph_learned_step": (C.c_int32, [_P, _P, C.c_int32, C.c_int32, C.c_float, C.c_float, C.POINTER(LearnedReport)]),
+    "sph_refresh_density": (C.c_int32, [_P]),
     "sph_scene_reference_grid": (C.c_int32, [_P, C.c_uint32, C.c_float]),
     "sph_scene_fill": (C.c_int32, [_P, C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_float,
                                    C.c_float, C.c_uint64]),
@@ -284,6 +305,87 @@ class Sim:
         ms = C.c_float()
         _check(lib.sph_autotune(self._ctx, trial_steps, C.byref(ms)), self._ctx)
         return float(ms.value)
+
+
+    def refresh_density(self) -> None:
+        """rho and pres at the current positions (sph_refresh_density)."""
+        _check(lib.sph_refresh_density(self._ctx), self._ctx)
+
+    def learned_step(self, net: "Net", n_macro: int, judge_every: int = 8, density_tol: float = 0.01,
+                     momentum_tol: float = 0.01) -> LearnedReport:
+        rep = LearnedReport()
+        _check(lib.sph_learned_step(self._ctx, net.handle, n_macro, judge_every, density_tol, momentum_tol,
+                                    C.byref(rep)), self._ctx)
+        return rep
+
+
+class Net:
+    """The learned macro-step network (sph_mpnn_*): parameters, training frames, training."""
+
+    def __init__(self, n_frame: int, stream=None):
+        self._h = C.c_void_p()
+        s = C.c_void_p(int(stream) if stream is not None else 0)
+        _check(lib.sph_mpnn_create(n_frame, s, C.byref(self._h)), what="sph_mpnn_create")
+        self.n_params = int(lib.sph_mpnn_num_params())
+
+    @property
+    def handle(self):
+        return self._h
+
+    def _check(self, code):
+        if code != OK:
+            raise SphError(code, lib.sph_mpnn_last_error(self._h).decode())
+
+    def close(self):
+        if self._h:
+            lib.sph_mpnn_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_params(self, flat: np.ndarray) -> None:
+        a = np.ascontiguousarray(flat, dtype=np.float32)
+        self._check(lib.sph_mpnn_set_params(self._h, a.ctypes.data, len(a)))
+
+    def get_params(self) -> np.ndarray:
+        a = np.zeros(self.n_params, dtype=np.float32)
+        self._check(lib.sph_mpnn_get_params(self._h, a.ctypes.data, len(a)))
+        return a
+
+    def loss_grad(self, pos4, vel4, rhop2, nb, cnt, target4, fc):
+        n = len(pos4)
+        arrs = [np.ascontiguousarray(x, dtype=t) for x, t in
+                ((pos4, np.float32), (vel4, np.float32), (rhop2, np.float32), (nb, np.int32), (cnt, np.int32),
+                 (target4, np.float32), (fc, np.float32))]
+        out = np.zeros((n, 4), dtype=np.float32)
+        grad = np.zeros(self.n_params, dtype=np.float32)
+        loss = C.c_double()
+        self._check(lib.sph_mpnn_loss_grad(self._h, n, *[a.ctypes.data for a in arrs], C.byref(loss), out.ctypes.data,
+                                           grad.ctypes.data))
+        return loss.value, out, grad
+
+    def record(self, sim: Sim, n_frames: int) -> int:
+        tot = C.c_uint32()
+        self._check(lib.sph_mpnn_record(self._h, sim.ctx, n_frames, C.byref(tot)))
+        return tot.value
+
+    def clear_frames(self) -> None:
+        self._check(lib.sph_mpnn_clear_frames(self._h))
+
+    def train(self, steps: int, lr: float = 1e-3, seed: int = 0) -> np.ndarray:
+        losses = np.zeros(steps, dtype=np.float32)
+        self._check(lib.sph_mpnn_train(self._h, steps, C.c_float(lr), C.c_uint64(seed), losses.ctypes.data))
+        return losses
 
 
 # ---- scenes -------------------------------------------------------------------------------

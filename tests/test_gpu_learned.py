@@ -1,0 +1,132 @@
+"""The learned macro-step: GPU forward/backward against the FP64 restatement
+(oracle/mpnn_oracle.py), training on frames recorded from the plain step, the judge, and
+the gain of the trained network over the same macro-step without it (a zero network:
+v' = v, x' = x + 4 dt v)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def random_frame(seed: int, n: int = 96):
+    from oracle import mpnn_oracle as MO
+
+    rng = np.random.default_rng(seed)
+    h, c = 0.02, 44.72
+    pos = rng.uniform(0.0, 0.06, (n, 3))
+    d = np.linalg.norm(pos[:, None, :] - pos[None, :, :], axis=-1)
+    nb = np.full((n, MO.K), -1, dtype=np.int32)
+    cnt = np.zeros(n, dtype=np.int32)
+    for i in range(n):
+        js = [j for j in np.argsort(d[i]) if j != i and d[i, j] < h][:MO.K]
+        cnt[i] = len(js)
+        nb[i, :len(js)] = js
+    vel = rng.normal(0.0, 1.0, (n, 3))
+    rho = rng.uniform(3900.0, 20000.0, n)
+    target = rng.normal(0.0, 0.05, (n, 3))
+    fc = np.array([h, c, 3916.7, 1000.0, np.log10(3000.0) / 4.0])
+    return pos, vel, rho, nb, cnt, target, fc
+
+
+def test_forward_and_gradient_match_fp64_oracle(sph, gpu):
+    from oracle import mpnn_oracle as MO
+
+    pos, vel, rho, nb, cnt, target, fc = random_frame(3)
+    n = len(pos)
+    assert cnt.min() >= 0 and cnt.max() > 4
+    f32 = lambda a: np.asarray(a, np.float32).astype(np.float64)  # the GPU sees FP32 inputs
+    flat = MO.init_params(7)
+    pos4 = np.zeros((n, 4), np.float32); pos4[:, :3] = pos
+    vel4 = np.zeros((n, 4), np.float32); vel4[:, :3] = vel
+    rhop = np.zeros((n, 2), np.float32); rhop[:, 0] = rho
+    tg4 = np.zeros((n, 4), np.float32); tg4[:, :3] = target
+    with sph.Net(128) as net:
+        net.set_params(flat)
+        loss, out, grad = net.loss_grad(pos4, vel4, rhop, nb, cnt, tg4, fc)
+    e, mask, nf = MO.features(f32(pos), f32(vel), f32(rho), nb, cnt, *[float(np.float32(x)) for x in fc[:2]],
+                              float(np.float32(fc[2])), float(np.float32(fc[3])), 3000.0)
+    ref_loss, ref_out, ref_grad = MO.loss_and_grad(flat.astype(np.float64), e, mask, nf, nb, f32(target))
+    np.testing.assert_allclose(out[:, :3], ref_out, rtol=0, atol=2e-5 * np.abs(ref_out).max())
+    assert loss == pytest.approx(ref_loss, rel=1e-4)
+    off = 0
+    for name, shape in MO.LAYOUT:
+        size = int(np.prod(shape))
+        g, r = grad[off:off + size], ref_grad[off:off + size]
+        scale = np.abs(r).max() + 1e-12
+        assert np.max(np.abs(g - r)) <= 2e-4 * scale, (name, np.max(np.abs(g - r)) / scale)
+        off += size
+
+
+@pytest.fixture(scope="module")
+def trained(sph, gpu):
+    """A network trained briefly on frames of two small dam breaks (k and mu varied)."""
+    from oracle import mpnn_oracle as MO
+
+    net = sph.Net(20000)
+    net.set_params(MO.init_params(0))
+    for seed, k, mu in ((11, 2000.0, 3000.0), (12, 1200.0, 1.0)):
+        sc = sph.dam_break(16, 32, 32, seed=seed, flags=sph.FLAG_KEEP_FORCE)
+        p = sc.params.copy()
+        p.gas_const, p.visc = k, mu
+        with sph.Sim(p, n_max=len(sc.particles)) as sim:
+            sim.upload(sc.particles)
+            sim.step(8)
+            net.record(sim, 6)
+    losses = net.train(600, lr=2e-3, seed=1)
+    yield net, losses
+    net.close()
+
+
+def test_training_reduces_the_loss(trained):
+    _, losses = trained
+    assert np.all(np.isfinite(losses))
+    assert losses[-50:].mean() < 0.5 * losses[:20].mean()
+
+
+def test_trained_network_beats_the_macro_step_without_it(sph, trained):
+    from oracle import mpnn_oracle as MO
+
+    net, _ = trained
+    sc = sph.dam_break(16, 32, 32, seed=21)
+    devs = {}
+    with sph.Net(16) as zero:
+        zero.set_params(np.zeros(MO.n_params(), np.float32))
+        for name, nn in (("trained", net), ("zero", zero)):
+            with sph.Sim(sc.params, n_max=len(sc.particles)) as sim:
+                sim.upload(sc.particles)
+                sim.step(8)
+                rep = sim.learned_step(nn, 1, judge_every=1, density_tol=1.0, momentum_tol=1e9)
+                assert rep.judged == 1 and rep.fallbacks == 0
+                devs[name] = rep.last_density_dev
+    assert devs["trained"] < devs["zero"], devs
+
+
+def test_judge_falls_back_to_plain(sph, trained):
+    net, _ = trained
+    sc = sph.dam_break(16, 32, 32, seed=22)
+    with sph.Sim(sc.params, n_max=len(sc.particles)) as sim:
+        sim.upload(sc.particles)
+        sim.step(4)
+        rep = sim.learned_step(net, 6, judge_every=2, density_tol=0.0, momentum_tol=0.0)
+        assert rep.judged >= 1 and rep.fallbacks >= 1
+        assert rep.learned_macro_steps + rep.plain_macro_steps == 6
+        assert sim.steps == 4 + 6 * 4
+        d = sim.reduce()
+        assert d.nonfinite == 0
+
+
+def test_learned_run_stays_finite(sph, trained):
+    net, _ = trained
+    sc = sph.dam_break(16, 32, 32, seed=23)
+    with sph.Sim(sc.params, n_max=len(sc.particles)) as sim:
+        sim.upload(sc.particles)
+        sim.step(4)
+        rep = sim.learned_step(net, 16, judge_every=8, density_tol=0.05, momentum_tol=0.05)
+        d = sim.reduce()
+        out = sim.download()
+    assert rep.judged == 2
+    assert d.nonfinite == 0
+    lo, hi = np.array(sc.params.lower[:3]), np.array(sc.params.upper[:3])
+    assert np.all(out["pos"][:, :3] >= lo) and np.all(out["pos"][:, :3] <= hi)
