@@ -231,6 +231,73 @@ def extra_workloads(args, stream) -> dict:
     return out
 
 
+WEIGHTS = REPO / "npr-sph_gb300" / "weights" / "mpnn_w64.npy"
+
+
+def learned_workload(args, stream, flush) -> dict:
+    """The learned macro-step on the same dam break: units of 8 macro-steps (32 dt, one judged
+    against plain SPH), each timed with CUDA events, L2 flushed between units; plain SPH timed
+    the same way over the same interval from the same state; and the end states compared."""
+    import torch
+    import nprsph as S
+
+    if not WEIGHTS.exists():
+        return {"unavailable": f"no trained weights at {WEIGHTS.relative_to(REPO)}"}
+    params = np.load(WEIGHTS).astype(np.float32)
+    sc = S.dam_break(seed=2)
+    n = len(sc.particles)
+    units = max(1, args.steps // 32)
+    judge_every, tol = 8, 0.01
+
+    def timed_units(fn) -> float:
+        total = 0.0
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for _ in range(units):
+            with torch.cuda.stream(stream):
+                flush.add_(1.0)
+            torch.cuda.synchronize()
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            total += a.elapsed_time(b) / 1e3
+        return total
+
+    out = {"workload": "dam break 1,048,576 particles (as above), learned macro-steps of 4 dt, judged every 8 "
+                       "against 4 plain steps from the same state (tolerance 1% mean density deviation, "
+                       "1% momentum)", "units": units, "macro_steps": units * judge_every,
+           "dt_equivalents": units * 32}
+    with S.Net(16, stream=stream.cuda_stream) as net, \
+            S.Sim(sc.params, n_max=n, stream=stream.cuda_stream) as learned, \
+            S.Sim(sc.params, n_max=n, stream=stream.cuda_stream) as plain:
+        net.set_params(params)
+        reps = []
+        for sim in (learned, plain):
+            sim.upload(sc.particles)
+            sim.step(args.warmup)
+        learned.learned_step(net, judge_every, judge_every, tol, tol)  # warm-up unit (allocations)
+        plain.step(32)
+        t_l = timed_units(lambda: reps.append(learned.learned_step(net, judge_every, judge_every, tol, tol)))
+        t_p = timed_units(lambda: plain.step(32))
+        learned.refresh_density()
+        plain.refresh_density()
+        a, b = learned.download(), plain.download()
+    rl, rp = a["extras"][:, 0].astype(np.float64), b["extras"][:, 0].astype(np.float64)
+    judged = sum(r.judged for r in reps)
+    out.update({
+        "value": n * 32 * units / t_l, "unit": UNIT, "ms_per_dt": 1e3 * t_l / (32 * units),
+        "plain_value": n * 32 * units / t_p, "plain_ms_per_dt": 1e3 * t_p / (32 * units),
+        "speedup_vs_plain": t_p / t_l,
+        "judged": judged, "fallbacks": sum(r.fallbacks for r in reps),
+        "judged_mean_density_dev": sum(r.sum_density_dev for r in reps) / max(judged, 1),
+        "judged_max_density_dev": max((r.max_density_dev for r in reps), default=0.0),
+        "end_state_mean_density_dev": float(np.mean(np.abs(rl - rp) / rp)),
+        "precision": "BF16 weights/activations, FP32 accumulate (mma.sync m16n8k16)",
+        "weights": str(WEIGHTS.relative_to(REPO)),
+    })
+    return out
+
+
 def run_ours(args) -> None:
     import torch
     import nprsph as S
@@ -311,6 +378,7 @@ def run_ours(args) -> None:
     if rank != 0:
         return
     extra = extra_workloads(args, stream) if args.extra_steps > 0 else {}
+    learned = learned_workload(args, stream, flush) if args.learned else {"skipped": "--no-learned"}
     peaks, src = measured_peaks()
     hbm = float(peaks["hbm_gbs"])
     value = world * n * args.steps / total_s
@@ -347,6 +415,7 @@ def run_ours(args) -> None:
         "clocks": clk.summary(),
         "final_state": {"mean_rho": diag.mean_rho, "nonfinite": int(diag.nonfinite), "step": int(diag.step)},
         "other_configs": extra,
+        "learned": learned,
     }
     print(json.dumps(line), flush=True)
     if world > 1:
@@ -364,6 +433,8 @@ def main() -> None:
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample length (0: skip)")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="keep the default launch shape instead of timing the candidates first")
+    ap.add_argument("--no-learned", dest="learned", action="store_false",
+                    help="skip the learned macro-step measurement")
     ap.add_argument("--extra-steps", type=int, default=100,
                     help="steps of the batched-scenes and 10k reference-scene measurements (0: skip)")
     args = ap.parse_args()

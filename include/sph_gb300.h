@@ -238,6 +238,13 @@ sph_status sph_mpnn_loss_grad(sph_mpnn* net, uint32_t n, const float* pos4, cons
                               const float* rhop2, const int32_t* nb, const int32_t* cnt,
                               const float* target4, const float fc[5], double* loss, float* out4,
                               float* grad);
+/* Network output (velocity change / c, n x 4) of a host frame as above: precision 1 runs the
+ * BF16 tensor-core inference kernels (the macro-step's path), 0 the FP32 training forward. */
+sph_status sph_mpnn_forward(sph_mpnn* net, uint32_t n, const float* pos4, const float* vel4,
+                            const float* rhop2, const int32_t* nb, const int32_t* cnt, const float fc[5],
+                            int32_t precision, float* out4);
+/* Precision of sph_learned_step: 1 BF16 tensor cores (default), 0 FP32 CUDA cores. */
+sph_status sph_mpnn_set_precision(sph_mpnn* net, int32_t precision);
 /* Record n_frames frames of every scene of ctx (created with SPH_FLAG_KEEP_FORCE): the state,
  * its neighbour lists and density, and as target the velocity change of the next 4 plain
  * steps from the forces alone. Advances ctx by 4 * n_frames steps. */

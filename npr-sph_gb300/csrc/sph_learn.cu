@@ -21,6 +21,7 @@
 #include "sph_ctx.h"
 #include "sph_device.cuh"
 #include "sph_mpnn.h"
+#include <cuda_bf16.h>
 
 using namespace sphgb;
 using sphgb::engine::fail;
@@ -50,6 +51,13 @@ struct sph_mpnn {
     int hcap = 0;
     void* harena = nullptr;
     int adam_t = 0;  // Adam steps taken since the parameters were last set
+    // BF16 tensor-core inference
+    int precision = 1;               // 1: BF16 tensor cores (default), 0: FP32 CUDA cores
+    uint32_t* frags = nullptr;       // parameters in MMA fragment order
+    bool frags_dirty = true;
+    __nv_bfloat16* H1b = nullptr;    // [n][64]
+    uint16_t* Pperm = nullptr;       // [n][64], permuted
+    int bcap = 0;
 };
 
 namespace {
@@ -177,12 +185,14 @@ __global__ void __launch_bounds__(kT) k_frame_copy(const float4* __restrict__ po
     fvel[k] = vel_s[s];
     frhop[k] = rhop[s];
     fid[k] = id_of(vel_s[s]);
-    const int c = cnt[s];
-    fcnt[k] = c;
-    for (int q = 0; q < M::K; ++q) {
+    const int c = min(max(cnt[s], 0), M::K);
+    int w = 0;  // neighbours are in the same scene; anything else is dropped, never passed on
+    for (int q = 0; q < c; ++q) {
         const int j = nb[(size_t)s * M::K + q];
-        fnb[(size_t)k * M::K + q] = (q < c && j >= first && j < first + m) ? j - first : -1;
+        if (j >= first && j < first + m) fnb[(size_t)k * M::K + w++] = j - first;
     }
+    for (int q = w; q < M::K; ++q) fnb[(size_t)k * M::K + q] = -1;
+    fcnt[k] = w;
 }
 
 __global__ void __launch_bounds__(kT) k_frame_target(const int* __restrict__ fid, const float4* __restrict__ acc,
@@ -289,6 +299,28 @@ sph_status refresh_density(sph_ctx* ctx) {
     return SPH_OK;
 }
 
+// Fragment-ordered parameters and the BF16 activations for n particles.
+sph_status ensure_bf16(sph_mpnn* net, int n, cudaStream_t st) {
+    if (!net->frags) {
+        NCK(cudaMalloc(&net->frags, sizeof(uint32_t) * M::infer_frag_words()));
+        net->frags_dirty = true;
+    }
+    if (n > net->bcap) {
+        if (net->H1b) cudaFree(net->H1b);
+        if (net->Pperm) cudaFree(net->Pperm);
+        net->H1b = nullptr;
+        net->Pperm = nullptr;
+        NCK(cudaMalloc(&net->H1b, sizeof(__nv_bfloat16) * (size_t)n * M::W));
+        NCK(cudaMalloc(&net->Pperm, sizeof(uint16_t) * (size_t)n * M::W));
+        net->bcap = n;
+    }
+    if (net->frags_dirty) {
+        M::infer_prep(M::trainer_params(net->tr), net->frags, st);
+        net->frags_dirty = false;
+    }
+    return SPH_OK;
+}
+
 // One learned macro-step on ctx (4*dt).
 sph_status learned_macro(sph_ctx* ctx, sph_mpnn* net) {
     const int n = ctx->b.n;
@@ -296,10 +328,16 @@ sph_status learned_macro(sph_ctx* ctx, sph_mpnn* net) {
     launch_nb_density(ctx, net->nb, net->cnt);
     M::Frame f{ctx->b.pos_s, ctx->b.vel_s, ctx->b.rhop, net->nb, net->cnt, nullptr, n, frame_const(ctx->s0)};
     f.fc.log_mu = (float)(std::log10((double)ctx->params[0].visc) / 4.0);
-    M::trainer_forward(net->inf, f, ctx->stream);
-    k_macro_integrate<<<nblk(n), kT, 0, ctx->stream>>>(ctx->b.pos_s, ctx->b.vel_s, M::trainer_out(net->inf), ctx->s0,
-                                                       f.fc.c, ctx->b.pos, ctx->b.vel, ctx->b.key, ctx->b.rank,
-                                                       ctx->b.count, n);
+    if (net->precision == 1) {
+        M::infer_round1(f, net->frags, net->H1b, net->Pperm, ctx->stream);
+        M::infer_round2(f, net->frags, M::trainer_params(net->tr), net->H1b, net->Pperm, ctx->s0, ctx->b.pos,
+                        ctx->b.vel, nullptr, ctx->b.key, ctx->b.rank, ctx->b.count, true, ctx->stream);
+    } else {
+        M::trainer_forward(net->inf, f, ctx->stream);
+        k_macro_integrate<<<nblk(n), kT, 0, ctx->stream>>>(ctx->b.pos_s, ctx->b.vel_s, M::trainer_out(net->inf),
+                                                           ctx->s0, f.fc.c, ctx->b.pos, ctx->b.vel, ctx->b.key,
+                                                           ctx->b.rank, ctx->b.count, n);
+    }
     ctx->need_hash = false;  // the integrate hashed the new positions
     ctx->steps += 4;
     ctx->stepped = true;
@@ -344,7 +382,8 @@ sph_status sph_mpnn_destroy(sph_mpnn* net) {
     if (net->inf) M::trainer_delete(net->inf);
     for (auto& r : net->frames) cudaFree(r.arena);
     void* ptrs[] = {net->nb, net->cnt, net->snap_pos, net->snap_vel, net->snap_rhop, net->l_pos, net->l_vel,
-                    net->l_rhop, net->acc, net->rho_l, net->rho_p, net->vel_l, net->vel_p, net->cmp, net->harena};
+                    net->l_rhop, net->acc, net->rho_l, net->rho_p, net->vel_l, net->vel_p, net->cmp, net->harena,
+                    net->frags, net->H1b, net->Pperm};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (net->own_stream) cudaStreamDestroy(net->stream);
@@ -363,6 +402,7 @@ sph_status sph_mpnn_set_params(sph_mpnn* net, const float* params, uint32_t n) {
                             net->stream));
     M::trainer_reset_adam(net->tr);
     net->adam_t = 0;
+    net->frags_dirty = true;
     NCK(cudaStreamSynchronize(net->stream));
     return SPH_OK;
 }
@@ -415,6 +455,64 @@ sph_status sph_mpnn_loss_grad(sph_mpnn* net, uint32_t n, const float* pos4, cons
     if (loss) *loss = l;
     if (out4) NCK(cudaMemcpyAsync(out4, M::trainer_out(net->tr), (size_t)n * 16, cudaMemcpyDeviceToHost, st));
     if (grad) NCK(cudaMemcpyAsync(grad, M::trainer_grad(net->tr), sizeof(float) * M::kParams, cudaMemcpyDeviceToHost, st));
+    NCK(cudaStreamSynchronize(st));
+    NCK(cudaGetLastError());
+    return SPH_OK;
+}
+
+sph_status sph_mpnn_set_precision(sph_mpnn* net, int32_t precision) {
+    if (!net || (precision != 0 && precision != 1)) return SPH_ERR_INVALID_ARG;
+    net->precision = precision;
+    return SPH_OK;
+}
+
+sph_status sph_mpnn_forward(sph_mpnn* net, uint32_t n, const float* pos4, const float* vel4, const float* rhop2,
+                            const int32_t* nb, const int32_t* cnt, const float fc[5], int32_t precision, float* out4) {
+    if (!net || !pos4 || !vel4 || !rhop2 || !nb || !cnt || !fc || !out4 || n == 0) return SPH_ERR_INVALID_ARG;
+    if (precision != 0 && precision != 1) return SPH_ERR_INVALID_ARG;
+    if ((int)n > M::trainer_capacity(net->tr)) { net->err = "frame larger than the training workspace"; return SPH_ERR_CAPACITY; }
+    for (uint32_t i = 0; i < n; ++i) {
+        if (cnt[i] < 0 || cnt[i] > M::K) { net->err = "neighbour count out of [0, 32]"; return SPH_ERR_INVALID_ARG; }
+        for (int q = 0; q < cnt[i]; ++q)
+            if (nb[(size_t)i * M::K + q] < 0 || nb[(size_t)i * M::K + q] >= (int)n) {
+                net->err = "neighbour index out of range";
+                return SPH_ERR_INVALID_ARG;
+            }
+    }
+    NCK(cudaSetDevice(net->device));
+    const size_t bytes = (size_t)n * (16 + 16 + 8 + 16 + 4) + (size_t)n * M::K * 4;
+    if ((int)n > net->hcap) {
+        if (net->harena) cudaFree(net->harena);
+        net->harena = nullptr;
+        NCK(cudaMalloc(&net->harena, bytes));
+        net->hcap = (int)n;
+    }
+    char* a = (char*)net->harena;
+    float4* dpos = (float4*)a; a += (size_t)n * 16;
+    float4* dvel = (float4*)a; a += (size_t)n * 16;
+    float4* dout = (float4*)a; a += (size_t)n * 16;
+    float2* drh = (float2*)a; a += (size_t)n * 8;
+    int* dcnt = (int*)a; a += (size_t)n * 4;
+    int* dnb = (int*)a;
+    cudaStream_t st = net->stream;
+    NCK(cudaMemcpyAsync(dpos, pos4, (size_t)n * 16, cudaMemcpyHostToDevice, st));
+    NCK(cudaMemcpyAsync(dvel, vel4, (size_t)n * 16, cudaMemcpyHostToDevice, st));
+    NCK(cudaMemcpyAsync(drh, rhop2, (size_t)n * 8, cudaMemcpyHostToDevice, st));
+    NCK(cudaMemcpyAsync(dcnt, cnt, (size_t)n * 4, cudaMemcpyHostToDevice, st));
+    NCK(cudaMemcpyAsync(dnb, nb, (size_t)n * M::K * 4, cudaMemcpyHostToDevice, st));
+    M::Frame f{dpos, dvel, drh, dnb, dcnt, nullptr, (int)n, {fc[0], fc[1], fc[2], fc[3], fc[4]}};
+    if (precision == 1) {
+        sph_status s2 = ensure_bf16(net, (int)n, st);
+        if (s2) return s2;
+        SceneDev S{};
+        M::infer_round1(f, net->frags, net->H1b, net->Pperm, st);
+        M::infer_round2(f, net->frags, M::trainer_params(net->tr), net->H1b, net->Pperm, S, nullptr, nullptr, dout,
+                        nullptr, nullptr, nullptr, false, st);
+        NCK(cudaMemcpyAsync(out4, dout, (size_t)n * 16, cudaMemcpyDeviceToHost, st));
+    } else {
+        M::trainer_forward(net->tr, f, st);
+        NCK(cudaMemcpyAsync(out4, M::trainer_out(net->tr), (size_t)n * 16, cudaMemcpyDeviceToHost, st));
+    }
     NCK(cudaStreamSynchronize(st));
     NCK(cudaGetLastError());
     return SPH_OK;
@@ -502,6 +600,7 @@ sph_status sph_mpnn_train(sph_mpnn* net, uint32_t steps, float lr, uint64_t seed
         M::trainer_adam(net->tr, ++net->adam_t, lr, net->stream);
         if (loss_per_step) loss_per_step[s] = (float)l;
     }
+    net->frags_dirty = true;
     NCK(cudaStreamSynchronize(net->stream));
     NCK(cudaGetLastError());
     if (net->inf)
@@ -527,7 +626,7 @@ sph_status sph_learned_step(sph_ctx* ctx, sph_mpnn* net, int32_t n_macro, int32_
     if (n_macro < 0 || judge_every < 0) return fail(ctx, SPH_ERR_INVALID_ARG, "negative count");
     cudaSetDevice(ctx->device);
     const int n = ctx->b.n;
-    if (!net->inf || M::trainer_capacity(net->inf) < n) {
+    if (net->precision == 0 && (!net->inf || M::trainer_capacity(net->inf) < n)) {
         if (net->inf) M::trainer_delete(net->inf);
         net->inf = M::trainer_new(n, false);
         if (!net->inf) return fail(ctx, SPH_ERR_OUT_OF_MEMORY, "network workspace");
@@ -536,6 +635,7 @@ sph_status sph_learned_step(sph_ctx* ctx, sph_mpnn* net, int32_t n_macro, int32_
             return fail(ctx, SPH_ERR_CUDA, "copy of the network parameters");
     }
     sph_status st = ensure_ctx_scratch(net, n);
+    if (!st && net->precision == 1) st = ensure_bf16(net, n, ctx->stream);
     if (st) return fail(ctx, st, net->err);
     sph_learned_report r{};
     int plain_left = 0;

@@ -68,8 +68,8 @@ __global__ void __launch_bounds__(kT) k_edge1_fwd(Frame f, const float* __restri
     for (int k = 0; k < K; ++k) {
         float e[FE];
         unsigned long long bits = 0ull;
-        if (k < cnt) {
-            const int j = f.nb[i * K + k];
+        const int j = k < cnt ? f.nb[i * K + k] : -1;
+        if (j >= 0 && j < f.n) {
             edge_feat(pi, vi, f.pos[j], f.vel[j], f.fc, e);
 #pragma unroll
             for (int o = 0; o < W; ++o) {
@@ -111,8 +111,8 @@ __global__ void __launch_bounds__(kT) k_edge2_fwd(Frame f, const float* __restri
     for (int o = 0; o < W; ++o) m[o] = 0.0f;
     for (int k = 0; k < K; ++k) {
         unsigned long long bits = 0ull;
-        if (k < cnt) {
-            const int j = f.nb[i * K + k];
+        const int j = k < cnt ? f.nb[i * K + k] : -1;
+        if (j >= 0 && j < f.n) {
             float e[FE];
 #pragma unroll
             for (int q = 0; q < FE; ++q) e[q] = E[((size_t)i * K + k) * FE + q];
@@ -250,7 +250,8 @@ __global__ void __launch_bounds__(kT) k_rev_count(const int* __restrict__ nb, co
     const long long r = (long long)blockIdx.x * kT + threadIdx.x;
     if (r >= (long long)n * K) return;
     const int i = (int)(r / K), e = (int)(r % K);
-    if (e < cnt[i]) atomicAdd(&rc[nb[r]], 1);
+    const int j = e < cnt[i] ? nb[r] : -1;
+    if (j >= 0 && j < n) atomicAdd(&rc[j], 1);
 }
 
 // Exclusive scan of rc[0, n) into off[0, n] by one CTA of 1024 threads (frames are small).
@@ -278,8 +279,8 @@ __global__ void __launch_bounds__(kT) k_rev_fill(const int* __restrict__ nb, con
     const long long r = (long long)blockIdx.x * kT + threadIdx.x;
     if (r >= (long long)n * K) return;
     const int i = (int)(r / K), e = (int)(r % K);
-    if (e >= cnt[i]) return;
-    const int j = nb[r];
+    const int j = e < cnt[i] ? nb[r] : -1;
+    if (j < 0 || j >= n) return;
     edges[off[j] + atomicAdd(&cur[j], 1)] = (int)r;
 }
 

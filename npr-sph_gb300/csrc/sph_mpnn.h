@@ -13,7 +13,10 @@
 #pragma once
 
 #include <cstdint>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
+
+#include "sph_internal.h"
 
 namespace sphgb {
 namespace mpnn {
@@ -72,6 +75,18 @@ void trainer_reset_adam(Trainer* t);
 void trainer_forward(Trainer* t, const Frame& f, cudaStream_t st);
 double trainer_loss_grad(Trainer* t, const Frame& f, cudaStream_t st);  // synchronous (reads the loss)
 void trainer_adam(Trainer* t, int step, float lr, cudaStream_t st);
+
+// BF16 tensor-core inference (sph_mpnn_infer.cu). `frags` (infer_frag_words() u32) holds the
+// parameters in MMA fragment order, rebuilt by infer_prep whenever the parameters change.
+int infer_frag_words();
+void infer_prep(const float* prm, uint32_t* frags, cudaStream_t st);
+// H1 and P (permuted) for all particles of f; bf16 [n][64] each.
+void infer_round1(const Frame& f, const uint32_t* frags, __nv_bfloat16* H1, uint16_t* Pperm, cudaStream_t st);
+// Round 2 and the output O (written to `out` if non-null); with `integrate` the macro-step
+// update of f's state into (pos_out, vel_out) and the cell hash of the new positions.
+void infer_round2(const Frame& f, const uint32_t* frags, const float* prm, const __nv_bfloat16* H1,
+                  const uint16_t* Pperm, const SceneDev& S, float4* pos_out, float4* vel_out, float4* out, int* key,
+                  int* rank, int* count, bool integrate, cudaStream_t st);
 
 }  // namespace mpnn
 }  // namespace sphgb

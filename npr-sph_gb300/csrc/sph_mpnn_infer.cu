@@ -1,0 +1,418 @@
+// sph_mpnn_infer.cu -- inference of the learned macro-step network on BF16
+// tensor cores (mma.sync m16n8k16, FP32 accumulate), the path that runs at
+// scale. The network is the one of sph_mpnn.h; the FP32 kernels of
+// sph_mpnn.cu are its reference.
+//
+// Two kernels, one warp per tile of 16 particles (sorted order):
+//   k_infer_r1  per particle: edge features of its <= 32 neighbours, the
+//               round-1 edge layer as Z^T = We1^T E^T (features on the MMA M
+//               side, 4 tiles of 16; edges on N, 4 tiles of 8), relu and the
+//               edge sum inside the lane plus two shuffles -> M1 in a shared
+//               tile; per 16 particles: H1 = relu([M1 n 1] Wn1'), P = H1 Wp
+//               (H1 is reused from the accumulator registers as the A operand).
+//   k_infer_r2  round 2 likewise, with the gathered P_j as the accumulator's
+//               initial value; per 16 particles: H2 = relu([M2 H1 1] Wn2'),
+//               O = H2 Wo + bo, then the macro-step integrate and cell hash.
+// Biases ride on a constant-1 feature column, so padded edges (all features
+// zero) contribute exactly zero, as in the reference.
+// P is stored permuted: for particle j, lane group g reads the 8 features
+// {16 m + g + 8 r} it needs as one 16-byte load.
+#include <cuda_bf16.h>
+
+#include "sph_device.cuh"
+#include "sph_mpnn.h"
+
+namespace sphgb {
+namespace mpnn {
+
+namespace {
+
+constexpr int kWarps = 4;
+constexpr int kThreads = kWarps * 32;
+constexpr int kTile = 16;         // particles per warp tile
+constexpr int kLd1 = 88;          // X1 tile row stride (80 used), bf16
+constexpr int kLd2 = 152;         // X2 tile row stride (144 used), bf16
+constexpr int kK1 = 80, kK2 = 144; // padded K of the two node layers (bias column at 72 / 128)
+
+// Fragment-ordered weights (u32 = 2 x bf16), built by k_prep_frags.
+constexpr int kFragWe1 = 0;                          // [4 mt][32 lanes][4]
+constexpr int kFragWe2 = kFragWe1 + 4 * 32 * 4;      // [4 mt][32][4]
+constexpr int kFragWn1 = kFragWe2 + 4 * 32 * 4;      // [5 kt][8 nt][32][2]
+constexpr int kFragWp = kFragWn1 + 5 * 8 * 32 * 2;   // [4 kt][8 nt][32][2]
+constexpr int kFragWn2 = kFragWp + 4 * 8 * 32 * 2;   // [9 kt][8 nt][32][2]
+constexpr int kFragWo = kFragWn2 + 9 * 8 * 32 * 2;   // [4 kt][32][2]
+constexpr int kFragTotal = kFragWo + 4 * 32 * 2;
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t*>(&v);
+}
+__device__ __forceinline__ float bf16_lo(uint32_t u) { return __uint_as_float(u << 16); }
+__device__ __forceinline__ float bf16_hi(uint32_t u) { return __uint_as_float(u & 0xffff0000u); }
+
+__device__ __forceinline__ void mma(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// Weight matrix element (row k, column o) of a layer with a bias row at `brow`, zero padded.
+__device__ __forceinline__ float wel(const float* Wm, int kin, int nout, const float* b, int brow, int k, int o) {
+    if (o >= nout) return 0.0f;
+    if (k < kin) return Wm[k * nout + o];
+    if (k == brow && b) return b[o];
+    return 0.0f;
+}
+
+__global__ void k_prep_frags(const float* __restrict__ prm, uint32_t* __restrict__ fr) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= kFragTotal) return;
+    int r = t;
+    if (r < kFragWn1) {  // edge layers, transposed: A[o][k] = W[k][o]; bias row 8
+        const bool second = r >= kFragWe2;
+        if (second) r -= kFragWe2;
+        const float* Wm = prm + (second ? kWe2 : kWe1);
+        const float* b = prm + (second ? kBe2 : kBe1);
+        const int mt = r / 128, lane = (r / 4) % 32, q = r % 4;
+        const int g = lane >> 2, tq = lane & 3;
+        const int o = mt * 16 + g + ((q & 1) ? 8 : 0);
+        const int k = 2 * tq + ((q & 2) ? 8 : 0);
+        fr[t] = pack_bf16(wel(Wm, FE, W, b, 8, k, o), wel(Wm, FE, W, b, 8, k + 1, o));
+        return;
+    }
+    // node layers: B[k][o], b0 rows k0, k0+1; b1 rows k0+8, k0+9
+    const float *Wm, *b;
+    int kin, nout, brow, base;
+    if (r < kFragWp) { Wm = prm + kWn1; b = prm + kBn1; kin = W + FN; nout = W; brow = 72; base = kFragWn1; }
+    else if (r < kFragWn2) { Wm = prm + kWp; b = nullptr; kin = W; nout = W; brow = -1; base = kFragWp; }
+    else if (r < kFragWo) { Wm = prm + kWn2; b = prm + kBn2; kin = 2 * W; nout = W; brow = 128; base = kFragWn2; }
+    else { Wm = prm + kWo; b = nullptr; kin = W; nout = FO; brow = -1; base = kFragWo; }
+    r -= base;
+    const int ntiles = (base == kFragWo) ? 1 : 8;
+    const int q = r % 2, lane = (r / 2) % 32, nt = (r / 64) % ntiles, kt = r / (64 * ntiles);
+    const int g = lane >> 2, tq = lane & 3;
+    const int o = nt * 8 + g;
+    const int k = kt * 16 + 2 * tq + (q ? 8 : 0);
+    fr[t] = pack_bf16(wel(Wm, kin, nout, b, brow, k, o), wel(Wm, kin, nout, b, brow, k + 1, o));
+}
+
+// Edge features 2t, 2t+1 of the edge (i -> j) as bf16x2 (B fragment row pair), and the bias pair.
+__device__ __forceinline__ void edge_b(float4 pi, float4 vi, float4 pj, float4 vj, float ih, float ic, int tq,
+                                       bool valid, uint32_t& b0, uint32_t& b1) {
+    const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+    float f0, f1;
+    if (tq == 0) { f0 = dx * ih; f1 = dy * ih; }
+    else if (tq == 1) { f0 = dz * ih; f1 = (vj.x - vi.x) * ic; }
+    else if (tq == 2) { f0 = (vj.y - vi.y) * ic; f1 = (vj.z - vi.z) * ic; }
+    else { const float r = sqrtf(dx * dx + dy * dy + dz * dz) * ih; f0 = r; f1 = 1.0f - r; }
+    b0 = valid ? pack_bf16(f0, f1) : 0u;
+    b1 = (valid && tq == 0) ? pack_bf16(1.0f, 0.0f) : 0u;
+}
+
+struct EdgeFrags {
+    uint32_t a[4][4];  // [mt][reg]
+};
+
+// Round-1/2 edge layer of particle i: returns the per-lane sums over edges of relu(Z) for the
+// features (16 mt + g, 16 mt + g + 8), already reduced over the lane quad (all tq hold them).
+template <bool ROUND2>
+__device__ __forceinline__ void edge_layer(const EdgeFrags& A, int i, const float4* __restrict__ pos,
+                                           const float4* __restrict__ vel, const int* __restrict__ nb, int cnt,
+                                           float ih, float ic, const uint4* __restrict__ Pperm, float (&s)[4][2]) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
+    const float4 pi = pos[i], vi = vel[i];
+#pragma unroll
+    for (int mt = 0; mt < 4; ++mt) s[mt][0] = s[mt][1] = 0.0f;
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) {
+        if (nt * 8 >= cnt) break;  // warp-uniform: cnt is the particle's
+        const int e = nt * 8 + g;
+        const bool valid = e < cnt;
+        const int j = valid ? nb[(size_t)i * K + e] : i;
+        uint32_t b0, b1;
+        edge_b(pi, vi, pos[j], vel[j], ih, ic, tq, valid, b0, b1);
+        float c[4][4];
+        if constexpr (ROUND2) {
+            // accumulator starts at P_j for the two edge columns 2tq, 2tq+1 of this n-tile
+            const int e0 = nt * 8 + 2 * tq, e1 = e0 + 1;
+            uint4 p0 = make_uint4(0, 0, 0, 0), p1 = make_uint4(0, 0, 0, 0);
+            if (e0 < cnt) p0 = Pperm[(size_t)nb[(size_t)i * K + e0] * 8 + g];
+            if (e1 < cnt) p1 = Pperm[(size_t)nb[(size_t)i * K + e1] * 8 + g];
+            const uint32_t w0[4] = {p0.x, p0.y, p0.z, p0.w}, w1[4] = {p1.x, p1.y, p1.z, p1.w};
+#pragma unroll
+            for (int mt = 0; mt < 4; ++mt) {  // chunk word mt holds features (16 mt + g, 16 mt + g + 8)
+                c[mt][0] = bf16_lo(w0[mt]);
+                c[mt][1] = bf16_lo(w1[mt]);
+                c[mt][2] = bf16_hi(w0[mt]);
+                c[mt][3] = bf16_hi(w1[mt]);
+            }
+        } else {
+#pragma unroll
+            for (int mt = 0; mt < 4; ++mt) c[mt][0] = c[mt][1] = c[mt][2] = c[mt][3] = 0.0f;
+        }
+#pragma unroll
+        for (int mt = 0; mt < 4; ++mt) {
+            mma(c[mt], A.a[mt], b0, b1);
+            s[mt][0] += fmaxf(c[mt][0], 0.0f) + fmaxf(c[mt][1], 0.0f);
+            s[mt][1] += fmaxf(c[mt][2], 0.0f) + fmaxf(c[mt][3], 0.0f);
+        }
+    }
+#pragma unroll
+    for (int mt = 0; mt < 4; ++mt)
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            s[mt][r] += __shfl_xor_sync(0xffffffffu, s[mt][r], 1);
+            s[mt][r] += __shfl_xor_sync(0xffffffffu, s[mt][r], 2);
+        }
+}
+
+// A fragment of k-tile kt from a bf16 smem tile with row stride ld (16 rows).
+__device__ __forceinline__ void load_a(const __nv_bfloat16* X, int ld, int kt, uint32_t (&a)[4]) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
+    const uint32_t* r0 = reinterpret_cast<const uint32_t*>(X + g * ld + kt * 16 + 2 * tq);
+    const uint32_t* r1 = reinterpret_cast<const uint32_t*>(X + (g + 8) * ld + kt * 16 + 2 * tq);
+    a[0] = r0[0];
+    a[1] = r1[0];
+    a[2] = r0[4];
+    a[3] = r1[4];
+}
+
+// D[16 x 64] = X (16 x 16*KT, smem) * B (frags) ; d[nt][4]
+template <int KT>
+__device__ __forceinline__ void node_gemm(const __nv_bfloat16* X, int ld, const uint2* __restrict__ Bf, float (&d)[8][4]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) d[nt][0] = d[nt][1] = d[nt][2] = d[nt][3] = 0.0f;
+#pragma unroll
+    for (int kt = 0; kt < KT; ++kt) {
+        uint32_t a[4];
+        load_a(X, ld, kt, a);
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) {
+            const uint2 b = __ldg(Bf + (kt * 8 + nt) * 32 + lane);
+            mma(d[nt], a, b.x, b.y);
+        }
+    }
+}
+
+// Write 8 feature sums (or zeros) of particle row p into a tile: lanes tq == 0 own them.
+__device__ __forceinline__ void put_m(__nv_bfloat16* X, int ld, int p, const float (&s)[4][2], float scale) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
+    if (tq != 0) return;
+#pragma unroll
+    for (int mt = 0; mt < 4; ++mt) {
+        X[p * ld + mt * 16 + g] = __float2bfloat16_rn(s[mt][0] * scale);
+        X[p * ld + mt * 16 + g + 8] = __float2bfloat16_rn(s[mt][1] * scale);
+    }
+}
+
+__device__ __forceinline__ void load_edge_frags(const uint32_t* __restrict__ fr, int base, EdgeFrags& A) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int mt = 0; mt < 4; ++mt) {
+        const uint4 v = __ldg(reinterpret_cast<const uint4*>(fr + base) + mt * 32 + lane);
+        A.a[mt][0] = v.x; A.a[mt][1] = v.y; A.a[mt][2] = v.z; A.a[mt][3] = v.w;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_infer_r1(const float4* __restrict__ pos, const float4* __restrict__ vel,
+                                                      const float2* __restrict__ rhop, const int* __restrict__ nb,
+                                                      const int* __restrict__ cnt, FrameConst fc, int n,
+                                                      const uint32_t* __restrict__ fr,
+                                                      __nv_bfloat16* __restrict__ H1out, uint16_t* __restrict__ Pperm) {
+    __shared__ __align__(16) __nv_bfloat16 xs[kWarps][kTile * kLd1];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
+    __nv_bfloat16* X = xs[warp];
+    EdgeFrags A;
+    load_edge_frags(fr, kFragWe1, A);
+    const float ih = 1.0f / fc.h, ic = 1.0f / fc.c;
+    const int ntiles = (n + kTile - 1) / kTile;
+    for (int tile = blockIdx.x * kWarps + warp; tile < ntiles; tile += gridDim.x * kWarps) {
+        const int base = tile * kTile;
+        for (int p = 0; p < kTile; ++p) {
+            const int i = base + p;
+            float s[4][2];
+            if (i < n) {
+                const int c = min(max(cnt[i], 0), K);
+                edge_layer<false>(A, i, pos, vel, nb, c, ih, ic, nullptr, s);
+                put_m(X, kLd1, p, s, 1.0f / K);
+                if (lane < 16) {  // node features, bias column, padding (columns 64 .. 79)
+                    float v = 0.0f;
+                    const float4 vi = vel[i];
+                    const float rho = rhop[i].x;
+                    switch (lane) {
+                        case 0: v = vi.x * ic; break;
+                        case 1: v = vi.y * ic; break;
+                        case 2: v = vi.z * ic; break;
+                        case 3: v = rho / fc.rho_self - 1.0f; break;
+                        case 4: v = (rho - fc.rho0) / fc.rho_self; break;
+                        case 5: v = fc.log_mu; break;
+                        case 6: v = (float)c / K; break;
+                        case 7: v = 1.0f; break;
+                        case 8: v = 1.0f; break;  // bias column 72
+                        default: v = 0.0f;
+                    }
+                    X[p * kLd1 + 64 + lane] = __float2bfloat16_rn(v);
+                }
+            } else {
+                for (int q = lane; q < kK1; q += 32) X[p * kLd1 + q] = __float2bfloat16_rn(0.0f);
+            }
+        }
+        __syncwarp();
+        float d[8][4];
+        node_gemm<5>(X, kLd1, reinterpret_cast<const uint2*>(fr + kFragWn1), d);
+        // H1 = relu(Y1): store, and reuse as the A operand of P = H1 Wp
+        uint32_t ha[4][4];
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) {
+            const float h0 = fmaxf(d[nt][0], 0.f), h1 = fmaxf(d[nt][1], 0.f), h2 = fmaxf(d[nt][2], 0.f),
+                        h3 = fmaxf(d[nt][3], 0.f);
+            const uint32_t lo = pack_bf16(h0, h1), hi = pack_bf16(h2, h3);
+            const int kt = nt >> 1, half = nt & 1;
+            ha[kt][half ? 2 : 0] = lo;
+            ha[kt][half ? 3 : 1] = hi;
+            const int r0 = base + g, r1 = base + g + 8, col = nt * 8 + 2 * tq;
+            if (r0 < n) *reinterpret_cast<uint32_t*>(H1out + (size_t)r0 * W + col) = lo;
+            if (r1 < n) *reinterpret_cast<uint32_t*>(H1out + (size_t)r1 * W + col) = hi;
+        }
+        float pd[8][4];
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) pd[nt][0] = pd[nt][1] = pd[nt][2] = pd[nt][3] = 0.0f;
+#pragma unroll
+        for (int kt = 0; kt < 4; ++kt)
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt) {
+                const uint2 b = __ldg(reinterpret_cast<const uint2*>(fr + kFragWp) + (kt * 8 + nt) * 32 + lane);
+                mma(pd[nt], ha[kt], b.x, b.y);
+            }
+        // P permuted: feature f = 16 m + gg + 8 r  ->  P[j][gg][m][r]
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                const int f = nt * 8 + 2 * tq + q;
+                const int gg = f & 7, m = f >> 4, rr = (f >> 3) & 1;
+                const int slot = gg * 8 + m * 2 + rr;
+                const int r0 = base + g, r1 = base + g + 8;
+                if (r0 < n) Pperm[(size_t)r0 * W + slot] = __bfloat16_as_ushort(__float2bfloat16_rn(pd[nt][q]));
+                if (r1 < n) Pperm[(size_t)r1 * W + slot] = __bfloat16_as_ushort(__float2bfloat16_rn(pd[nt][2 + q]));
+            }
+        __syncwarp();
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_infer_r2(const float4* __restrict__ pos, const float4* __restrict__ vel,
+                                                      const int* __restrict__ nb, const int* __restrict__ cnt,
+                                                      FrameConst fc, int n, const uint32_t* __restrict__ fr,
+                                                      const float* __restrict__ prm,
+                                                      const __nv_bfloat16* __restrict__ H1,
+                                                      const uint4* __restrict__ Pperm, SceneDev S,
+                                                      float4* __restrict__ pos_out, float4* __restrict__ vel_out,
+                                                      float4* __restrict__ out, int* __restrict__ key_out,
+                                                      int* __restrict__ rank_out, int* __restrict__ count,
+                                                      int integrate) {
+    __shared__ __align__(16) __nv_bfloat16 xs[kWarps][kTile * kLd2];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
+    __nv_bfloat16* X = xs[warp];
+    EdgeFrags A;
+    load_edge_frags(fr, kFragWe2, A);
+    const float ih = 1.0f / fc.h, ic = 1.0f / fc.c;
+    const float bo[3] = {prm[kBo], prm[kBo + 1], prm[kBo + 2]};
+    const int ntiles = (n + kTile - 1) / kTile;
+    for (int tile = blockIdx.x * kWarps + warp; tile < ntiles; tile += gridDim.x * kWarps) {
+        const int base = tile * kTile;
+        for (int p = 0; p < kTile; ++p) {
+            const int i = base + p;
+            float s[4][2];
+            if (i < n) {
+                const int c = min(max(cnt[i], 0), K);
+                edge_layer<true>(A, i, pos, vel, nb, c, ih, ic, Pperm, s);
+                put_m(X, kLd2, p, s, 1.0f / K);
+                // H1 row (columns 64 .. 127), bias column 128, padding to 143
+                reinterpret_cast<uint32_t*>(X + p * kLd2 + 64)[lane] =
+                    reinterpret_cast<const uint32_t*>(H1 + (size_t)i * W)[lane];
+                if (lane < 16) X[p * kLd2 + 128 + lane] = __float2bfloat16_rn(lane == 0 ? 1.0f : 0.0f);
+            } else {
+                for (int q = lane; q < kK2; q += 32) X[p * kLd2 + q] = __float2bfloat16_rn(0.0f);
+            }
+        }
+        __syncwarp();
+        float d[8][4];
+        node_gemm<9>(X, kLd2, reinterpret_cast<const uint2*>(fr + kFragWn2), d);
+        uint32_t ha[4][4];
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) {
+            const int kt = nt >> 1, half = nt & 1;
+            ha[kt][half ? 2 : 0] = pack_bf16(fmaxf(d[nt][0], 0.f), fmaxf(d[nt][1], 0.f));
+            ha[kt][half ? 3 : 1] = pack_bf16(fmaxf(d[nt][2], 0.f), fmaxf(d[nt][3], 0.f));
+        }
+        float o[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int kt = 0; kt < 4; ++kt) {
+            const uint2 b = __ldg(reinterpret_cast<const uint2*>(fr + kFragWo) + kt * 32 + lane);
+            mma(o, ha[kt], b.x, b.y);
+        }
+        // O rows g (o[0], o[1]) and g + 8 (o[2], o[3]), columns 2 tq, 2 tq + 1; column 2 sits in tq == 1
+        const float c2_r0 = __shfl_sync(0xffffffffu, o[0], (lane & ~3) | 1);
+        const float c2_r1 = __shfl_sync(0xffffffffu, o[2], (lane & ~3) | 1);
+        if (tq == 0) {
+#pragma unroll
+            for (int rr = 0; rr < 2; ++rr) {
+                const int i = base + g + rr * 8;
+                if (i >= n) continue;
+                const float O[3] = {(rr ? o[2] : o[0]) + bo[0], (rr ? o[3] : o[1]) + bo[1], (rr ? c2_r1 : c2_r0) + bo[2]};
+                if (out) out[i] = make_float4(O[0], O[1], O[2], 0.0f);
+                if (!integrate) continue;
+                const float4 pp = pos[i], vv = vel[i];
+                const float p3[3] = {pp.x, pp.y, pp.z}, v3[3] = {vv.x, vv.y, vv.z};
+                float np[3], nv[3];
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    const float dv = fc.c * O[a];
+                    nv[a] = v3[a] + dv;
+                    np[a] = p3[a] + 4.0f * S.dt * v3[a] + 2.5f * S.dt * dv;
+                    if (np[a] < S.lo[a]) { np[a] = S.lo[a]; nv[a] *= -S.damp; }  // integrate_comp.glsl:45-77
+                    else if (np[a] > S.up[a]) { np[a] = S.up[a]; nv[a] *= -S.damp; }
+                }
+                pos_out[i] = make_float4(np[0], np[1], np[2], pp.w);
+                vel_out[i] = make_float4(nv[0], nv[1], nv[2], vv.w);
+                const int k = cell_key(S, np[0], np[1], np[2]);
+                key_out[i] = k;
+                rank_out[i] = atomicAdd(&count[k], 1);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+}  // namespace
+
+int infer_frag_words() { return kFragTotal; }
+
+void infer_prep(const float* prm, uint32_t* frags, cudaStream_t st) {
+    k_prep_frags<<<(kFragTotal + 255) / 256, 256, 0, st>>>(prm, frags);
+}
+
+static int infer_grid(int n) {
+    const int tiles = (n + kTile - 1) / kTile;
+    const int blocks = (tiles + kWarps - 1) / kWarps;
+    const int cap = device_sm_count() * 8;
+    return blocks < cap ? (blocks < 1 ? 1 : blocks) : cap;
+}
+
+void infer_round1(const Frame& f, const uint32_t* frags, __nv_bfloat16* H1, uint16_t* Pperm, cudaStream_t st) {
+    k_infer_r1<<<infer_grid(f.n), kThreads, 0, st>>>(f.pos, f.vel, f.rhop, f.nb, f.cnt, f.fc, f.n, frags, H1, Pperm);
+}
+
+void infer_round2(const Frame& f, const uint32_t* frags, const float* prm, const __nv_bfloat16* H1,
+                  const uint16_t* Pperm, const SceneDev& S, float4* pos_out, float4* vel_out, float4* out, int* key,
+                  int* rank, int* count, bool integrate, cudaStream_t st) {
+    k_infer_r2<<<infer_grid(f.n), kThreads, 0, st>>>(f.pos, f.vel, f.nb, f.cnt, f.fc, f.n, frags, prm, H1,
+                                                     reinterpret_cast<const uint4*>(Pperm), S, pos_out, vel_out, out,
+                                                     key, rank, count, integrate ? 1 : 0);
+}
+
+}  // namespace mpnn
+}  // namespace sphgb

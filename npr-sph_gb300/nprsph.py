@@ -113,6 +113,8 @@ _SIGS = {
     "sph_mpnn_set_params": (C.c_int32, [_P, _P, C.c_uint32]),
     "sph_mpnn_get_params": (C.c_int32, [_P, _P, C.c_uint32]),
     "sph_mpnn_loss_grad": (C.c_int32, [_P, C.c_uint32, _P, _P, _P, _P, _P, _P, _P, C.POINTER(C.c_double), _P, _P]),
+    "sph_mpnn_forward": (C.c_int32, [_P, C.c_uint32, _P, _P, _P, _P, _P, _P, C.c_int32, _P]),
+    "sph_mpnn_set_precision": (C.c_int32, [_P, C.c_int32]),
     "sph_mpnn_record": (C.c_int32, [_P, _P, C.c_uint32, C.POINTER(C.c_uint32)]),
     "sph_mpnn_clear_frames": (C.c_int32, [_P]),
     "sph_mpnn_train": (C.c_int32, [_P, C.c_uint32, C.c_float, C.c_uint64, _P]),
@@ -373,6 +375,18 @@ class Net:
         self._check(lib.sph_mpnn_loss_grad(self._h, n, *[a.ctypes.data for a in arrs], C.byref(loss), out.ctypes.data,
                                            grad.ctypes.data))
         return loss.value, out, grad
+
+    def forward(self, pos4, vel4, rhop2, nb, cnt, fc, precision: int = 1) -> np.ndarray:
+        n = len(pos4)
+        arrs = [np.ascontiguousarray(x, dtype=t) for x, t in
+                ((pos4, np.float32), (vel4, np.float32), (rhop2, np.float32), (nb, np.int32), (cnt, np.int32),
+                 (fc, np.float32))]
+        out = np.zeros((n, 4), dtype=np.float32)
+        self._check(lib.sph_mpnn_forward(self._h, n, *[a.ctypes.data for a in arrs], precision, out.ctypes.data))
+        return out
+
+    def set_precision(self, precision: int) -> None:
+        self._check(lib.sph_mpnn_set_precision(self._h, precision))
 
     def record(self, sim: Sim, n_frames: int) -> int:
         tot = C.c_uint32()

@@ -1,0 +1,133 @@
+"""Train the learned macro-step network on trajectories the GPU SPH step generates.
+
+    python npr-sph_gb300/train_mpnn.py [--scenes 200] [--particles 65536] [--frames 10]
+                                       [--gap 96] [--steps 20000] [--out npr-sph_gb300/weights/mpnn_w64.npy]
+
+Training data: `scenes` seeded runs of `particles` particles each, advanced together in one
+batched context with the literal mass and smoothing length and g = -9.81. Per run the stiffness k
+and viscosity mu and the drop geometry are drawn from the seed:
+  - even runs: a dam break, a block against the x = 0 wall of a 4:1:1 box, k ~ U[1500, 2500],
+    mu = 3000 * U[0.5, 1.5] (around the literal uniforms);
+  - odd runs: a lattice block in the lower corner, or a ball dropped from mid-height, of a cubic
+    box, k ~ U[500, 3000], mu log-uniform in [0.1, 3000].
+Every `gap` steps each run contributes a frame: its state, the <= 32 nearest neighbours and
+density of every particle, and as target the velocity change of the next 4 plain steps (4*dt)
+from the forces. The network is then trained by Adam on the GPU (the library's own forward and
+backward kernels), one frame per step, with a cosine-decayed learning rate.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE))
+
+import nprsph as S  # noqa: E402
+
+DEFAULT_OUT = HERE / "weights" / "mpnn_w64.npy"
+
+
+def training_scenes(n_scene: int, n: int, seed: int):
+    rng = np.random.default_rng(seed)
+    p0 = S.default_params()
+    s = 0.5 * p0.h
+    plist, parts = [], []
+    for i in range(n_scene):
+        if i % 2 == 0:
+            nx = int(round(n ** (1 / 3) / 2 ** (1 / 3)))   # block nx x 2nx x nx ~ n
+            while nx * 2 * nx * nx < n:
+                nx += 1
+            by, bz = 2 * nx * s, nx * s
+            L = max(by, bz)
+            p = S.workload_params(lower=(0.0, 0.0, 0.0), upper=(4 * L, by, bz),
+                                  k=float(rng.uniform(1500, 2500)), mu=float(3000.0 * rng.uniform(0.5, 1.5)),
+                                  flags=S.FLAG_KEEP_FORCE)
+            a = S.scene_fill(n, (0.0, 0.0, 0.0), (nx * s, by, bz), s, 0.01 * p.h, seed * 7919 + i)
+        else:
+            edge = 2.0 * math.ceil(n ** (1 / 3) + 1) * s
+            p = S.workload_params(lower=(0.0, 0.0, 0.0), upper=(edge, edge, edge), k=float(rng.uniform(500, 3000)),
+                                  mu=float(10 ** rng.uniform(-1, math.log10(3000.0))), flags=S.FLAG_KEEP_FORCE)
+            if rng.integers(0, 2):
+                a = S.scene_ball(n, (0.5 * edge, 0.55 * edge, 0.5 * edge), s, 0.01 * p.h, seed * 7919 + i)
+            else:
+                a = S.scene_fill(n, (0.0, 0.0, 0.0), (0.5 * edge, edge, 0.5 * edge), s, 0.01 * p.h, seed * 7919 + i)
+        plist.append(p)
+        parts.append(a)
+    counts = np.full(n_scene, n, dtype=np.uint32)
+    return plist, counts, np.concatenate(parts)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--scenes", type=int, default=200)
+    ap.add_argument("--particles", type=int, default=65536)
+    ap.add_argument("--frames", type=int, default=10, help="frames per run")
+    ap.add_argument("--gap", type=int, default=96, help="plain steps between frames")
+    ap.add_argument("--steps", type=int, default=20000, help="Adam steps")
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--seed", type=int, default=4)
+    ap.add_argument("--out", type=Path, default=DEFAULT_OUT)
+    args = ap.parse_args()
+
+    t0 = time.time()
+    plist, counts, parts = training_scenes(args.scenes, args.particles, args.seed)
+    net = S.Net(args.particles)
+    net.set_params(init_params(args.seed))
+    with S.Sim(plist, counts=counts) as sim:
+        sim.upload(parts)
+        for f in range(args.frames):
+            total = net.record(sim, 1)
+            if f + 1 < args.frames:
+                sim.step(args.gap)
+        sim.synchronize()
+    t_rec = time.time() - t0
+    losses = []
+    chunk = 500
+    done = 0
+    t1 = time.time()
+    while done < args.steps:
+        k = min(chunk, args.steps - done)
+        lr = args.lr * (0.01 + 0.99 * 0.5 * (1 + math.cos(math.pi * done / args.steps)))
+        losses.append(net.train(k, lr=lr, seed=args.seed * 1000003 + done))
+        done += k
+    t_train = time.time() - t1
+    params = net.get_params()
+    net.close()
+    args.out.parent.mkdir(parents=True, exist_ok=True)
+    np.save(args.out, params)
+    loss = np.concatenate(losses)
+    meta = {"scenes": args.scenes, "particles": args.particles, "frames_per_run": args.frames, "gap": args.gap,
+            "frames": int(total), "adam_steps": args.steps, "lr": args.lr, "seed": args.seed,
+            "loss_first_500": float(loss[:500].mean()), "loss_last_500": float(loss[-500:].mean()),
+            "record_s": t_rec, "train_s": t_train}
+    args.out.with_suffix(".json").write_text(json.dumps(meta, indent=1))
+    print(json.dumps(meta))
+
+
+def init_params(seed: int) -> np.ndarray:
+    """He-style initial parameters in the library's flat layout (sph_mpnn_set_params)."""
+    rng = np.random.default_rng(seed)
+    W, FE, FN, FO = 64, 8, 8, 3
+    shapes = [("We1", (FE, W)), ("be1", (W,)), ("Wn1", (W + FN, W)), ("bn1", (W,)), ("Wp", (W, W)),
+              ("We2", (FE, W)), ("be2", (W,)), ("Wn2", (2 * W, W)), ("bn2", (W,)), ("Wo", (W, FO)), ("bo", (FO,))]
+    out = []
+    for name, shape in shapes:
+        if name.startswith("W"):
+            scale = math.sqrt(2.0 / shape[0]) if name != "Wo" else 0.1 / math.sqrt(shape[0])
+            out.append(rng.normal(0.0, scale, shape).reshape(-1))
+        else:
+            out.append(np.zeros(int(np.prod(shape))))
+    flat = np.concatenate(out).astype(np.float32)
+    assert len(flat) == int(S.lib.sph_mpnn_num_params())
+    return flat
+
+
+if __name__ == "__main__":
+    main()

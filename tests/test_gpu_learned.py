@@ -59,6 +59,30 @@ def test_forward_and_gradient_match_fp64_oracle(sph, gpu):
         off += size
 
 
+@pytest.mark.parametrize("seed", [5, 6])
+def test_bf16_tensor_core_inference_matches_fp32_forward(sph, gpu, seed):
+    """The macro-step's inference kernels (BF16 mma.sync, FP32 accumulate) against the FP32
+    forward on the same frame: BF16 rounds weights and activations to 8 mantissa bits, so the
+    outputs agree to a few percent of their scale."""
+    from oracle import mpnn_oracle as MO
+
+    pos, vel, rho, nb, cnt, target, fc = random_frame(seed, n=200)
+    n = len(pos)
+    pos4 = np.zeros((n, 4), np.float32); pos4[:, :3] = pos
+    vel4 = np.zeros((n, 4), np.float32); vel4[:, :3] = vel
+    rhop = np.zeros((n, 2), np.float32); rhop[:, 0] = rho
+    with sph.Net(256) as net:
+        net.set_params(MO.init_params(seed))
+        o32 = net.forward(pos4, vel4, rhop, nb, cnt, fc, precision=0)[:, :3]
+        o16 = net.forward(pos4, vel4, rhop, nb, cnt, fc, precision=1)[:, :3]
+    scale = np.abs(o32).max()
+    assert scale > 0
+    err = np.abs(o16 - o32).max() / scale
+    assert err < 0.05, err
+    corr = np.corrcoef(o16.ravel(), o32.ravel())[0, 1]
+    assert corr > 0.999, corr
+
+
 @pytest.fixture(scope="module")
 def trained(sph, gpu):
     """A network trained briefly on frames of two small dam breaks (k and mu varied)."""
@@ -126,7 +150,8 @@ def test_learned_run_stays_finite(sph, trained):
         rep = sim.learned_step(net, 16, judge_every=8, density_tol=0.05, momentum_tol=0.05)
         d = sim.reduce()
         out = sim.download()
-    assert rep.judged == 2
+    assert 1 <= rep.judged <= 2  # a failed judge hands the next interval to plain SPH
+    assert rep.learned_macro_steps + rep.plain_macro_steps == 16
     assert d.nonfinite == 0
     lo, hi = np.array(sc.params.lower[:3]), np.array(sc.params.upper[:3])
     assert np.all(out["pos"][:, :3] >= lo) and np.all(out["pos"][:, :3] <= hi)
