@@ -85,7 +85,26 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         if r.returncode:
             raise RuntimeError("link failed")
     stamp.write_text(machine)
+    build_headless(force or bool(jobs), verbose)
     return LIB
+
+
+HEADLESS = PKG / "sph_headless"
+
+
+def build_headless(force: bool = False, verbose: bool = False) -> Path:
+    """The C++ host loop (host/sph_headless.cpp) linked against libsph_gb300.so."""
+    src = PKG / "host" / "sph_headless.cpp"
+    if not force and HEADLESS.exists() and HEADLESS.stat().st_mtime >= max(src.stat().st_mtime, LIB.stat().st_mtime):
+        return HEADLESS
+    cmd = ["g++", "-O2", "-std=c++17", "-Wall", "-I", str(REPO / "include"), str(src), "-o", str(HEADLESS),
+           "-L", str(PKG), "-lsph_gb300", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if verbose or r.returncode:
+        sys.stderr.write(r.stdout + r.stderr)
+    if r.returncode:
+        raise RuntimeError("headless driver build failed")
+    return HEADLESS
 
 
 if __name__ == "__main__":

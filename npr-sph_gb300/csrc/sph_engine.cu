@@ -379,6 +379,8 @@ sph_status sph_set_params(sph_ctx* ctx, const sph_params* p) {
     if (!ctx || !p) return SPH_ERR_INVALID_ARG;
     if (ctx->batched) return fail(ctx, SPH_ERR_UNSUPPORTED, "a batch takes its parameters at creation");
     if (sph_params_validate(p) != SPH_OK) return fail(ctx, SPH_ERR_INVALID_ARG, "invalid sph_params");
+    // Callers upload the uniforms every frame (sendUniforms, Main.cpp:274-278): unchanged ones cost nothing.
+    if (std::memcmp(&ctx->params[0], p, sizeof(sph_params)) == 0) return SPH_OK;
     GUARD_BEGIN
     CK(cudaSetDevice(ctx->device));
     ctx->params[0] = *p;

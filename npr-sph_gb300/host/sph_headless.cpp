@@ -1,0 +1,169 @@
+// sph_headless.cpp -- the reference's host loop without a window, over the C ABI.
+//
+// Mirrors NPR-SPH/Main.cpp:
+//   init_particles()   Main.cpp:510-539  make_grid() lattice -> sph_scene_reference_grid + sph_upload_aos
+//   sendUniforms()     Main.cpp:254-279  ConstantsUniform/BoundaryUniform -> sph_set_params, every frame,
+//                                        after the step (so a step uses the previous frame's uniforms)
+//   display()          Main.cpp:285-305  if simulate: the three dispatches -> sph_step(ctx, 1)
+//   keyboard()         Main.cpp:454-476  'p' toggles simulate (which starts false, Main.cpp:87),
+//                                        'r' re-initialises the particles
+// Keys come from a script instead of GLFW: --keys "p@0,r@500,p@501" presses a key at a frame.
+// Every --report frames one JSON line goes to stdout: frame, steps, wall time per frame and the
+// FP64 diagnostics (sph_reduce). --scene dam_break runs the 1,048,576-particle dam break instead
+// of the reference's 10,000-particle lattice.
+//
+//   sph_headless [--frames N] [--keys "p@0"] [--report N] [--scene reference|dam_break]
+//                [--visc V] [--smoothing S] [--mass M] [--rest-rho R]
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "sph_gb300.h"
+
+namespace {
+
+struct Options {
+    int frames = 600;
+    int report = 60;
+    std::string scene = "reference";
+    std::map<int, std::string> keys;  // frame -> keys pressed
+    float visc = -1, smoothing = -1, mass = -1, rest_rho = -1;
+};
+
+bool parse(int argc, char** argv, Options& o) {
+    for (int i = 1; i < argc; ++i) {
+        std::string a = argv[i];
+        auto next = [&](const char* what) -> const char* {
+            if (i + 1 >= argc) { std::fprintf(stderr, "%s needs a value\n", what); std::exit(2); }
+            return argv[++i];
+        };
+        if (a == "--frames") o.frames = std::atoi(next("--frames"));
+        else if (a == "--report") o.report = std::atoi(next("--report"));
+        else if (a == "--scene") o.scene = next("--scene");
+        else if (a == "--visc") o.visc = (float)std::atof(next("--visc"));
+        else if (a == "--smoothing") o.smoothing = (float)std::atof(next("--smoothing"));
+        else if (a == "--mass") o.mass = (float)std::atof(next("--mass"));
+        else if (a == "--rest-rho") o.rest_rho = (float)std::atof(next("--rest-rho"));
+        else if (a == "--keys") {
+            std::string s = next("--keys");
+            size_t p = 0;
+            while (p < s.size()) {
+                size_t q = s.find(',', p);
+                if (q == std::string::npos) q = s.size();
+                std::string tok = s.substr(p, q - p);
+                size_t at = tok.find('@');
+                if (at == std::string::npos || at == 0) { std::fprintf(stderr, "bad key event '%s'\n", tok.c_str()); return false; }
+                o.keys[std::atoi(tok.c_str() + at + 1)] += tok.substr(0, at);
+                p = q + 1;
+            }
+        } else {
+            std::fprintf(stderr, "unknown argument %s\n", a.c_str());
+            return false;
+        }
+    }
+    return o.frames >= 0 && o.report > 0 && (o.scene == "reference" || o.scene == "dam_break");
+}
+
+// The scene the 'r' key re-creates.
+std::vector<sph_particle> make_particles(const Options& o, sph_params& p) {
+    std::vector<sph_particle> parts;
+    if (o.scene == "reference") {
+        parts.resize(10000);
+        sph_scene_reference_grid(parts.data(), 10000, p.particle_radius);  // make_grid(), Main.cpp:488-505
+    } else {
+        // 64 x 128 x 128 block at 0.5h against the x = 0 wall of a 5.12 x 1.28 x 1.28 box
+        const float s = 0.5f * p.smoothing_coeff * p.particle_radius;
+        const float lo[3] = {0, 0, 0}, hi[3] = {64 * s, 128 * s, 128 * s};
+        p.lower[0] = p.lower[1] = p.lower[2] = 0.0f;
+        p.upper[0] = 4 * 128 * s;
+        p.upper[1] = p.upper[2] = 128 * s;
+        p.gravity[1] = -9.81f;
+        parts.resize(64u * 128u * 128u);
+        sph_scene_fill(parts.data(), (uint32_t)parts.size(), lo, hi, s, 0.01f * 2 * s, 2);
+    }
+    return parts;
+}
+
+void report(sph_ctx* ctx, int frame, double ms_per_frame) {
+    sph_diag d;
+    if (sph_reduce(ctx, &d) != SPH_OK) {
+        std::printf("{\"frame\": %d, \"error\": \"%s\"}\n", frame, sph_last_error(ctx));
+        return;
+    }
+    std::printf("{\"frame\": %d, \"steps\": %llu, \"ms_per_frame\": %.4f, \"mean_rho\": %.6g, \"max_rho\": %.6g, "
+                "\"kinetic_energy\": %.6g, \"momentum\": [%.6g, %.6g, %.6g], \"nonfinite\": %llu}\n",
+                frame, (unsigned long long)d.step, ms_per_frame, d.mean_rho, d.max_rho, d.kinetic_energy,
+                d.momentum[0], d.momentum[1], d.momentum[2], (unsigned long long)d.nonfinite);
+    std::fflush(stdout);
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    Options o;
+    if (!parse(argc, argv, o)) {
+        std::fprintf(stderr, "usage: %s [--frames N] [--keys \"p@0,r@500\"] [--report N] "
+                             "[--scene reference|dam_break] [--visc V] [--smoothing S] [--mass M] [--rest-rho R]\n",
+                     argv[0]);
+        return 2;
+    }
+    sph_params p;
+    sph_params_default(&p);  // ConstantsData / BoundaryData initial values (Main.cpp:110-122)
+    std::vector<sph_particle> parts = make_particles(o, p);
+    sph_ctx* ctx = nullptr;
+    if (sph_create(&p, (uint32_t)parts.size(), nullptr, &ctx) != SPH_OK) {
+        std::fprintf(stderr, "sph_create failed\n");
+        return 1;
+    }
+    if (sph_upload_aos(ctx, parts.data(), (uint32_t)parts.size()) != SPH_OK) {
+        std::fprintf(stderr, "upload: %s\n", sph_last_error(ctx));
+        return 1;
+    }
+    bool simulate = false;  // Main.cpp:87: a zero-initialised global, so the simulation starts paused
+    auto t0 = std::chrono::steady_clock::now();
+    int frames_since = 0;
+    for (int frame = 0; frame < o.frames; ++frame) {
+        auto it = o.keys.find(frame);
+        if (it != o.keys.end()) {
+            for (char k : it->second) {
+                if (k == 'p' || k == 'P') simulate = !simulate;  // Main.cpp:466-468
+                if (k == 'r' || k == 'R') {                      // Main.cpp:460-464
+                    parts = make_particles(o, p);
+                    if (sph_upload_aos(ctx, parts.data(), (uint32_t)parts.size()) != SPH_OK) {
+                        std::fprintf(stderr, "reset: %s\n", sph_last_error(ctx));
+                        return 1;
+                    }
+                }
+            }
+        }
+        if (simulate && sph_step(ctx, 1) != SPH_OK) {  // display(), Main.cpp:291-304
+            std::fprintf(stderr, "step: %s\n", sph_last_error(ctx));
+            return 1;
+        }
+        // sendUniforms() after the dispatches (Main.cpp:314): slider edits reach the next frame
+        if (o.visc > 0) p.visc = o.visc;
+        if (o.smoothing > 0) p.smoothing_coeff = o.smoothing;
+        if (o.mass > 0) p.mass = o.mass;
+        if (o.rest_rho > 0) p.resting_rho = o.rest_rho;
+        if (sph_set_params(ctx, &p) != SPH_OK) std::fprintf(stderr, "uniforms: %s\n", sph_last_error(ctx));
+        ++frames_since;
+        if ((frame + 1) % o.report == 0 || frame + 1 == o.frames) {
+            if (sph_synchronize(ctx) != SPH_OK) {
+                std::fprintf(stderr, "device: %s\n", sph_last_error(ctx));
+                return 1;
+            }
+            auto t1 = std::chrono::steady_clock::now();
+            double ms = std::chrono::duration<double, std::milli>(t1 - t0).count() / frames_since;
+            report(ctx, frame + 1, ms);
+            frames_since = 0;
+            t0 = std::chrono::steady_clock::now();
+        }
+    }
+    sph_destroy(ctx);
+    return 0;
+}
