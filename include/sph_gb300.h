@@ -202,25 +202,32 @@ sph_status sph_tile_stats(sph_ctx* ctx, uint32_t out[2]);
 
 /* ---- learned macro-step (new; no reference counterpart) -----------------
  * A message-passing network (2 rounds over the <= 32 nearest neighbours,
- * hidden width 64) predicts each particle's velocity change over 4*dt; one
- * network pass replaces 4 plain steps. It is trained on the GPU, by this
- * library's own forward/backward/Adam kernels, on frames recorded from the
- * plain step itself. Every judge_every macro-steps plain SPH re-runs the same
- * interval from the same state; when the mean relative density deviation
- * between the two results exceeds density_tol, or their momentum difference
- * (relative to sum m|v| + M |G| 4 dt) exceeds momentum_tol, the plain result is
- * kept and plain SPH runs the next judge_every macro-steps. */
+ * hidden width 64) predicts, per particle, the mean accelerations of the next
+ * 4 plain steps: O_v = (a0+a1+a2+a3)/(4A) and O_x = (4a0+3a1+2a2+a3)/(10A),
+ * A = k/h. One network pass replaces 4 plain steps:
+ *   v' = v + 4 dt A O_v,  x' = x + 4 dt v + 10 dt^2 A O_x,  then the wall clamp.
+ * The network is trained on the GPU, by this library's own forward/backward/Adam
+ * kernels, on frames recorded from the plain step itself.
+ * Judge: the macro-steps run in intervals of judge_every. Each learned interval
+ * starts from a checkpoint; its last macro-step is judged: from the same state a
+ * learned macro-step and 4 plain steps are compared by particle id. When the mean
+ * relative density deviation exceeds density_tol, or the momentum difference
+ * (relative to sum m|v| + M |G| 4 dt) exceeds momentum_tol, the interval is rolled
+ * back to its checkpoint and run by plain SPH, and after the k-th failure in a row
+ * plain SPH also runs the next 2^(k-1) - 1 intervals (at most 7). This judge state
+ * lives in the context across sph_learned_step calls; an upload clears it. */
 typedef struct sph_mpnn sph_mpnn;
 
 typedef struct sph_learned_report {
-    uint64_t learned_macro_steps;
-    uint64_t plain_macro_steps;   /* macro-steps (4 plain steps each) run by plain SPH */
+    uint64_t learned_macro_steps;  /* macro-steps whose learned result was kept */
+    uint64_t plain_macro_steps;    /* macro-steps (4 plain steps each) run by plain SPH */
     uint64_t judged;
-    uint64_t fallbacks;           /* judged macro-steps that kept the plain result */
-    double last_density_dev;      /* mean |rho_learned - rho_plain| / rho_plain at the last judge */
+    uint64_t fallbacks;            /* judged intervals that failed and were rolled back */
+    double last_density_dev;       /* mean |rho_learned - rho_plain| / rho_plain at the last judge */
     double last_momentum_dev;
     double max_density_dev;
-    double sum_density_dev;       /* over all judges */
+    double sum_density_dev;        /* over all judges */
+    uint64_t discarded_macro_steps;/* learned macro-steps thrown away by roll-backs */
 } sph_learned_report;
 
 uint32_t sph_mpnn_num_params(void);
@@ -232,22 +239,23 @@ const char* sph_mpnn_last_error(const sph_mpnn* net);
 sph_status sph_mpnn_set_params(sph_mpnn* net, const float* params, uint32_t n);
 sph_status sph_mpnn_get_params(sph_mpnn* net, float* params, uint32_t n);
 /* Loss, outputs and gradient of one frame given in host memory (n particles; pos4/vel4
- * n x 4, rhop2 n x 2 (rho, pres), nb n x 32 (-1 padded), cnt n, target4 n x 4 = velocity
- * change / c; fc = {h, c, rho_self, rho0, log10(mu)/4}). out4: n x 4, grad: num_params. */
+ * n x 4, rhop2 n x 2 (rho, pres), nb n x 32 (-1 padded), cnt n, target8 n x 8 = (O_v, O_x, 0, 0);
+ * fc = {h, c = sqrt(k), rho_self, rho0, log10(mu)/4, c dt / h}). The loss is the mean over
+ * particles of |O - target|^2. out8: n x 8 (O_v, O_x, 0, 0), grad: num_params. */
 sph_status sph_mpnn_loss_grad(sph_mpnn* net, uint32_t n, const float* pos4, const float* vel4,
                               const float* rhop2, const int32_t* nb, const int32_t* cnt,
-                              const float* target4, const float fc[5], double* loss, float* out4,
+                              const float* target8, const float fc[6], double* loss, float* out8,
                               float* grad);
-/* Network output (velocity change / c, n x 4) of a host frame as above: precision 1 runs the
+/* Network output (n x 8: O_v, O_x, 0, 0) of a host frame as above: precision 1 runs the
  * BF16 tensor-core inference kernels (the macro-step's path), 0 the FP32 training forward. */
 sph_status sph_mpnn_forward(sph_mpnn* net, uint32_t n, const float* pos4, const float* vel4,
-                            const float* rhop2, const int32_t* nb, const int32_t* cnt, const float fc[5],
-                            int32_t precision, float* out4);
+                            const float* rhop2, const int32_t* nb, const int32_t* cnt, const float fc[6],
+                            int32_t precision, float* out8);
 /* Precision of sph_learned_step: 1 BF16 tensor cores (default), 0 FP32 CUDA cores. */
 sph_status sph_mpnn_set_precision(sph_mpnn* net, int32_t precision);
 /* Record n_frames frames of every scene of ctx (created with SPH_FLAG_KEEP_FORCE): the state,
- * its neighbour lists and density, and as target the velocity change of the next 4 plain
- * steps from the forces alone. Advances ctx by 4 * n_frames steps. */
+ * its neighbour lists and density, and as targets (O_v, O_x) of the next 4 plain steps from
+ * the forces alone (no wall clamp). Advances ctx by 4 * n_frames steps. */
 sph_status sph_mpnn_record(sph_mpnn* net, sph_ctx* ctx, uint32_t n_frames, uint32_t* frames_total);
 sph_status sph_mpnn_clear_frames(sph_mpnn* net);
 /* `steps` Adam steps (lr), each on one recorded frame drawn from `seed`; loss_per_step may be NULL. */

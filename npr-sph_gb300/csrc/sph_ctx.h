@@ -26,6 +26,9 @@ struct sph_ctx {
     bool graph_dirty = true;
     bool have_state = false, need_hash = true, stepped = false;
     uint64_t steps = 0;
+    // judge state of the learned macro-step, kept across sph_learned_step calls (cleared by uploads)
+    int judge_failures = 0;  // failed judges in a row
+    int judge_backoff = 0;   // plain intervals still to run before the next learned attempt
     long long cell_cap = 0;
     int tile_cap = 0;
     double* diag_dev = nullptr;

@@ -271,6 +271,8 @@ sph_status upload_common(sph_ctx* ctx, const sph_particle* src, uint32_t n, bool
     ctx->need_hash = true;
     ctx->stepped = false;
     ctx->steps = 0;
+    ctx->judge_failures = 0;
+    ctx->judge_backoff = 0;
     if (host) CK(cudaStreamSynchronize(ctx->stream));  // caller may reuse its buffer on return
     return SPH_OK;
     GUARD_END

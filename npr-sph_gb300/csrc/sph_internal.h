@@ -100,6 +100,12 @@ void launch_density(const Buffers& b, const SceneDev& s0, bool batched, const La
                     cudaStream_t st);
 void launch_force_integrate(const Buffers& b, const SceneDev& s0, bool batched, const LaunchCfg& c,
                             cudaStream_t st);
+// Density (bit-identical to launch_density) plus, per particle, the kNbList nearest neighbours
+// j != i with r < h as sorted slots into nb[n][kNbList] (-1 padded) and their number in cnt
+// (the learned macro-step's input). The threads of a CTA run kNbList-entry lists of 128.
+constexpr int kNbList = 32;
+void launch_density_nb(const Buffers& b, const SceneDev& s0, bool batched, const LaunchCfg& c, int* nb, int* cnt,
+                       cudaStream_t st);
 // ---- launchers (sph_io.cu) ----
 // Per-scene FP64 sums into out[nscene * kDiagFields] (device), deterministic:
 // 0-2 sum m v, 3 kinetic, 4 potential, 5 sum rho, 6 min rho, 7 max rho,

@@ -4,10 +4,11 @@
 // the plain-SPH judge that takes over when the learned state drifts.
 //
 // Macro-step on a context (single scene):
-//   sort -> neighbours+density (k_nb_density) -> network -> integrate
-//   v' = v + c*O,  x' = x + 4 dt v + 2.5 dt c*O  (the constant-acceleration
-//   position of 4 symplectic sub-steps), then the wall clamp of
-//   integrate_comp.glsl:45-77 with the damping, then the cell hash.
+//   sort -> neighbours+density -> network -> update
+//   v' = v + 4 dt A O_v,  x' = x + 4 dt v + 10 dt^2 A O_x  (A = k/h; the exact
+//   result of 4 symplectic sub-steps when O holds the sub-steps' mean
+//   accelerations), then the wall clamp of integrate_comp.glsl:45-77 with the
+//   damping, then the cell hash.
 // Judge (every judge_every macro-steps): from the same state, one learned
 // macro-step and 4 plain steps; the mean relative density deviation between
 // the two results and their momentum difference decide. Above the bounds the
@@ -42,7 +43,9 @@ struct sph_mpnn {
     // context-sized scratch
     int cap = 0;
     int *nb = nullptr, *cnt = nullptr;
-    float4 *snap_pos = nullptr, *snap_vel = nullptr, *l_pos = nullptr, *l_vel = nullptr, *acc = nullptr;
+    float4 *snap_pos = nullptr, *snap_vel = nullptr, *l_pos = nullptr, *l_vel = nullptr, *acc = nullptr,
+           *accx = nullptr, *ck_pos = nullptr, *ck_vel = nullptr;
+    float2* ck_rhop = nullptr;
     float2 *snap_rhop = nullptr, *l_rhop = nullptr;
     float *rho_l = nullptr, *rho_p = nullptr;
     float4 *vel_l = nullptr, *vel_p = nullptr;
@@ -76,100 +79,43 @@ inline int nblk(long long n, int t = kT) { return (int)((n + t - 1) / t); }
 
 // ---- kernels ------------------------------------------------------------------------------
 
-// Density (the exact predicate, Kahan) and the K nearest neighbours j != i with r < h, over the
-// sorted state. Candidate order is the stencil walk, so the lists are deterministic.
-template <bool BATCHED, int R>
-__global__ void __launch_bounds__(kT) k_nb_density(const float4* __restrict__ pos_s, const int* __restrict__ start,
-                                                  SceneDev s0, const SceneDev* __restrict__ scenes, int nscene,
-                                                  float2* __restrict__ rhop, int* __restrict__ nb,
-                                                  int* __restrict__ cnt, int n) {
-    for (int t = blockIdx.x * kT + threadIdx.x; t < n; t += gridDim.x * kT) {
-        const float4 p = pos_s[t];
-        int sc = 0;
-        if constexpr (BATCHED) sc = min(max(scene_of(p), 0), nscene - 1);
-        const SceneDev& S = scene_params<BATCHED>(s0, scenes, sc);
-        const int cx = cell_coord(p.x, S.lo[0], S.inv_edge, S.dim[0]);
-        const int cy = cell_coord(p.y, S.lo[1], S.inv_edge, S.dim[1]);
-        const int cz = cell_coord(p.z, S.lo[2], S.inv_edge, S.dim[2]);
-        float bd[M::K];
-        int bj[M::K];
-        int c = 0, wpos = 0;
-        float worst = -1.0f, sum = 0.0f, comp = 0.0f;
-        const int x0 = max(cx - R, 0), x1 = min(cx + R, S.dim[0] - 1);
-        for (int z = max(cz - R, 0); z <= min(cz + R, S.dim[2] - 1); ++z)
-            for (int y = max(cy - R, 0); y <= min(cy + R, S.dim[1] - 1); ++y) {
-                const int row = S.cell_base + S.dim[0] * (y + S.dim[1] * z);
-                const int a = max(__ldg(start + row + x0), 0), b = min(__ldg(start + row + x1 + 1), n);
-                for (int j = a; j < b; ++j) {
-                    const float4 o = __ldg(pos_s + j);
-                    float dx, dy, dz;
-                    const float d2 = canon_d2(p.x, p.y, p.z, o.x, o.y, o.z, dx, dy, dz);
-                    if (!(d2 < S.cut_d2)) continue;
-                    const float w = S.h2 - d2;
-                    const float yk = w * w * w - comp, tk = sum + yk;  // Kahan
-                    comp = (tk - sum) - yk;
-                    sum = tk;
-                    if (j == t) continue;
-                    if (c < M::K) {
-                        bd[c] = d2;
-                        bj[c] = j;
-                        if (d2 > worst) { worst = d2; wpos = c; }
-                        ++c;
-                    } else if (d2 < worst) {
-                        bd[wpos] = d2;
-                        bj[wpos] = j;
-                        worst = -1.0f;
-                        for (int q = 0; q < M::K; ++q)
-                            if (bd[q] > worst) { worst = bd[q]; wpos = q; }
-                    }
-                }
-            }
-        const float rho = S.poly6c * sum;
-        const float pr = S.gas_k * (rho - S.rho0);
-        rhop[t] = make_float2(rho, pr < 0.0f ? 0.0f : pr);
-        for (int q = 0; q < M::K; ++q) nb[(size_t)t * M::K + q] = q < c ? bj[q] : -1;
-        cnt[t] = c;
-    }
-}
+static_assert(M::K == kNbList, "the network reads the neighbour lists of launch_density_nb");
 
-// Macro-step integrate from the network output O (= velocity change / c), fused with the hash.
+// Macro-step update from the network output O (FP32 path), fused with the hash.
 __global__ void __launch_bounds__(kT) k_macro_integrate(const float4* __restrict__ pos_s, const float4* __restrict__ vel_s,
-                                                       const float* __restrict__ O, SceneDev S, float c,
+                                                       const float* __restrict__ O, SceneDev S,
                                                        float4* __restrict__ pos_out, float4* __restrict__ vel_out,
                                                        int* __restrict__ key_out, int* __restrict__ rank_out,
                                                        int* __restrict__ count, int n) {
     const int t = blockIdx.x * kT + threadIdx.x;
     if (t >= n) return;
-    const float4 p = pos_s[t], v = vel_s[t];
-    const float dv[3] = {c * O[t * 4 + 0], c * O[t * 4 + 1], c * O[t * 4 + 2]};
-    const float vv[3] = {v.x, v.y, v.z}, pp[3] = {p.x, p.y, p.z};
-    float nv[3], np[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        nv[a] = vv[a] + dv[a];
-        np[a] = pp[a] + 4.0f * S.dt * vv[a] + 2.5f * S.dt * dv[a];
-        if (np[a] < S.lo[a]) { np[a] = S.lo[a]; nv[a] *= -S.damp; }        // integrate_comp.glsl:45-77
-        else if (np[a] > S.up[a]) { np[a] = S.up[a]; nv[a] *= -S.damp; }
-    }
-    pos_out[t] = make_float4(np[0], np[1], np[2], p.w);
-    vel_out[t] = make_float4(nv[0], nv[1], nv[2], v.w);
-    const int k = cell_key(S, np[0], np[1], np[2]);
+    float4 np, nv;
+    const float* o = O + (size_t)t * M::kOS;
+    M::macro_update(S, o[0], o[1], o[2], o[3], o[4], o[5], pos_s[t], vel_s[t], np, nv);
+    pos_out[t] = np;
+    vel_out[t] = nv;
+    const int k = cell_key(S, np.x, np.y, np.z);
     key_out[t] = k;
     rank_out[t] = atomicAdd(&count[k], 1);
 }
 
-// acc[id] += F / rho after a plain step (slot order of that step).
+// After plain sub-step `sub` (0..3, slot order of that step): acc[id] += a and
+// accx[id] += (4 - sub) a, with a = F / rho.
 __global__ void __launch_bounds__(kT) k_accum_accel(const float4* __restrict__ vel, const float4* __restrict__ force_s,
-                                                   const float2* __restrict__ rhop, int n, float4* __restrict__ acc) {
+                                                   const float2* __restrict__ rhop, int n, float wx,
+                                                   float4* __restrict__ acc, float4* __restrict__ accx) {
     const int s = blockIdx.x * kT + threadIdx.x;
     if (s >= n) return;
     const int id = id_of(vel[s]);
     if (id < 0 || id >= n) return;
     const float4 f = force_s[s];
     const float ir = 1.0f / rhop[s].x;
-    float4 a = acc[id];
-    a.x += f.x * ir; a.y += f.y * ir; a.z += f.z * ir;
+    const float ax = f.x * ir, ay = f.y * ir, az = f.z * ir;
+    float4 a = acc[id], b = accx[id];
+    a.x += ax; a.y += ay; a.z += az;
+    b.x += wx * ax; b.y += wx * ay; b.z += wx * az;
     acc[id] = a;
+    accx[id] = b;
 }
 
 // Frame arrays of one scene from the sorted state: neighbour slots made frame-local.
@@ -195,12 +141,17 @@ __global__ void __launch_bounds__(kT) k_frame_copy(const float4* __restrict__ po
     fcnt[k] = w;
 }
 
+// Targets of one frame: O_v = sum a / (4A), O_x = sum (4 - s) a / (10A) (inv_a = 1/A).
 __global__ void __launch_bounds__(kT) k_frame_target(const int* __restrict__ fid, const float4* __restrict__ acc,
-                                                    int m, float scale, float4* __restrict__ target) {
+                                                    const float4* __restrict__ accx, int m, float inv_a,
+                                                    float* __restrict__ target) {
     const int k = blockIdx.x * kT + threadIdx.x;
     if (k >= m) return;
-    const float4 a = acc[fid[k]];
-    target[k] = make_float4(a.x * scale, a.y * scale, a.z * scale, 0.0f);
+    const float4 a = acc[fid[k]], b = accx[fid[k]];
+    const float sv = 0.25f * inv_a, sx = 0.1f * inv_a;
+    float4* row = reinterpret_cast<float4*>(target + (size_t)k * M::kOS);
+    row[0] = make_float4(a.x * sv, a.y * sv, a.z * sv, b.x * sx);
+    row[1] = make_float4(b.y * sx, b.z * sx, 0.0f, 0.0f);
 }
 
 // Density and velocity by particle id (slot order -> id order).
@@ -241,31 +192,21 @@ __global__ void __launch_bounds__(kT) k_compare(const float* __restrict__ rl, co
 
 constexpr int kCmpBlocks = 256;
 
-M::FrameConst frame_const(const SceneDev& S) {
+M::FrameConst frame_const(const SceneDev& S, float visc) {
     M::FrameConst fc;
     const double PI = 3.141592741f, h = S.h;
     fc.h = S.h;
     fc.c = (float)std::sqrt((double)S.gas_k);
     fc.rho_self = (float)((double)S.mass * 315.0 / (64.0 * PI * h * h * h));
     fc.rho0 = S.rho0;
-    fc.log_mu = 0.0f;
+    fc.log_mu = (float)(std::log10((double)visc) / 4.0);
+    fc.courant = (float)(std::sqrt((double)S.gas_k) * (double)S.dt / h);
     return fc;
 }
 
+// Neighbour lists and density of the sorted state of a context.
 void launch_nb_density(sph_ctx* ctx, int* nb, int* cnt) {
-    const Buffers& b = ctx->b;
-    const int blocks = nblk(b.n);
-    if (ctx->batched) {
-        if (ctx->cfg.stencil == 2)
-            k_nb_density<true, 2><<<blocks, kT, 0, ctx->stream>>>(b.pos_s, b.start, ctx->s0, b.scenes, b.nscene, b.rhop, nb, cnt, b.n);
-        else
-            k_nb_density<true, 1><<<blocks, kT, 0, ctx->stream>>>(b.pos_s, b.start, ctx->s0, b.scenes, b.nscene, b.rhop, nb, cnt, b.n);
-    } else {
-        if (ctx->cfg.stencil == 2)
-            k_nb_density<false, 2><<<blocks, kT, 0, ctx->stream>>>(b.pos_s, b.start, ctx->s0, b.scenes, 1, b.rhop, nb, cnt, b.n);
-        else
-            k_nb_density<false, 1><<<blocks, kT, 0, ctx->stream>>>(b.pos_s, b.start, ctx->s0, b.scenes, 1, b.rhop, nb, cnt, b.n);
-    }
+    launch_density_nb(ctx->b, ctx->s0, ctx->batched, ctx->cfg, nb, cnt, ctx->stream);
 }
 
 template <class T>
@@ -280,8 +221,9 @@ sph_status ensure_ctx_scratch(sph_mpnn* net, int n) {
     const size_t m = (size_t)n;
     NCK(dal(&net->nb, m * M::K)); NCK(dal(&net->cnt, m));
     NCK(dal(&net->snap_pos, m)); NCK(dal(&net->snap_vel, m)); NCK(dal(&net->snap_rhop, m));
+    NCK(dal(&net->ck_pos, m)); NCK(dal(&net->ck_vel, m)); NCK(dal(&net->ck_rhop, m));
     NCK(dal(&net->l_pos, m)); NCK(dal(&net->l_vel, m)); NCK(dal(&net->l_rhop, m));
-    NCK(dal(&net->acc, m)); NCK(dal(&net->rho_l, m)); NCK(dal(&net->rho_p, m));
+    NCK(dal(&net->acc, m)); NCK(dal(&net->accx, m)); NCK(dal(&net->rho_l, m)); NCK(dal(&net->rho_p, m));
     NCK(dal(&net->vel_l, m)); NCK(dal(&net->vel_p, m)); NCK(dal(&net->cmp, (size_t)kCmpBlocks * 5));
     net->cap = n;
     return SPH_OK;
@@ -297,6 +239,19 @@ sph_status refresh_density(sph_ctx* ctx) {
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(ctx, SPH_ERR_CUDA, std::string("density refresh: ") + cudaGetErrorString(e));
     return SPH_OK;
+}
+
+// Device staging of one host frame (sph_mpnn_loss_grad, sph_mpnn_forward): pos, vel, target /
+// output rows, rhop, cnt, nb.
+cudaError_t ensure_host_arena(sph_mpnn* net, uint32_t n) {
+    if ((int)n <= net->hcap) return cudaSuccess;
+    if (net->harena) cudaFree(net->harena);
+    net->harena = nullptr;
+    net->hcap = 0;
+    const size_t bytes = (size_t)n * (16 + 16 + 4 * M::kOS + 8 + 4) + (size_t)n * M::K * 4;
+    const cudaError_t e = cudaMalloc(&net->harena, bytes);
+    if (e == cudaSuccess) net->hcap = (int)n;
+    return e;
 }
 
 // Fragment-ordered parameters and the BF16 activations for n particles.
@@ -326,8 +281,8 @@ sph_status learned_macro(sph_ctx* ctx, sph_mpnn* net) {
     const int n = ctx->b.n;
     engine::sort_state(ctx);
     launch_nb_density(ctx, net->nb, net->cnt);
-    M::Frame f{ctx->b.pos_s, ctx->b.vel_s, ctx->b.rhop, net->nb, net->cnt, nullptr, n, frame_const(ctx->s0)};
-    f.fc.log_mu = (float)(std::log10((double)ctx->params[0].visc) / 4.0);
+    M::Frame f{ctx->b.pos_s, ctx->b.vel_s, ctx->b.rhop, net->nb, net->cnt, nullptr, n,
+               frame_const(ctx->s0, ctx->params[0].visc)};
     if (net->precision == 1) {
         M::infer_round1(f, net->frags, net->H1b, net->Pperm, ctx->stream);
         M::infer_round2(f, net->frags, M::trainer_params(net->tr), net->H1b, net->Pperm, ctx->s0, ctx->b.pos,
@@ -335,7 +290,7 @@ sph_status learned_macro(sph_ctx* ctx, sph_mpnn* net) {
     } else {
         M::trainer_forward(net->inf, f, ctx->stream);
         k_macro_integrate<<<nblk(n), kT, 0, ctx->stream>>>(ctx->b.pos_s, ctx->b.vel_s, M::trainer_out(net->inf),
-                                                           ctx->s0, f.fc.c, ctx->b.pos, ctx->b.vel, ctx->b.key,
+                                                           ctx->s0, ctx->b.pos, ctx->b.vel, ctx->b.key,
                                                            ctx->b.rank, ctx->b.count, n);
     }
     ctx->need_hash = false;  // the integrate hashed the new positions
@@ -351,6 +306,61 @@ void copy_state(sph_ctx* ctx, float4* dp, float4* dv, float2* dr, const float4* 
     cudaMemcpyAsync(dp, sp, n * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->stream);
     cudaMemcpyAsync(dv, sv, n * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->stream);
     cudaMemcpyAsync(dr, sr, n * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream);
+}
+
+// A saved state of a context: the particles and the step count. Restoring it re-hashes at the
+// next sort (the cell counts of whatever the integrate hashed last are cleared).
+struct Saved {
+    float4* pos;
+    float4* vel;
+    float2* rhop;
+    uint64_t steps;
+};
+
+Saved save_state(sph_ctx* ctx, float4* p, float4* v, float2* r) {
+    copy_state(ctx, p, v, r, ctx->b.pos, ctx->b.vel, ctx->b.rhop);
+    return Saved{p, v, r, ctx->steps};
+}
+
+void restore_state(sph_ctx* ctx, const Saved& s) {
+    copy_state(ctx, ctx->b.pos, ctx->b.vel, ctx->b.rhop, s.pos, s.vel, s.rhop);
+    cudaMemsetAsync(ctx->b.count, 0, sizeof(int) * (size_t)ctx->b.ncell, ctx->stream);
+    ctx->need_hash = true;
+    ctx->steps = s.steps;
+}
+
+// One judged macro-step from the current state: a learned macro-step and 4 plain steps, both
+// from that state, compared by particle id. Returns the mean relative density deviation and
+// the momentum difference; the learned result is left in (l_pos, l_vel, l_rhop) and the plain
+// one in the context.
+sph_status judge_macro(sph_ctx* ctx, sph_mpnn* net, double& dev, double& mom) {
+    const int n = ctx->b.n;
+    const Saved s0 = save_state(ctx, net->snap_pos, net->snap_vel, net->snap_rhop);
+    if (!ctx->need_hash) cudaMemsetAsync(ctx->b.count, 0, sizeof(int) * (size_t)ctx->b.ncell, ctx->stream);
+    ctx->need_hash = true;
+    sph_status st = learned_macro(ctx, net);
+    if (!st) st = refresh_density(ctx);
+    if (st) return st;
+    k_by_id<<<nblk(n), kT, 0, ctx->stream>>>(ctx->b.vel, ctx->b.rhop, n, net->rho_l, net->vel_l);
+    copy_state(ctx, net->l_pos, net->l_vel, net->l_rhop, ctx->b.pos, ctx->b.vel, ctx->b.rhop);
+    restore_state(ctx, s0);
+    st = engine::run_steps(ctx, 4);
+    if (!st) st = refresh_density(ctx);
+    if (st) return st;
+    k_by_id<<<nblk(n), kT, 0, ctx->stream>>>(ctx->b.vel, ctx->b.rhop, n, net->rho_p, net->vel_p);
+    k_compare<<<kCmpBlocks, kT, 0, ctx->stream>>>(net->rho_l, net->rho_p, net->vel_l, net->vel_p, n, net->cmp);
+    std::vector<double> h((size_t)kCmpBlocks * 5);
+    if (cudaMemcpyAsync(h.data(), net->cmp, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, ctx->stream) ||
+        cudaStreamSynchronize(ctx->stream))
+        return fail(ctx, SPH_ERR_CUDA, "judge readback");
+    double sum[5] = {0, 0, 0, 0, 0};
+    for (int b = 0; b < kCmpBlocks; ++b)
+        for (int f = 0; f < 5; ++f) sum[f] += h[(size_t)b * 5 + f];
+    dev = sum[0] / n;
+    const double g = std::sqrt((double)ctx->s0.g[0] * ctx->s0.g[0] + (double)ctx->s0.g[1] * ctx->s0.g[1] +
+                               (double)ctx->s0.g[2] * ctx->s0.g[2]);
+    mom = std::sqrt(sum[1] * sum[1] + sum[2] * sum[2] + sum[3] * sum[3]) / (sum[4] + n * g * 4.0 * ctx->s0.dt);
+    return SPH_OK;
 }
 
 }  // namespace
@@ -381,8 +391,9 @@ sph_status sph_mpnn_destroy(sph_mpnn* net) {
     if (net->tr) M::trainer_delete(net->tr);
     if (net->inf) M::trainer_delete(net->inf);
     for (auto& r : net->frames) cudaFree(r.arena);
-    void* ptrs[] = {net->nb, net->cnt, net->snap_pos, net->snap_vel, net->snap_rhop, net->l_pos, net->l_vel,
-                    net->l_rhop, net->acc, net->rho_l, net->rho_p, net->vel_l, net->vel_p, net->cmp, net->harena,
+    void* ptrs[] = {net->nb, net->cnt, net->snap_pos, net->snap_vel, net->snap_rhop, net->ck_pos, net->ck_vel,
+                    net->ck_rhop, net->l_pos, net->l_vel,
+                    net->l_rhop, net->acc, net->accx, net->rho_l, net->rho_p, net->vel_l, net->vel_p, net->cmp, net->harena,
                     net->frags, net->H1b, net->Pperm};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -416,9 +427,9 @@ sph_status sph_mpnn_get_params(sph_mpnn* net, float* params, uint32_t n) {
 }
 
 sph_status sph_mpnn_loss_grad(sph_mpnn* net, uint32_t n, const float* pos4, const float* vel4, const float* rhop2,
-                              const int32_t* nb, const int32_t* cnt, const float* target4, const float fc[5],
-                              double* loss, float* out4, float* grad) {
-    if (!net || !pos4 || !vel4 || !rhop2 || !nb || !cnt || !target4 || !fc || n == 0) return SPH_ERR_INVALID_ARG;
+                              const int32_t* nb, const int32_t* cnt, const float* target8, const float fc[6],
+                              double* loss, float* out8, float* grad) {
+    if (!net || !pos4 || !vel4 || !rhop2 || !nb || !cnt || !target8 || !fc || n == 0) return SPH_ERR_INVALID_ARG;
     if ((int)n > M::trainer_capacity(net->tr)) { net->err = "frame larger than the training workspace"; return SPH_ERR_CAPACITY; }
     for (uint32_t i = 0; i < n; ++i) {
         if (cnt[i] < 0 || cnt[i] > M::K) { net->err = "neighbour count out of [0, 32]"; return SPH_ERR_INVALID_ARG; }
@@ -429,31 +440,26 @@ sph_status sph_mpnn_loss_grad(sph_mpnn* net, uint32_t n, const float* pos4, cons
             }
     }
     NCK(cudaSetDevice(net->device));
-    const size_t bytes = (size_t)n * (16 + 16 + 8 + 16 + 4) + (size_t)n * M::K * 4;
-    if ((int)n > net->hcap) {
-        if (net->harena) cudaFree(net->harena);
-        net->harena = nullptr;
-        NCK(cudaMalloc(&net->harena, bytes));
-        net->hcap = (int)n;
-    }
+    NCK(ensure_host_arena(net, n));
     char* a = (char*)net->harena;
     float4* dpos = (float4*)a; a += (size_t)n * 16;
     float4* dvel = (float4*)a; a += (size_t)n * 16;
-    float4* dtg = (float4*)a; a += (size_t)n * 16;
+    float* dtg = (float*)a; a += (size_t)n * 4 * M::kOS;
     float2* drh = (float2*)a; a += (size_t)n * 8;
     int* dcnt = (int*)a; a += (size_t)n * 4;
     int* dnb = (int*)a;
     cudaStream_t st = net->stream;
     NCK(cudaMemcpyAsync(dpos, pos4, (size_t)n * 16, cudaMemcpyHostToDevice, st));
     NCK(cudaMemcpyAsync(dvel, vel4, (size_t)n * 16, cudaMemcpyHostToDevice, st));
-    NCK(cudaMemcpyAsync(dtg, target4, (size_t)n * 16, cudaMemcpyHostToDevice, st));
+    NCK(cudaMemcpyAsync(dtg, target8, (size_t)n * 4 * M::kOS, cudaMemcpyHostToDevice, st));
     NCK(cudaMemcpyAsync(drh, rhop2, (size_t)n * 8, cudaMemcpyHostToDevice, st));
     NCK(cudaMemcpyAsync(dcnt, cnt, (size_t)n * 4, cudaMemcpyHostToDevice, st));
     NCK(cudaMemcpyAsync(dnb, nb, (size_t)n * M::K * 4, cudaMemcpyHostToDevice, st));
-    M::Frame f{dpos, dvel, drh, dnb, dcnt, dtg, (int)n, {fc[0], fc[1], fc[2], fc[3], fc[4]}};
+    M::Frame f{dpos, dvel, drh, dnb, dcnt, dtg, (int)n, {fc[0], fc[1], fc[2], fc[3], fc[4], fc[5]}};
     const double l = M::trainer_loss_grad(net->tr, f, st);
     if (loss) *loss = l;
-    if (out4) NCK(cudaMemcpyAsync(out4, M::trainer_out(net->tr), (size_t)n * 16, cudaMemcpyDeviceToHost, st));
+    if (out8)
+        NCK(cudaMemcpyAsync(out8, M::trainer_out(net->tr), (size_t)n * 4 * M::kOS, cudaMemcpyDeviceToHost, st));
     if (grad) NCK(cudaMemcpyAsync(grad, M::trainer_grad(net->tr), sizeof(float) * M::kParams, cudaMemcpyDeviceToHost, st));
     NCK(cudaStreamSynchronize(st));
     NCK(cudaGetLastError());
@@ -467,8 +473,8 @@ sph_status sph_mpnn_set_precision(sph_mpnn* net, int32_t precision) {
 }
 
 sph_status sph_mpnn_forward(sph_mpnn* net, uint32_t n, const float* pos4, const float* vel4, const float* rhop2,
-                            const int32_t* nb, const int32_t* cnt, const float fc[5], int32_t precision, float* out4) {
-    if (!net || !pos4 || !vel4 || !rhop2 || !nb || !cnt || !fc || !out4 || n == 0) return SPH_ERR_INVALID_ARG;
+                            const int32_t* nb, const int32_t* cnt, const float fc[6], int32_t precision, float* out8) {
+    if (!net || !pos4 || !vel4 || !rhop2 || !nb || !cnt || !fc || !out8 || n == 0) return SPH_ERR_INVALID_ARG;
     if (precision != 0 && precision != 1) return SPH_ERR_INVALID_ARG;
     if ((int)n > M::trainer_capacity(net->tr)) { net->err = "frame larger than the training workspace"; return SPH_ERR_CAPACITY; }
     for (uint32_t i = 0; i < n; ++i) {
@@ -480,17 +486,11 @@ sph_status sph_mpnn_forward(sph_mpnn* net, uint32_t n, const float* pos4, const 
             }
     }
     NCK(cudaSetDevice(net->device));
-    const size_t bytes = (size_t)n * (16 + 16 + 8 + 16 + 4) + (size_t)n * M::K * 4;
-    if ((int)n > net->hcap) {
-        if (net->harena) cudaFree(net->harena);
-        net->harena = nullptr;
-        NCK(cudaMalloc(&net->harena, bytes));
-        net->hcap = (int)n;
-    }
+    NCK(ensure_host_arena(net, n));
     char* a = (char*)net->harena;
     float4* dpos = (float4*)a; a += (size_t)n * 16;
     float4* dvel = (float4*)a; a += (size_t)n * 16;
-    float4* dout = (float4*)a; a += (size_t)n * 16;
+    float* dout = (float*)a; a += (size_t)n * 4 * M::kOS;
     float2* drh = (float2*)a; a += (size_t)n * 8;
     int* dcnt = (int*)a; a += (size_t)n * 4;
     int* dnb = (int*)a;
@@ -500,7 +500,7 @@ sph_status sph_mpnn_forward(sph_mpnn* net, uint32_t n, const float* pos4, const 
     NCK(cudaMemcpyAsync(drh, rhop2, (size_t)n * 8, cudaMemcpyHostToDevice, st));
     NCK(cudaMemcpyAsync(dcnt, cnt, (size_t)n * 4, cudaMemcpyHostToDevice, st));
     NCK(cudaMemcpyAsync(dnb, nb, (size_t)n * M::K * 4, cudaMemcpyHostToDevice, st));
-    M::Frame f{dpos, dvel, drh, dnb, dcnt, nullptr, (int)n, {fc[0], fc[1], fc[2], fc[3], fc[4]}};
+    M::Frame f{dpos, dvel, drh, dnb, dcnt, nullptr, (int)n, {fc[0], fc[1], fc[2], fc[3], fc[4], fc[5]}};
     if (precision == 1) {
         sph_status s2 = ensure_bf16(net, (int)n, st);
         if (s2) return s2;
@@ -508,10 +508,10 @@ sph_status sph_mpnn_forward(sph_mpnn* net, uint32_t n, const float* pos4, const 
         M::infer_round1(f, net->frags, net->H1b, net->Pperm, st);
         M::infer_round2(f, net->frags, M::trainer_params(net->tr), net->H1b, net->Pperm, S, nullptr, nullptr, dout,
                         nullptr, nullptr, nullptr, false, st);
-        NCK(cudaMemcpyAsync(out4, dout, (size_t)n * 16, cudaMemcpyDeviceToHost, st));
+        NCK(cudaMemcpyAsync(out8, dout, (size_t)n * 4 * M::kOS, cudaMemcpyDeviceToHost, st));
     } else {
         M::trainer_forward(net->tr, f, st);
-        NCK(cudaMemcpyAsync(out4, M::trainer_out(net->tr), (size_t)n * 16, cudaMemcpyDeviceToHost, st));
+        NCK(cudaMemcpyAsync(out8, M::trainer_out(net->tr), (size_t)n * 4 * M::kOS, cudaMemcpyDeviceToHost, st));
     }
     NCK(cudaStreamSynchronize(st));
     NCK(cudaGetLastError());
@@ -542,36 +542,37 @@ sph_status sph_mpnn_record(sph_mpnn* net, sph_ctx* ctx, uint32_t n_frames, uint3
             const SceneDev& S = ctx->sc_h[s];
             const int m = S.count;
             sph_mpnn::Rec r;
-            const size_t bytes = (size_t)m * (16 + 16 + 8 + 16 + 4 + 4) + (size_t)m * M::K * 4;
+            const size_t bytes = (size_t)m * (16 + 16 + 4 * M::kOS + 8 + 4 + 4) + (size_t)m * M::K * 4;
             NCK(cudaMalloc(&r.arena, bytes));
             char* a = (char*)r.arena;
             float4* fpos = (float4*)a; a += (size_t)m * 16;
             float4* fvel = (float4*)a; a += (size_t)m * 16;
-            float4* ftg = (float4*)a; a += (size_t)m * 16;
+            float* ftg = (float*)a; a += (size_t)m * 4 * M::kOS;
             float2* frh = (float2*)a; a += (size_t)m * 8;
             int* fcnt = (int*)a; a += (size_t)m * 4;
             int* fid = (int*)a; a += (size_t)m * 4;
             int* fnb = (int*)a;
             k_frame_copy<<<nblk(m), kT, 0, ctx->stream>>>(ctx->b.pos_s, ctx->b.vel_s, ctx->b.rhop, net->nb, net->cnt,
                                                           S.first, m, fpos, fvel, frh, fnb, fcnt, fid);
-            r.f = M::Frame{fpos, fvel, frh, fnb, fcnt, ftg, m, frame_const(S)};
-            r.f.fc.log_mu = (float)(std::log10((double)ctx->params[s].visc) / 4.0);
+            r.f = M::Frame{fpos, fvel, frh, fnb, fcnt, ftg, m, frame_const(S, ctx->params[s].visc)};
             net->frames.push_back(r);
             first_idx.push_back(net->frames.size() - 1);
         }
-        // target: velocity change over the next 4 plain steps from the forces alone (no wall clamp)
+        // targets: the mean accelerations of the next 4 plain steps, from the forces alone (no wall clamp)
         NCK(cudaMemsetAsync(net->acc, 0, sizeof(float4) * n, ctx->stream));
+        NCK(cudaMemsetAsync(net->accx, 0, sizeof(float4) * n, ctx->stream));
         for (int sub = 0; sub < 4; ++sub) {
             st = engine::run_steps(ctx, 1);
             if (st) { net->err = ctx->err; return st; }
-            k_accum_accel<<<nblk(n), kT, 0, ctx->stream>>>(ctx->b.vel, ctx->b.force_s, ctx->b.rhop, n, net->acc);
+            k_accum_accel<<<nblk(n), kT, 0, ctx->stream>>>(ctx->b.vel, ctx->b.force_s, ctx->b.rhop, n,
+                                                           (float)(4 - sub), net->acc, net->accx);
         }
         for (size_t s = 0; s < ctx->sc_h.size(); ++s) {
             sph_mpnn::Rec& r = net->frames[first_idx[s]];
             const SceneDev& S = ctx->sc_h[s];
-            const int* fid = (const int*)((const char*)r.arena + (size_t)S.count * (16 + 16 + 16 + 8 + 4));
-            k_frame_target<<<nblk(S.count), kT, 0, ctx->stream>>>(fid, net->acc, S.count, S.dt / r.f.fc.c,
-                                                                 (float4*)r.f.target);
+            const int* fid = (const int*)((const char*)r.arena + (size_t)S.count * (16 + 16 + 4 * M::kOS + 8 + 4));
+            k_frame_target<<<nblk(S.count), kT, 0, ctx->stream>>>(fid, net->acc, net->accx, S.count, S.h / S.gas_k,
+                                                                 const_cast<float*>(r.f.target));
         }
         NCK(cudaGetLastError());
     }
@@ -638,53 +639,35 @@ sph_status sph_learned_step(sph_ctx* ctx, sph_mpnn* net, int32_t n_macro, int32_
     if (!st && net->precision == 1) st = ensure_bf16(net, n, ctx->stream);
     if (st) return fail(ctx, st, net->err);
     sph_learned_report r{};
-    int plain_left = 0;
-    for (int k = 0; k < n_macro; ++k) {
-        if (plain_left > 0) {
-            st = engine::run_steps(ctx, 4);
+    int& backoff = ctx->judge_backoff;    // plain intervals still to run before the next learned attempt
+    int& failures = ctx->judge_failures;  // consecutive failed judges
+    for (int k = 0; k < n_macro;) {
+        const int len = judge_every > 0 ? std::min(judge_every, n_macro - k) : n_macro - k;
+        k += len;
+        if (backoff > 0) {
+            st = engine::run_steps(ctx, 4 * len);
             if (st) return st;
-            --plain_left;
-            ++r.plain_macro_steps;
+            r.plain_macro_steps += len;
+            --backoff;
             continue;
         }
-        const bool judge = judge_every > 0 && (k % judge_every) == judge_every - 1;
-        if (!judge) {
+        if (judge_every == 0) {
+            for (int q = 0; q < len; ++q) {
+                st = learned_macro(ctx, net);
+                if (st) return st;
+            }
+            r.learned_macro_steps += len;
+            continue;
+        }
+        // a learned interval: checkpoint, len - 1 learned macro-steps, then the judged one
+        const Saved ck = save_state(ctx, net->ck_pos, net->ck_vel, net->ck_rhop);
+        for (int q = 0; q + 1 < len; ++q) {
             st = learned_macro(ctx, net);
             if (st) return st;
-            ++r.learned_macro_steps;
-            continue;
         }
-        // judged macro-step: learned and plain from the same state
-        copy_state(ctx, net->snap_pos, net->snap_vel, net->snap_rhop, ctx->b.pos, ctx->b.vel, ctx->b.rhop);
-        const bool hash0 = ctx->need_hash;
-        const uint64_t steps0 = ctx->steps;
-        if (!hash0) cudaMemsetAsync(ctx->b.count, 0, sizeof(int) * (size_t)ctx->b.ncell, ctx->stream);
-        ctx->need_hash = true;
-        st = learned_macro(ctx, net);
-        if (!st) st = refresh_density(ctx);
+        double dev = 0.0, mom = 0.0;
+        st = judge_macro(ctx, net, dev, mom);
         if (st) return st;
-        k_by_id<<<nblk(n), kT, 0, ctx->stream>>>(ctx->b.vel, ctx->b.rhop, n, net->rho_l, net->vel_l);
-        copy_state(ctx, net->l_pos, net->l_vel, net->l_rhop, ctx->b.pos, ctx->b.vel, ctx->b.rhop);
-        copy_state(ctx, ctx->b.pos, ctx->b.vel, ctx->b.rhop, net->snap_pos, net->snap_vel, net->snap_rhop);
-        cudaMemsetAsync(ctx->b.count, 0, sizeof(int) * (size_t)ctx->b.ncell, ctx->stream);
-        ctx->need_hash = true;
-        ctx->steps = steps0;
-        st = engine::run_steps(ctx, 4);
-        if (!st) st = refresh_density(ctx);
-        if (st) return st;
-        k_by_id<<<nblk(n), kT, 0, ctx->stream>>>(ctx->b.vel, ctx->b.rhop, n, net->rho_p, net->vel_p);
-        k_compare<<<kCmpBlocks, kT, 0, ctx->stream>>>(net->rho_l, net->rho_p, net->vel_l, net->vel_p, n, net->cmp);
-        std::vector<double> h((size_t)kCmpBlocks * 5);
-        if (cudaMemcpyAsync(h.data(), net->cmp, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, ctx->stream) ||
-            cudaStreamSynchronize(ctx->stream))
-            return fail(ctx, SPH_ERR_CUDA, "judge readback");
-        double s[5] = {0, 0, 0, 0, 0};
-        for (int b = 0; b < kCmpBlocks; ++b)
-            for (int f = 0; f < 5; ++f) s[f] += h[(size_t)b * 5 + f];
-        const double dev = s[0] / n;
-        const double g = std::sqrt((double)ctx->s0.g[0] * ctx->s0.g[0] + (double)ctx->s0.g[1] * ctx->s0.g[1] +
-                                   (double)ctx->s0.g[2] * ctx->s0.g[2]);
-        const double mom = std::sqrt(s[1] * s[1] + s[2] * s[2] + s[3] * s[3]) / (s[4] + n * g * 4.0 * ctx->s0.dt);
         ++r.judged;
         r.last_density_dev = dev;
         r.last_momentum_dev = mom;
@@ -692,13 +675,21 @@ sph_status sph_learned_step(sph_ctx* ctx, sph_mpnn* net, int32_t n_macro, int32_
         r.sum_density_dev += dev;
         if (dev <= density_tol && mom <= momentum_tol) {
             copy_state(ctx, ctx->b.pos, ctx->b.vel, ctx->b.rhop, net->l_pos, net->l_vel, net->l_rhop);
-            ctx->need_hash = true;
             cudaMemsetAsync(ctx->b.count, 0, sizeof(int) * (size_t)ctx->b.ncell, ctx->stream);
-            ++r.learned_macro_steps;
+            ctx->need_hash = true;
+            r.learned_macro_steps += len;
+            failures = 0;
         } else {
+            // roll the interval back and run it with plain SPH; retry the network after
+            // 0, 1, 3, 7, 7, ... further plain intervals
+            restore_state(ctx, ck);
+            st = engine::run_steps(ctx, 4 * len);
+            if (st) return st;
             ++r.fallbacks;
-            ++r.plain_macro_steps;
-            plain_left = judge_every;  // plain SPH runs the next interval
+            r.plain_macro_steps += len;
+            r.discarded_macro_steps += len;
+            ++failures;
+            backoff = std::min((1 << std::min(failures - 1, 3)) - 1, 7);
         }
     }
     if (rep) *rep = r;

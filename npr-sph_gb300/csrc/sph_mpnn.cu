@@ -49,6 +49,7 @@ __device__ __forceinline__ void node_feat(float4 vi, float rho, int cnt, const F
     nf[5] = fc.log_mu;
     nf[6] = (float)cnt / K;
     nf[7] = 1.0f;
+    nf[8] = fc.courant;
 }
 
 // Round 1 edge layer per particle: E (stored), relu masks, X1 = [M1, n].
@@ -212,17 +213,20 @@ __global__ void __launch_bounds__(kT) k_reduce_split(const float* __restrict__ p
     else if (gb) gb[t - nw] = s;
 }
 
-__global__ void __launch_bounds__(kT) k_loss(const float* __restrict__ O, const float4* __restrict__ target, int n,
+// Loss: mean over particles of |O - target|^2 (both heads); dO = 2 (O - target) / n.
+__global__ void __launch_bounds__(kT) k_loss(const float* __restrict__ O, const float* __restrict__ target, int n,
                                             float* __restrict__ dO, double* __restrict__ part) {
     __shared__ double sh[kT];
     const int i = blockIdx.x * kT + threadIdx.x;
     double l = 0.0;
     if (i < n) {
-        const float4 tg = target[i];
-        const float d0 = O[i * 4 + 0] - tg.x, d1 = O[i * 4 + 1] - tg.y, d2 = O[i * 4 + 2] - tg.z;
         const float s = 2.0f / (float)n;
-        dO[i * 4 + 0] = s * d0; dO[i * 4 + 1] = s * d1; dO[i * 4 + 2] = s * d2; dO[i * 4 + 3] = 0.0f;
-        l = (double)d0 * d0 + (double)d1 * d1 + (double)d2 * d2;
+#pragma unroll
+        for (int q = 0; q < kOS; ++q) {
+            const float d = q < FO ? O[(size_t)i * kOS + q] - target[(size_t)i * kOS + q] : 0.0f;
+            dO[(size_t)i * kOS + q] = s * d;
+            l += (double)d * d;
+        }
     }
     sh[threadIdx.x] = l;
     __syncthreads();
@@ -333,10 +337,11 @@ struct Trainer {
         auto A = [&](cudaError_t x) { if (r == cudaSuccess) r = x; };
         A(al(&prm, kParams));
         A(al(&E, e * FE)); A(al(&X1, n * (W + FN))); A(al(&H1, n * W)); A(al(&P, n * W)); A(al(&X2, n * 2 * W));
-        A(al(&H2, n * W)); A(al(&O, n * 4)); A(al(&mask1, e)); A(al(&mask2, e));
+        A(al(&H2, n * W)); A(al(&O, n * kOS)); A(al(&mask1, e)); A(al(&mask2, e));
+        if (r == cudaSuccess) r = cudaMemset(O, 0, sizeof(float) * n * kOS);  // columns FO.. stay zero
         if (train) {
             A(al(&grad, kParams)); A(al(&adam_m, kParams)); A(al(&adam_v, kParams));
-            A(al(&dO, n * 4)); A(al(&dY2, n * W)); A(al(&dX2, n * 2 * W));
+            A(al(&dO, n * kOS)); A(al(&dY2, n * W)); A(al(&dX2, n * 2 * W));
             A(al(&dZ2, e * W)); A(al(&dP, n * W)); A(al(&dY1, n * W)); A(al(&dX1, n * (W + FN)));
             A(al(&part, (size_t)splits * (2 * W + 1) * W)); A(al(&loss_part, (size_t)nblk(n) + 1));
             A(al(&rev_cnt, n)); A(al(&rev_off, n + 1)); A(al(&rev_edges, e));
@@ -377,7 +382,7 @@ struct Trainer {
         k_reduce_split<<<nblk(total), kT, 0, st>>>(part, splits, total, grad + woff, FE * W, grad + boff);
     }
 
-    // Forward: O (n x 4) from the frame.
+    // Forward: O (n x kOS) from the frame.
     void forward(const Frame& f, cudaStream_t st) {
         const int n = f.n;
         k_edge1_fwd<<<nblk(n), kT, 0, st>>>(f, prm, E, mask1, X1);
@@ -385,15 +390,15 @@ struct Trainer {
         dense(H1, W, W, kWp, -1, W, P, W, n, 0, st);
         k_edge2_fwd<<<nblk(n), kT, 0, st>>>(f, prm, E, P, H1, mask2, X2);
         dense(X2, 2 * W, 2 * W, kWn2, kBn2, W, H2, W, n, 1, st);
-        dense(H2, W, W, kWo, kBo, FO, O, 4, n, 0, st);
+        dense(H2, W, W, kWo, kBo, FO, O, kOS, n, 0, st);
     }
 
     // Loss partials and the full parameter gradient (forward must have run).
     void backward(const Frame& f, cudaStream_t st) {
         const int n = f.n;
         k_loss<<<nblk(n), kT, 0, st>>>(O, f.target, n, dO, loss_part);
-        wgrad(H2, W, W, dO, 4, FO, n, kWo, kBo, st);
-        k_dense_bwd_data<<<nblk((long long)n * W), kT, 0, st>>>(dO, 4, FO, prm + kWo, W, nullptr, 0, H2, W, dY2, W, n);
+        wgrad(H2, W, W, dO, kOS, FO, n, kWo, kBo, st);
+        k_dense_bwd_data<<<nblk((long long)n * W), kT, 0, st>>>(dO, kOS, FO, prm + kWo, W, nullptr, 0, H2, W, dY2, W, n);
         wgrad(X2, 2 * W, 2 * W, dY2, W, W, n, kWn2, kBn2, st);
         k_dense_bwd_data<<<nblk((long long)n * 2 * W), kT, 0, st>>>(dY2, W, W, prm + kWn2, 2 * W, nullptr, 0, nullptr,
                                                                     0, dX2, 2 * W, n);

@@ -12,7 +12,7 @@
 //               (H1 is reused from the accumulator registers as the A operand).
 //   k_infer_r2  round 2 likewise, with the gathered P_j as the accumulator's
 //               initial value; per 16 particles: H2 = relu([M2 H1 1] Wn2'),
-//               O = H2 Wo + bo, then the macro-step integrate and cell hash.
+//               O = H2 Wo + bo (both heads), then the macro-step update and cell hash.
 // Biases ride on a constant-1 feature column, so padded edges (all features
 // zero) contribute exactly zero, as in the reference.
 // P is stored permuted: for particle j, lane group g reads the 8 features
@@ -32,7 +32,10 @@ constexpr int kThreads = kWarps * 32;
 constexpr int kTile = 16;         // particles per warp tile
 constexpr int kLd1 = 88;          // X1 tile row stride (80 used), bf16
 constexpr int kLd2 = 152;         // X2 tile row stride (144 used), bf16
-constexpr int kK1 = 80, kK2 = 144; // padded K of the two node layers (bias column at 72 / 128)
+constexpr int kK1 = 80, kK2 = 144; // padded K of the two node layers (bias column at W+FN / 128)
+constexpr int kBias1 = W + FN;     // bias column of the round-1 node layer
+static_assert(kBias1 < kK1, "round-1 node input does not fit its padded K");
+static_assert(FO <= 8, "the output layer is one n-tile of 8 columns");
 
 // Fragment-ordered weights (u32 = 2 x bf16), built by k_prep_frags.
 constexpr int kFragWe1 = 0;                          // [4 mt][32 lanes][4]
@@ -85,7 +88,7 @@ __global__ void k_prep_frags(const float* __restrict__ prm, uint32_t* __restrict
     // node layers: B[k][o], b0 rows k0, k0+1; b1 rows k0+8, k0+9
     const float *Wm, *b;
     int kin, nout, brow, base;
-    if (r < kFragWp) { Wm = prm + kWn1; b = prm + kBn1; kin = W + FN; nout = W; brow = 72; base = kFragWn1; }
+    if (r < kFragWp) { Wm = prm + kWn1; b = prm + kBn1; kin = W + FN; nout = W; brow = kBias1; base = kFragWn1; }
     else if (r < kFragWn2) { Wm = prm + kWp; b = nullptr; kin = W; nout = W; brow = -1; base = kFragWp; }
     else if (r < kFragWo) { Wm = prm + kWn2; b = prm + kBn2; kin = 2 * W; nout = W; brow = 128; base = kFragWn2; }
     else { Wm = prm + kWo; b = nullptr; kin = W; nout = FO; brow = -1; base = kFragWo; }
@@ -251,7 +254,8 @@ __global__ void __launch_bounds__(kThreads) k_infer_r1(const float4* __restrict_
                         case 5: v = fc.log_mu; break;
                         case 6: v = (float)c / K; break;
                         case 7: v = 1.0f; break;
-                        case 8: v = 1.0f; break;  // bias column 72
+                        case 8: v = fc.courant; break;
+                        case kBias1 - W: v = 1.0f; break;  // bias column
                         default: v = 0.0f;
                     }
                     X[p * kLd1 + 64 + lane] = __float2bfloat16_rn(v);
@@ -310,7 +314,7 @@ __global__ void __launch_bounds__(kThreads) k_infer_r2(const float4* __restrict_
                                                       const __nv_bfloat16* __restrict__ H1,
                                                       const uint4* __restrict__ Pperm, SceneDev S,
                                                       float4* __restrict__ pos_out, float4* __restrict__ vel_out,
-                                                      float4* __restrict__ out, int* __restrict__ key_out,
+                                                      float* __restrict__ out, int* __restrict__ key_out,
                                                       int* __restrict__ rank_out, int* __restrict__ count,
                                                       int integrate) {
     __shared__ __align__(16) __nv_bfloat16 xs[kWarps][kTile * kLd2];
@@ -319,7 +323,10 @@ __global__ void __launch_bounds__(kThreads) k_infer_r2(const float4* __restrict_
     EdgeFrags A;
     load_edge_frags(fr, kFragWe2, A);
     const float ih = 1.0f / fc.h, ic = 1.0f / fc.c;
-    const float bo[3] = {prm[kBo], prm[kBo + 1], prm[kBo + 2]};
+    static_assert(FO == 6, "the output gather below is written for two heads of 3");
+    float bo[FO];
+#pragma unroll
+    for (int q = 0; q < FO; ++q) bo[q] = prm[kBo + q];
     const int ntiles = (n + kTile - 1) / kTile;
     for (int tile = blockIdx.x * kWarps + warp; tile < ntiles; tile += gridDim.x * kWarps) {
         const int base = tile * kTile;
@@ -354,31 +361,36 @@ __global__ void __launch_bounds__(kThreads) k_infer_r2(const float4* __restrict_
             const uint2 b = __ldg(reinterpret_cast<const uint2*>(fr + kFragWo) + kt * 32 + lane);
             mma(o, ha[kt], b.x, b.y);
         }
-        // O rows g (o[0], o[1]) and g + 8 (o[2], o[3]), columns 2 tq, 2 tq + 1; column 2 sits in tq == 1
-        const float c2_r0 = __shfl_sync(0xffffffffu, o[0], (lane & ~3) | 1);
-        const float c2_r1 = __shfl_sync(0xffffffffu, o[2], (lane & ~3) | 1);
+        // O rows g (o[0], o[1]) and g + 8 (o[2], o[3]), columns 2 tq, 2 tq + 1: lane tq == 0 of each
+        // quad gathers the 6 columns of both rows from tq = 1 (columns 2, 3) and tq = 2 (4, 5).
+        // col[r][c]: row g + 8 r, column c
+        const float c10 = __shfl_sync(0xffffffffu, o[0], (lane & ~3) | 1);
+        const float c11 = __shfl_sync(0xffffffffu, o[1], (lane & ~3) | 1);
+        const float c12 = __shfl_sync(0xffffffffu, o[2], (lane & ~3) | 1);
+        const float c13 = __shfl_sync(0xffffffffu, o[3], (lane & ~3) | 1);
+        const float c20 = __shfl_sync(0xffffffffu, o[0], (lane & ~3) | 2);
+        const float c21 = __shfl_sync(0xffffffffu, o[1], (lane & ~3) | 2);
+        const float c22 = __shfl_sync(0xffffffffu, o[2], (lane & ~3) | 2);
+        const float c23 = __shfl_sync(0xffffffffu, o[3], (lane & ~3) | 2);
         if (tq == 0) {
 #pragma unroll
             for (int rr = 0; rr < 2; ++rr) {
                 const int i = base + g + rr * 8;
                 if (i >= n) continue;
-                const float O[3] = {(rr ? o[2] : o[0]) + bo[0], (rr ? o[3] : o[1]) + bo[1], (rr ? c2_r1 : c2_r0) + bo[2]};
-                if (out) out[i] = make_float4(O[0], O[1], O[2], 0.0f);
-                if (!integrate) continue;
-                const float4 pp = pos[i], vv = vel[i];
-                const float p3[3] = {pp.x, pp.y, pp.z}, v3[3] = {vv.x, vv.y, vv.z};
-                float np[3], nv[3];
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    const float dv = fc.c * O[a];
-                    nv[a] = v3[a] + dv;
-                    np[a] = p3[a] + 4.0f * S.dt * v3[a] + 2.5f * S.dt * dv;
-                    if (np[a] < S.lo[a]) { np[a] = S.lo[a]; nv[a] *= -S.damp; }  // integrate_comp.glsl:45-77
-                    else if (np[a] > S.up[a]) { np[a] = S.up[a]; nv[a] *= -S.damp; }
+                const float O0 = (rr ? o[2] : o[0]) + bo[0], O1 = (rr ? o[3] : o[1]) + bo[1];
+                const float O2 = (rr ? c12 : c10) + bo[2], O3 = (rr ? c13 : c11) + bo[3];
+                const float O4 = (rr ? c22 : c20) + bo[4], O5 = (rr ? c23 : c21) + bo[5];
+                if (out) {
+                    float4* orow = reinterpret_cast<float4*>(out + (size_t)i * kOS);
+                    orow[0] = make_float4(O0, O1, O2, O3);
+                    orow[1] = make_float4(O4, O5, 0.0f, 0.0f);
                 }
-                pos_out[i] = make_float4(np[0], np[1], np[2], pp.w);
-                vel_out[i] = make_float4(nv[0], nv[1], nv[2], vv.w);
-                const int k = cell_key(S, np[0], np[1], np[2]);
+                if (!integrate) continue;
+                float4 np, nv;
+                macro_update(S, O0, O1, O2, O3, O4, O5, pos[i], vel[i], np, nv);
+                pos_out[i] = np;
+                vel_out[i] = nv;
+                const int k = cell_key(S, np.x, np.y, np.z);
                 key_out[i] = k;
                 rank_out[i] = atomicAdd(&count[k], 1);
             }
@@ -407,7 +419,7 @@ void infer_round1(const Frame& f, const uint32_t* frags, __nv_bfloat16* H1, uint
 }
 
 void infer_round2(const Frame& f, const uint32_t* frags, const float* prm, const __nv_bfloat16* H1,
-                  const uint16_t* Pperm, const SceneDev& S, float4* pos_out, float4* vel_out, float4* out, int* key,
+                  const uint16_t* Pperm, const SceneDev& S, float4* pos_out, float4* vel_out, float* out, int* key,
                   int* rank, int* count, bool integrate, cudaStream_t st) {
     k_infer_r2<<<infer_grid(f.n), kThreads, 0, st>>>(f.pos, f.vel, f.nb, f.cnt, f.fc, f.n, frags, prm, H1,
                                                      reinterpret_cast<const uint4*>(Pperm), S, pos_out, vel_out, out,

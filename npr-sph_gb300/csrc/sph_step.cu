@@ -434,6 +434,131 @@ __global__ void __launch_bounds__(BLOCK) k_force_integrate(const float4* __restr
     }
 }
 
+// ---- density + nearest-neighbour lists (the learned macro-step's input) ---------------------
+
+// Keep the kNbList nearest entries of a per-thread list of staged indices (stride BLOCK in
+// shared memory): the farthest entry is removed until kNbList remain (ties: the later entry).
+template <int BLOCK>
+__device__ __forceinline__ void prune_nearest(unsigned short* lst, int& cnt, const Staged& st, float px, float py,
+                                              float pz) {
+    while (cnt > kNbList) {
+        float worst = -1.0f;
+        int wk = 0;
+        for (int k = 0; k < cnt; ++k) {
+            const int j = lst[BLOCK * k];
+            const float dx = st.x[j] - px, dy = st.y[j] - py, dz = st.z[j] - pz;
+            const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+            if (d2 >= worst) { worst = d2; wk = k; }
+        }
+        lst[BLOCK * wk] = lst[BLOCK * (cnt - 1)];
+        --cnt;
+    }
+}
+
+template <bool BATCHED, int R, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_density_nb(const float4* __restrict__ pos_s, const int* __restrict__ start,
+                                                      SceneDev s0, const SceneDev* __restrict__ scenes, int nscene,
+                                                      float2* __restrict__ rhop, int* __restrict__ nb,
+                                                      int* __restrict__ nbc, int n, uint32_t* __restrict__ stats) {
+    using G = TileGeom<R>;
+    constexpr int kCap = stage_cap<R, BLOCK>();
+    __shared__ TileShared<R, BLOCK> T;
+    extern __shared__ float4 dyn_n[];
+    float* base = reinterpret_cast<float*>(dyn_n);
+    const Staged st{base, base + kCap, base + 2 * kCap, reinterpret_cast<int*>(base + 3 * kCap)};
+    unsigned short* lst = reinterpret_cast<unsigned short*>(base + 4 * kCap) + threadIdx.x;  // [kNbCapForce][BLOCK]
+    for (int c0 = blockIdx.x * BLOCK; c0 < n; c0 += gridDim.x * BLOCK) {
+        float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+        int sc = 0, cx = 0, lrow = 0;
+        const bool tiled =
+            stage_chunk<BATCHED, R, BLOCK>(T, st, c0, n, pos_s, start, s0, scenes, nscene, p, sc, cx, lrow);
+        const int t = c0 + threadIdx.x;
+        if (t < n) {
+            if (!tiled) p = pos_s[t];
+            if constexpr (BATCHED) sc = min(max(scene_of(p), 0), nscene - 1);
+            const SceneDev& S = scene_params<BATCHED>(s0, scenes, sc);
+            const float cut = S.cut_d2, h2 = S.h2;
+            float sum = 0.0f, comp = 0.0f;
+            int* out = nb + (size_t)t * kNbList;
+            int c = 0;
+            if (tiled) {
+                // density: the arithmetic of k_density, candidate for candidate; list: the passing
+                // candidates other than the particle itself, pruned to the nearest kNbList
+                const float2 npx = make_float2(-p.x, -p.x), npy = make_float2(-p.y, -p.y);
+                const float2 npz = make_float2(-p.z, -p.z);
+                const float2 h2v = make_float2(h2, h2);
+                float2 s2 = make_float2(0.f, 0.f), c2 = make_float2(0.f, 0.f);
+#pragma unroll 1
+                for (int r = 0; r < G::kSegPerRow; ++r) {
+                    int a, b;
+                    seg_range<R, BLOCK>(T, lrow * G::kSegPerRow + r, cx, S.dim[0], start, a, b);
+#pragma unroll 1
+                    for (int j = a; j < b; j += 2) {
+                        const float2 d2 = pair_d2(st, j, npx, npy, npz);
+                        float2 w = __fadd2_rn(h2v, make_float2(-d2.x, -d2.y));
+                        w.x = fmaxf(w.x, 0.0f);
+                        w.y = fmaxf(w.y, 0.0f);
+                        const float2 term = __fmul2_rn(__fmul2_rn(w, w), w);
+                        const float2 y = __fadd2_rn(term, make_float2(-c2.x, -c2.y));
+                        const float2 tt = __fadd2_rn(s2, y);
+                        const float2 lost = __fadd2_rn(tt, make_float2(-s2.x, -s2.y));
+                        c2 = __fadd2_rn(lost, make_float2(-y.x, -y.y));
+                        s2 = tt;
+                        if (d2.x < cut && st.slot[j] != t) lst[BLOCK * c++] = (unsigned short)j;
+                        if (d2.y < cut && st.slot[j + 1] != t) lst[BLOCK * c++] = (unsigned short)(j + 1);
+                        if (c > kNbCapForce - 2) prune_nearest<BLOCK>(lst, c, st, p.x, p.y, p.z);
+                    }
+                }
+                kahan_add(sum, comp, s2.x);
+                kahan_add(sum, comp, -c2.x);
+                kahan_add(sum, comp, s2.y);
+                kahan_add(sum, comp, -c2.y);
+                prune_nearest<BLOCK>(lst, c, st, p.x, p.y, p.z);
+                for (int k = 0; k < kNbList; ++k) out[k] = k < c ? st.slot[lst[BLOCK * k]] : -1;
+            } else {
+                // global-memory path: the list lives in the output row itself
+                float worst = -1.0f;
+                int wpos = 0;
+                const int gx = cell_coord(p.x, S.lo[0], S.inv_edge, S.dim[0]);
+                const int gy = cell_coord(p.y, S.lo[1], S.inv_edge, S.dim[1]);
+                const int gz = cell_coord(p.z, S.lo[2], S.inv_edge, S.dim[2]);
+                for_rows_global<R>(S, start, n, gx, gy, gz, [&](int a, int b) {
+                    for (int j = a; j < b; ++j) {
+                        const float4 o = __ldg(pos_s + j);
+                        float dx, dy, dz;
+                        const float d2 = canon_d2(p.x, p.y, p.z, o.x, o.y, o.z, dx, dy, dz);
+                        if (!(d2 < cut)) continue;
+                        const float wgt = h2 - d2;
+                        kahan_add(sum, comp, wgt * wgt * wgt);
+                        if (j == t) continue;
+                        if (c < kNbList) {
+                            out[c] = j;
+                            if (d2 >= worst) { worst = d2; wpos = c; }
+                            ++c;
+                        } else if (d2 < worst) {
+                            out[wpos] = j;
+                            worst = -1.0f;
+                            for (int k = 0; k < kNbList; ++k) {
+                                const float4 q = __ldg(pos_s + out[k]);
+                                float ex, ey, ez;
+                                const float e2 = canon_d2(p.x, p.y, p.z, q.x, q.y, q.z, ex, ey, ez);
+                                if (e2 >= worst) { worst = e2; wpos = k; }
+                            }
+                        }
+                    }
+                });
+                for (int k = c; k < kNbList; ++k) out[k] = -1;
+            }
+            nbc[t] = min(c, kNbList);
+            const float rho = S.poly6c * sum;
+            const float pr = S.gas_k * (rho - S.rho0);
+            rhop[t] = make_float2(rho, pr < 0.0f ? 0.0f : pr);
+        }
+        if (!tiled && threadIdx.x == 0 && stats) atomicAdd(&stats[0], 1u);
+        __syncthreads();
+    }
+}
+
 template <class K>
 int grid_size(K kernel, int block, size_t smem, int n) {
     int per_sm = 0;
@@ -459,6 +584,14 @@ void force_impl(const Buffers& b, const SceneDev& s0, float4* force_out, cudaStr
     k<<<grid_size(k, BLOCK, sm, b.n), BLOCK, sm, st>>>(b.pos_s, b.vel_s, b.rhop, b.start, s0, b.scenes, b.nscene,
                                                        b.pos, b.vel, force_out, b.key, b.rank, b.count, b.n,
                                                        b.tile_stats);
+}
+
+template <bool B, int R>
+void density_nb_impl(const Buffers& b, const SceneDev& s0, int* nb, int* cnt, cudaStream_t st) {
+    auto k = k_density_nb<B, R, 128>;
+    constexpr size_t sm = force_smem<R, 128>();
+    k<<<grid_size(k, 128, sm, b.n), 128, sm, st>>>(b.pos_s, b.start, s0, b.scenes, b.nscene, b.rhop, nb, cnt, b.n,
+                                                   b.tile_stats);
 }
 
 template <bool B, int R, int BLOCK>
@@ -491,6 +624,14 @@ void init_step_kernels() {
     set_attrs<true, 1, 256>();
     set_attrs<true, 2, 128>();
     set_attrs<true, 2, 256>();
+    cudaFuncSetAttribute(k_density_nb<false, 1, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)force_smem<1, 128>());
+    cudaFuncSetAttribute(k_density_nb<false, 2, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)force_smem<2, 128>());
+    cudaFuncSetAttribute(k_density_nb<true, 1, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)force_smem<1, 128>());
+    cudaFuncSetAttribute(k_density_nb<true, 2, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)force_smem<2, 128>());
 }
 
 void launch_density(const Buffers& b, const SceneDev& s0, bool batched, const LaunchCfg& c, cudaStream_t st) {
@@ -509,6 +650,18 @@ void launch_force_integrate(const Buffers& b, const SceneDev& s0, bool batched, 
         dispatch(c.block, c.stencil, [&](auto R, auto BL) { force_impl<true, R.value, BL.value>(b, s0, f, st); });
     else
         dispatch(c.block, c.stencil, [&](auto R, auto BL) { force_impl<false, R.value, BL.value>(b, s0, f, st); });
+}
+
+void launch_density_nb(const Buffers& b, const SceneDev& s0, bool batched, const LaunchCfg& c, int* nb, int* cnt,
+                       cudaStream_t st) {
+    if (b.n <= 0) return;
+    if (batched) {
+        if (c.stencil == 2) density_nb_impl<true, 2>(b, s0, nb, cnt, st);
+        else density_nb_impl<true, 1>(b, s0, nb, cnt, st);
+    } else {
+        if (c.stencil == 2) density_nb_impl<false, 2>(b, s0, nb, cnt, st);
+        else density_nb_impl<false, 1>(b, s0, nb, cnt, st);
+    }
 }
 
 }  // namespace sphgb

@@ -67,7 +67,8 @@ class Diag(C.Structure):
 class LearnedReport(C.Structure):
     _fields_ = [("learned_macro_steps", C.c_uint64), ("plain_macro_steps", C.c_uint64), ("judged", C.c_uint64),
                 ("fallbacks", C.c_uint64), ("last_density_dev", C.c_double), ("last_momentum_dev", C.c_double),
-                ("max_density_dev", C.c_double), ("sum_density_dev", C.c_double)]
+                ("max_density_dev", C.c_double), ("sum_density_dev", C.c_double),
+                ("discarded_macro_steps", C.c_uint64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -364,12 +365,14 @@ class Net:
         self._check(lib.sph_mpnn_get_params(self._h, a.ctypes.data, len(a)))
         return a
 
-    def loss_grad(self, pos4, vel4, rhop2, nb, cnt, target4, fc):
+    def loss_grad(self, pos4, vel4, rhop2, nb, cnt, target8, fc):
+        """Loss, outputs (n x 8) and gradient of one host frame (sph_mpnn_loss_grad)."""
         n = len(pos4)
         arrs = [np.ascontiguousarray(x, dtype=t) for x, t in
                 ((pos4, np.float32), (vel4, np.float32), (rhop2, np.float32), (nb, np.int32), (cnt, np.int32),
-                 (target4, np.float32), (fc, np.float32))]
-        out = np.zeros((n, 4), dtype=np.float32)
+                 (target8, np.float32), (fc, np.float32))]
+        assert arrs[5].shape == (n, 8) and arrs[6].shape == (6,)
+        out = np.zeros((n, 8), dtype=np.float32)
         grad = np.zeros(self.n_params, dtype=np.float32)
         loss = C.c_double()
         self._check(lib.sph_mpnn_loss_grad(self._h, n, *[a.ctypes.data for a in arrs], C.byref(loss), out.ctypes.data,
@@ -377,11 +380,13 @@ class Net:
         return loss.value, out, grad
 
     def forward(self, pos4, vel4, rhop2, nb, cnt, fc, precision: int = 1) -> np.ndarray:
+        """Network outputs (n x 8: O_v, O_x, 0, 0) of a host frame (sph_mpnn_forward)."""
         n = len(pos4)
         arrs = [np.ascontiguousarray(x, dtype=t) for x, t in
                 ((pos4, np.float32), (vel4, np.float32), (rhop2, np.float32), (nb, np.int32), (cnt, np.int32),
                  (fc, np.float32))]
-        out = np.zeros((n, 4), dtype=np.float32)
+        assert arrs[5].shape == (6,)
+        out = np.zeros((n, 8), dtype=np.float32)
         self._check(lib.sph_mpnn_forward(self._h, n, *[a.ctypes.data for a in arrs], precision, out.ctypes.data))
         return out
 

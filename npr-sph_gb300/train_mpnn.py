@@ -11,8 +11,8 @@ and viscosity mu and the drop geometry are drawn from the seed:
   - odd runs: a lattice block in the lower corner, or a ball dropped from mid-height, of a cubic
     box, k ~ U[500, 3000], mu log-uniform in [0.1, 3000].
 Every `gap` steps each run contributes a frame: its state, the <= 32 nearest neighbours and
-density of every particle, and as target the velocity change of the next 4 plain steps (4*dt)
-from the forces. The network is then trained by Adam on the GPU (the library's own forward and
+density of every particle, and as targets the mean accelerations of the next 4 plain steps
+(the velocity head O_v and the position head O_x, in units of k/h) from the forces. The network is then trained by Adam on the GPU (the library's own forward and
 backward kernels), one frame per step, with a cosine-decayed learning rate.
 """
 from __future__ import annotations
@@ -114,7 +114,7 @@ def main() -> None:
 def init_params(seed: int) -> np.ndarray:
     """He-style initial parameters in the library's flat layout (sph_mpnn_set_params)."""
     rng = np.random.default_rng(seed)
-    W, FE, FN, FO = 64, 8, 8, 3
+    W, FE, FN, FO = 64, 8, 9, 6
     shapes = [("We1", (FE, W)), ("be1", (W,)), ("Wn1", (W + FN, W)), ("bn1", (W,)), ("Wp", (W, W)),
               ("We2", (FE, W)), ("be2", (W,)), ("Wn2", (2 * W, W)), ("bn2", (W,)), ("Wo", (W, FO)), ("bo", (FO,))]
     out = []

@@ -6,21 +6,24 @@ numpy float64, the network the GPU kernels of npr-sph_gb300/csrc/sph_mpnn.cu com
 can be checked against it.
 
 The network has no counterpart in the reference (NPR-SPH has no learned component). It
-predicts, per particle, the velocity change over a macro-step of 4*dt from the particle's
-neighbourhood:
+predicts, per particle, the mean accelerations of the next 4 plain steps (a macro-step of
+4*dt) from the particle's neighbourhood:
 
   edge features  e_ij = [ (x_j-x_i)/h (3), (v_j-v_i)/c (3), r/h, 1-r/h ]          (8)
   node features  n_i  = [ v_i/c (3), rho_i/rho_self - 1, (rho_i-rho0)/rho_self,
-                          log10(mu)/4, cnt_i/K, 1 ]                                 (8)
+                          log10(mu)/4, cnt_i/K, 1, c*dt/h ]                         (9)
   round 1   Z1_ij = e_ij We1 + be1,  M1_i = sum_j relu(Z1_ij) / K
             Y1_i  = [M1_i, n_i] Wn1 + bn1,  H1_i = relu(Y1_i),  P_i = H1_i Wp
   round 2   Z2_ij = e_ij We2 + P_j + be2,  M2_i = sum_j relu(Z2_ij) / K
             Y2_i  = [M2_i, H1_i] Wn2 + bn2,  H2_i = relu(Y2_i)
-  output    O_i = H2_i Wo + bo  = predicted (v(t+4dt) - v(t)) / c                   (3)
+  output    O_i = H2_i Wo + bo = (O_v, O_x)                                          (6)
+            O_v = (a_0 + a_1 + a_2 + a_3) / (4A),  O_x = (4 a_0 + 3 a_1 + 2 a_2 + a_3) / (10A)
 
+with a_s the SPH acceleration F/rho of plain sub-step s and A = k/h; the macro-step is then
+v' = v + 4 dt A O_v, x' = x + 4 dt v + 10 dt^2 A O_x (exact for 4 symplectic sub-steps).
 j runs over the (at most K = 32) nearest neighbours of i with r < h, i excluded;
 c = sqrt(k) is the sound speed of the linear EOS; rho_self = m*315/(64*pi*h^3).
-Loss: mean over particles of |O_i - target_i|^2 (target = velocity change / c).
+Loss: mean over particles of |O_i - target_i|^2.
 """
 from __future__ import annotations
 
@@ -29,8 +32,8 @@ import numpy as np
 K = 32
 W = 64
 FE = 8
-FN = 8
-FO = 3
+FN = 9
+FO = 6
 
 # Flat parameter layout (float32 on the GPU), in this order.
 LAYOUT = [("We1", (FE, W)), ("be1", (W,)), ("Wn1", (W + FN, W)), ("bn1", (W,)), ("Wp", (W, W)),
@@ -68,8 +71,8 @@ def init_params(seed: int = 0) -> np.ndarray:
     return pack(p).astype(np.float32)
 
 
-def features(pos, vel, rho, nb, cnt, h, c, rho_self, rho0, mu):
-    """Edge features e (n, K, 8) with padded edges zeroed, edge mask (n, K), node features (n, 8)."""
+def features(pos, vel, rho, nb, cnt, h, c, rho_self, rho0, mu, dt):
+    """Edge features e (n, K, 8) with padded edges zeroed, edge mask (n, K), node features (n, 9)."""
     pos = np.asarray(pos, np.float64)
     vel = np.asarray(vel, np.float64)
     n = len(pos)
@@ -88,6 +91,7 @@ def features(pos, vel, rho, nb, cnt, h, c, rho_self, rho0, mu):
     nf[:, 5] = np.log10(mu) / 4.0
     nf[:, 6] = np.asarray(cnt, np.float64) / K
     nf[:, 7] = 1.0
+    nf[:, 8] = c * dt / h
     return e, mask, nf
 
 
