@@ -295,6 +295,41 @@ sph_status sph_refresh_density(sph_ctx* ctx);
 sph_status sph_reduce_aos_noalloc(const sph_particle* dev_particles, uint32_t n, const sph_params* p,
                                   double* dev_sums, void* stream);
 
+/* ---- snapshots and trajectories (new; no reference counterpart) --------
+ * The reference keeps its state only in the GL buffer and re-creates it on 'r'
+ * (Main.cpp:460-464). A snapshot file holds what resumes a run bit for bit:
+ * the records in caller order, the uniforms and particle count of every scene
+ * and the step count, with a checksum. A trajectory file is the same header
+ * followed by frames appended during a run. Format (little-endian):
+ *   64-byte header: magic "NPRSPHS1" (snapshot) / "NPRSPHT1" (trajectory),
+ *     u32 version 1, u32 header bytes 64, u64 particles, u32 scenes, u32 0,
+ *     u64 step count (trajectory: 0), u64 seed (a caller tag), u64 checksum
+ *     (snapshot: of all bytes after the header; trajectory: of the scene
+ *     table), u64 0;
+ *   scene table: scenes x sph_params, scenes x u32 counts, zero padding to a
+ *     multiple of 64 bytes;
+ *   snapshot: particles x sph_particle;
+ *   trajectory frames: u64 step, u64 particles, u64 checksum of the records,
+ *     u64 0, particles x sph_particle.
+ * Checksum: FNV-1a 64 over the 64-bit little-endian words of the bytes (a final
+ * partial word zero-padded), sph_checksum64. */
+typedef struct sph_trajectory sph_trajectory;
+
+sph_status sph_snapshot_save(sph_ctx* ctx, const char* path, uint64_t seed);
+/* Header fields of a snapshot file (no GPU needed). */
+sph_status sph_snapshot_info(const char* path, uint64_t* n, uint32_t* n_scene, uint64_t* steps, uint64_t* seed);
+/* SPH_OK when the file is a complete snapshot whose checksum matches (no GPU needed). */
+sph_status sph_snapshot_verify(const char* path);
+/* A new context (single-scene or batch, as saved) holding the snapshot's particles and
+ * uniforms, with the step count continued. A file that fails verification is refused. */
+sph_status sph_snapshot_load(const char* path, void* stream, sph_ctx** out);
+sph_status sph_trajectory_create(sph_ctx* ctx, const char* path, uint64_t seed, sph_trajectory** out);
+/* Append the context's current records as one frame. */
+sph_status sph_trajectory_append(sph_trajectory* t, sph_ctx* ctx);
+uint64_t sph_trajectory_frames(const sph_trajectory* t);
+sph_status sph_trajectory_close(sph_trajectory* t);
+uint64_t sph_checksum64(const void* data, uint64_t bytes);
+
 /* ---- scene generators (host only; no GPU needed) ----------------------- */
 
 /* The reference's make_grid()+init_particles() (Main.cpp:488-539): 10x100x10

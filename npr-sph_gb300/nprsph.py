@@ -121,6 +121,16 @@ _SIGS = {
     "sph_mpnn_train": (C.c_int32, [_P, C.c_uint32, C.c_float, C.c_uint64, _P]),
     "sph_learned_step": (C.c_int32, [_P, _P, C.c_int32, C.c_int32, C.c_float, C.c_float, C.POINTER(LearnedReport)]),
     "sph_refresh_density": (C.c_int32, [_P]),
+    "sph_snapshot_save": (C.c_int32, [_P, C.c_char_p, C.c_uint64]),
+    "sph_snapshot_info": (C.c_int32, [C.c_char_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32),
+                                      C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    "sph_snapshot_verify": (C.c_int32, [C.c_char_p]),
+    "sph_snapshot_load": (C.c_int32, [C.c_char_p, _P, C.POINTER(_P)]),
+    "sph_trajectory_create": (C.c_int32, [_P, C.c_char_p, C.c_uint64, C.POINTER(_P)]),
+    "sph_trajectory_append": (C.c_int32, [_P, _P]),
+    "sph_trajectory_frames": (C.c_uint64, [_P]),
+    "sph_trajectory_close": (C.c_int32, [_P]),
+    "sph_checksum64": (C.c_uint64, [_P, C.c_uint64]),
     "sph_scene_reference_grid": (C.c_int32, [_P, C.c_uint32, C.c_float]),
     "sph_scene_fill": (C.c_int32, [_P, C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_float,
                                    C.c_float, C.c_uint64]),
@@ -181,6 +191,99 @@ def empty_particles(n: int) -> np.ndarray:
     return np.zeros(n, dtype=PARTICLE_DTYPE)
 
 
+# ---- snapshot and trajectory files (format in include/sph_gb300.h) --------------------------
+
+_HEADER_DTYPE = np.dtype([("magic", "S8"), ("version", "<u4"), ("header_bytes", "<u4"), ("n", "<u8"),
+                          ("scenes", "<u4"), ("reserved0", "<u4"), ("steps", "<u8"), ("seed", "<u8"),
+                          ("checksum", "<u8"), ("reserved1", "<u8")])
+_FRAME_HEAD = np.dtype([("step", "<u8"), ("n", "<u8"), ("checksum", "<u8"), ("reserved", "<u8")])
+
+
+def checksum64(data) -> int:
+    """FNV-1a 64 over 64-bit little-endian words (sph_checksum64)."""
+    b = np.ascontiguousarray(np.frombuffer(memoryview(data).cast("B"), dtype=np.uint8))
+    return int(lib.sph_checksum64(b.ctypes.data, b.nbytes))
+
+
+def _read_head(raw: np.ndarray, magic: bytes):
+    h = raw[:64].view(_HEADER_DTYPE)[0]
+    if h["magic"] != magic or h["version"] != 1 or h["header_bytes"] != 64:
+        raise ValueError("not a %s file" % magic.decode())
+    scenes = int(h["scenes"])
+    tb = (scenes * (96 + 4) + 63) // 64 * 64
+    table = raw[64:64 + tb]
+    params = [Params.from_buffer_copy(table[96 * i:96 * (i + 1)].tobytes()) for i in range(scenes)]
+    counts = table[96 * scenes:96 * scenes + 4 * scenes].view("<u4").copy()
+    return h, params, counts, 64 + tb
+
+
+def snapshot_info(path) -> dict:
+    n, sc, steps, seed = C.c_uint64(), C.c_uint32(), C.c_uint64(), C.c_uint64()
+    _check(lib.sph_snapshot_info(str(path).encode(), C.byref(n), C.byref(sc), C.byref(steps), C.byref(seed)),
+           what="sph_snapshot_info")
+    return {"n": n.value, "scenes": sc.value, "steps": steps.value, "seed": seed.value}
+
+
+def snapshot_verify(path) -> bool:
+    return lib.sph_snapshot_verify(str(path).encode()) == 0
+
+
+def read_snapshot(path) -> dict:
+    """Header, uniforms, scene counts and records of a snapshot file (numpy, no GPU)."""
+    raw = np.fromfile(path, dtype=np.uint8)
+    h, params, counts, off = _read_head(raw, b"NPRSPHS1")
+    n = int(h["n"])
+    recs = raw[off:off + 64 * n].view(PARTICLE_DTYPE)
+    if len(recs) != n:
+        raise ValueError("truncated snapshot")
+    return {"n": n, "steps": int(h["steps"]), "seed": int(h["seed"]), "checksum": int(h["checksum"]),
+            "params": params, "counts": counts, "particles": recs}
+
+
+def read_trajectory(path) -> dict:
+    """Header, uniforms, scene counts and frames [(step, records)] of a trajectory file."""
+    raw = np.fromfile(path, dtype=np.uint8)
+    h, params, counts, off = _read_head(raw, b"NPRSPHT1")
+    n = int(h["n"])
+    frames = []
+    while off + 32 <= len(raw):
+        fh = raw[off:off + 32].view(_FRAME_HEAD)[0]
+        if int(fh["n"]) != n or off + 32 + 64 * n > len(raw):
+            raise ValueError("truncated or inconsistent frame")
+        recs = raw[off + 32:off + 32 + 64 * n].view(PARTICLE_DTYPE)
+        if checksum64(recs) != int(fh["checksum"]):
+            raise ValueError("frame checksum mismatch at step %d" % int(fh["step"]))
+        frames.append((int(fh["step"]), recs))
+        off += 32 + 64 * n
+    return {"n": n, "seed": int(h["seed"]), "params": params, "counts": counts, "frames": frames}
+
+
+class Trajectory:
+    """Append-only trajectory file of a context (sph_trajectory_*)."""
+
+    def __init__(self, sim: "Sim", path, seed: int = 0):
+        self._t = C.c_void_p()
+        _check(lib.sph_trajectory_create(sim.ctx, str(path).encode(), int(seed), C.byref(self._t)), sim.ctx)
+
+    def append(self, sim: "Sim") -> None:
+        _check(lib.sph_trajectory_append(self._t, sim.ctx), sim.ctx)
+
+    @property
+    def frames(self) -> int:
+        return int(lib.sph_trajectory_frames(self._t))
+
+    def close(self) -> None:
+        if self._t:
+            _check(lib.sph_trajectory_close(self._t), what="sph_trajectory_close")
+            self._t = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
 def _ptr(a) -> int:
     if isinstance(a, np.ndarray):
         if not a.flags["C_CONTIGUOUS"]:
@@ -205,6 +308,20 @@ class Sim:
                                         C.byref(self._ctx)), what="sph_create_batch")
             self.n_scene = len(counts)
             self._counts = counts
+
+    @classmethod
+    def from_snapshot(cls, path, stream=None) -> "Sim":
+        """A context restored from a snapshot file (sph_snapshot_load)."""
+        obj = cls.__new__(cls)
+        obj._ctx = C.c_void_p()
+        s = C.c_void_p(int(stream) if stream is not None else 0)
+        _check(lib.sph_snapshot_load(str(path).encode(), s, C.byref(obj._ctx)), what="sph_snapshot_load")
+        obj.n_scene = int(lib.sph_num_scenes(obj._ctx))
+        return obj
+
+    def save(self, path, seed: int = 0) -> None:
+        """Write a snapshot file (sph_snapshot_save)."""
+        _check(lib.sph_snapshot_save(self._ctx, str(path).encode(), int(seed)), self._ctx)
 
     def close(self) -> None:
         if self._ctx:
