@@ -228,7 +228,39 @@ def extra_workloads(args, stream) -> dict:
             "value": len(sc.particles) * args.extra_steps / sec, "unit": UNIT, "particles": len(sc.particles),
             "steps": args.extra_steps, "ms_per_step": 1e3 * sec / args.extra_steps,
             "workload": "10,000 particles, 0.5h lattice in the lower-corner quarter of the reference box"}
+    out["render_1m"] = render_workload(stream)
     return out
+
+
+def render_workload(stream, frames: int = 20) -> dict:
+    """The toon draw of the 1M dam break after 200 steps (sph_render into a device buffer,
+    1920 x 1080, 4-pixel sprites), timed with CUDA events per frame."""
+    import torch
+    import nprsph as S
+
+    sc = S.dam_break(seed=2)
+    w, h = 1920, 1080
+    v = S.view_default(w, h, 1.0)
+    S.view_camera(v, 0.0, 1.0, (2.56, 2.5, 6.0), (2.56, 0.5, 0.64))
+    v.point_size = 4.0
+    img = torch.zeros(w * h * 4, dtype=torch.uint8, device="cuda")
+    with S.Sim(sc.params, n_max=len(sc.particles), stream=stream.cuda_stream) as sim:
+        sim.upload(sc.particles)
+        sim.step(200)
+        for _ in range(3):
+            sim.render_device(v, img.data_ptr())
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(frames):
+            sim.render_device(v, img.data_ptr())
+        b.record(stream)
+        torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / frames
+    return {"frames_per_s": 1e3 / ms, "ms_per_frame": ms, "particles": len(sc.particles), "image": [w, h],
+            "point_size": 4.0, "frames": frames,
+            "workload": "toon draw (splat + depth test + cel shading + Sobel outline) of the 1M dam break at step "
+                        "200 into a device RGBA8 buffer"}
 
 
 WEIGHTS = REPO / "npr-sph_gb300" / "weights" / "mpnn_w64.npy"

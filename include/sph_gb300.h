@@ -295,6 +295,60 @@ sph_status sph_refresh_density(sph_ctx* ctx);
 sph_status sph_reduce_aos_noalloc(const sph_particle* dev_particles, uint32_t n, const sph_params* p,
                                   double* dev_sums, void* stream);
 
+/* ---- headless toon rendering of the particles ----------------------------
+ * The reference draws the particles after the step (Main.cpp:311-337, SPH
+ * mode): GL point sprites of sim_rad pixels through toon_vs.glsl /
+ * toon_fs.glsl in two passes. Pass 0 writes a coverage texture (its green
+ * channel is a flat depth 1.0, toon_vs.glsl:44); pass 1 shades each fragment
+ * with the cel model (toon_fs.glsl:90-124) and draws a Sobel outline where the
+ * 3x3 neighbourhood of the coverage texture has a gradient (:126-153). This
+ * library renders the same image with CUDA kernels into an RGBA8 buffer, rows
+ * bottom to top as GL stores them; there is no window, GL context or swapchain.
+ * The restated pipeline, per particle i (record order = draw order):
+ *   clip = (P V M)(x_i, 1); kept when w > 0 and |x|,|y|,|z| <= w;
+ *   window x_w = (x/w + 1) W/2, y_w = (y/w + 1) H/2, depth d = (z/w + 1)/2,
+ *     quantised to 24 bits;
+ *   covered pixels: centres within [x_w - s/2, x_w + s/2) x [y_w - s/2, y_w + s/2)
+ *     (s = point_size), with p = ((c_x - x_w), -(c_y - y_w)) / (s/2) and |p|^2 <= 1
+ *     (toon_fs.glsl:97-99);
+ *   depth test GL_LESS: per pixel the smallest (d, i) wins;
+ *   normal n = normalize(p.x, p.y, sqrt(1 - |p|^2)), pw = M (x_i, 1),
+ *   l = normalize(light - pw), v = normalize(eye - pw), r = normalize(reflect(-l, n));
+ *   colour = dark if dot(n, l) < 0 else midtone; highlight if dot(r, v) > 0 and
+ *     dot(r, v) > 0.95^(1/shininess) (the exact form of pow(dot(r,v), shininess) > 0.95);
+ *   outline colour where the Sobel gradient of the coverage (outside the image:
+ *     uncovered) is non-zero; clear colour where nothing is covered; alpha 1.
+ * Every operation is FP32 with round-to-nearest, so the CPU restatement
+ * matches the image byte for byte. */
+typedef struct sph_view {
+    float model[16];       /* M, column-major (glm): rotate(angle, y) * scale (Main.cpp:256) */
+    float view[16];        /* V = lookAt(eye, center, up y) (Main.cpp:257) */
+    float proj[16];        /* P = perspective(pi/4, aspect, 0.1, 100) (Main.cpp:258) */
+    float eye_w[4];        /* SceneUniforms.eye_w (Main.cpp:105) */
+    float light_w[4];      /* SceneUniforms.light_w (Main.cpp:106) */
+    float dark[4];         /* MaterialUniforms (Main.cpp:126-133) */
+    float midtone[4];
+    float highlight[4];
+    float outline[4];
+    float clear_color[4];  /* clear_color (Main.cpp:80) */
+    float shininess;       /* 0.3; >= 0 */
+    float point_size;      /* sim_rad, pixels (Main.cpp:88): 10 */
+    int32_t width, height;
+} sph_view;
+
+/* The reference's initial view (Main.cpp:80-89, :105-106, :126-133, :254-260): angle 0.75,
+ * scale 2.5 (times model_scale, the loaded mesh's mScaleFactor in the reference), eye
+ * (10, 2, 0) looking at the origin, light (0, 1, 1), aspect width/height. */
+sph_status sph_view_default(sph_view* v, int32_t width, int32_t height, float model_scale);
+/* M, V and P as sendUniforms builds them (Main.cpp:256-258) for the given camera. */
+sph_status sph_view_camera(sph_view* v, float angle, float scale, const float eye[3], const float center[3]);
+/* Render the context's particles (a single-scene context, or scene `scene` of a batch) into
+ * rgba (width x height x 4 bytes, rows bottom to top), in device memory when rgba_on_device,
+ * else in host memory. */
+sph_status sph_render(sph_ctx* ctx, const sph_view* v, uint32_t scene, uint8_t* rgba, int32_t rgba_on_device);
+/* Write an RGBA8 image (rows bottom to top) as a binary PPM (rows top to bottom, RGB). */
+sph_status sph_image_write_ppm(const char* path, const uint8_t* rgba, int32_t width, int32_t height);
+
 /* ---- snapshots and trajectories (new; no reference counterpart) --------
  * The reference keeps its state only in the GL buffer and re-creates it on 'r'
  * (Main.cpp:460-464). A snapshot file holds what resumes a run bit for bit:

@@ -40,6 +40,9 @@ struct sph_ctx {
     uint32_t* q_cnt = nullptr;
     unsigned long long* q_dig = nullptr;
     int q_cap = 0;
+    // render scratch (sph_render): depth/id keys, positions by id, a device image for host output
+    void* render_buf = nullptr;
+    size_t render_cap = 0;
 };
 
 namespace sphgb {

@@ -365,7 +365,8 @@ sph_status sph_destroy(sph_ctx* ctx) {
     Buffers& b = ctx->b;
     void* ptrs[] = {b.pos, b.vel, b.pos_s, b.vel_s, b.rhop, b.force_s, b.force_up, b.aux, b.aos, b.key, b.rank,
                     b.perm, b.count, b.start, b.scan_state, b.scan_ticket, b.slot_of_id, b.err, b.partials,
-                    b.scenes, b.tile_stats, ctx->diag_dev, ctx->scene_first_dev, ctx->q_ids, ctx->q_cnt, ctx->q_dig};
+                    b.scenes, b.tile_stats, ctx->diag_dev, ctx->scene_first_dev, ctx->q_ids, ctx->q_cnt, ctx->q_dig,
+                    ctx->render_buf};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (auto& e : ctx->ev)

@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <vector>
 
@@ -216,6 +217,130 @@ sph_status sph_scene_slosh(sph_particle* out, uint32_t n, float amplitude, float
     for (uint32_t i = 0; i < n; ++i)
         out[i].vel[0] += (float)(amplitude * std::sin(M_PI * ((double)out[i].pos[0] - x0) / length));
     return SPH_OK;
+}
+
+}  // extern "C"
+
+// ---- views for sph_render ----------------------------------------------------------------
+// Column-major 4x4 matrices as glm stores them: m[4 * column + row]. The formulas are the
+// standard OpenGL ones (glm::rotate, glm::scale, glm::lookAt, glm::perspective), computed in
+// FP64 and rounded once.
+namespace {
+
+void mat_mul(const double* a, const double* b, double* out) {
+    for (int c = 0; c < 4; ++c)
+        for (int r = 0; r < 4; ++r) {
+            double s = 0.0;
+            for (int k = 0; k < 4; ++k) s += a[4 * k + r] * b[4 * c + k];
+            out[4 * c + r] = s;
+        }
+}
+
+// M = rotate(angle, (0, 1, 0)) * scale(s, s, s) (Main.cpp:256)
+void model_matrix(double angle, double s, double* m) {
+    const double c = std::cos(angle), sn = std::sin(angle);
+    double rot[16] = {c, 0, -sn, 0, 0, 1, 0, 0, sn, 0, c, 0, 0, 0, 0, 1};
+    double sc[16] = {s, 0, 0, 0, 0, s, 0, 0, 0, 0, s, 0, 0, 0, 0, 1};
+    mat_mul(rot, sc, m);
+}
+
+// V = lookAt(eye, center, up = (0, 1, 0)) (Main.cpp:257), right-handed
+void view_matrix(const double* eye, const double* center, double* v) {
+    double f[3] = {center[0] - eye[0], center[1] - eye[1], center[2] - eye[2]};
+    const double fl = std::sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
+    for (double& x : f) x /= fl;
+    const double up[3] = {0.0, 1.0, 0.0};
+    double s[3] = {f[1] * up[2] - f[2] * up[1], f[2] * up[0] - f[0] * up[2], f[0] * up[1] - f[1] * up[0]};
+    const double sl = std::sqrt(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
+    for (double& x : s) x /= sl;
+    const double u[3] = {s[1] * f[2] - s[2] * f[1], s[2] * f[0] - s[0] * f[2], s[0] * f[1] - s[1] * f[0]};
+    std::memset(v, 0, 16 * sizeof(double));
+    for (int k = 0; k < 3; ++k) {
+        v[4 * k + 0] = s[k];
+        v[4 * k + 1] = u[k];
+        v[4 * k + 2] = -f[k];
+    }
+    v[12] = -(s[0] * eye[0] + s[1] * eye[1] + s[2] * eye[2]);
+    v[13] = -(u[0] * eye[0] + u[1] * eye[1] + u[2] * eye[2]);
+    v[14] = f[0] * eye[0] + f[1] * eye[1] + f[2] * eye[2];
+    v[15] = 1.0;
+}
+
+// P = perspective(fovy, aspect, near, far) (Main.cpp:258), clip depth -1..1
+void proj_matrix(double fovy, double aspect, double zn, double zf, double* p) {
+    const double t = std::tan(fovy / 2.0);
+    std::memset(p, 0, 16 * sizeof(double));
+    p[0] = 1.0 / (aspect * t);
+    p[5] = 1.0 / t;
+    p[10] = -(zf + zn) / (zf - zn);
+    p[11] = -1.0;
+    p[14] = -(2.0 * zf * zn) / (zf - zn);
+}
+
+void put(float* dst, const double* src) {
+    for (int i = 0; i < 16; ++i) dst[i] = (float)src[i];
+}
+
+void set4(float* d, float a, float b, float c, float w) {
+    d[0] = a;
+    d[1] = b;
+    d[2] = c;
+    d[3] = w;
+}
+
+}  // namespace
+
+extern "C" {
+
+sph_status sph_view_camera(sph_view* v, float angle, float scale, const float eye[3], const float center[3]) {
+    if (!v || !eye || !center || v->width <= 0 || v->height <= 0) return SPH_ERR_INVALID_ARG;
+    const double e[3] = {eye[0], eye[1], eye[2]}, c[3] = {center[0], center[1], center[2]};
+    if (e[0] == c[0] && e[1] == c[1] && e[2] == c[2]) return SPH_ERR_INVALID_ARG;
+    double m[16], vw[16], pr[16];
+    model_matrix(angle, scale, m);
+    view_matrix(e, c, vw);
+    proj_matrix(M_PI / 4.0, (double)v->width / (double)v->height, 0.1, 100.0, pr);
+    put(v->model, m);
+    put(v->view, vw);
+    put(v->proj, pr);
+    set4(v->eye_w, eye[0], eye[1], eye[2], 1.0f);
+    return SPH_OK;
+}
+
+sph_status sph_view_default(sph_view* v, int32_t width, int32_t height, float model_scale) {
+    if (!v || width <= 0 || height <= 0 || !(model_scale > 0.0f)) return SPH_ERR_INVALID_ARG;
+    std::memset(v, 0, sizeof(*v));
+    v->width = width;
+    v->height = height;
+    const float eye[3] = {10.0f, 2.0f, 0.0f}, center[3] = {0.0f, 0.0f, 0.0f};  // Main.cpp:89, :105
+    sph_status st = sph_view_camera(v, 0.75f, 2.5f * model_scale, eye, center);  // Main.cpp:82-83
+    if (st) return st;
+    set4(v->light_w, 0.0f, 1.0f, 1.0f, 1.0f);        // Main.cpp:106
+    set4(v->dark, 0.0f, 0.0f, 0.0f, 1.0f);           // Main.cpp:127-130
+    set4(v->midtone, 0.5f, 0.5f, 0.5f, 1.0f);
+    set4(v->highlight, 1.0f, 1.0f, 1.0f, 1.0f);
+    set4(v->outline, 0.0f, 0.0f, 0.0f, 1.0f);
+    set4(v->clear_color, 0.5f, 0.5f, 0.5f, 1.0f);    // Main.cpp:80
+    v->shininess = 0.3f;                             // Main.cpp:131
+    v->point_size = 10.0f;                           // simulation_radius, Main.cpp:88
+    return SPH_OK;
+}
+
+sph_status sph_image_write_ppm(const char* path, const uint8_t* rgba, int32_t width, int32_t height) {
+    if (!path || !rgba || width <= 0 || height <= 0) return SPH_ERR_INVALID_ARG;
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return SPH_ERR_INVALID_ARG;
+    std::fprintf(f, "P6\n%d %d\n255\n", width, height);
+    std::vector<unsigned char> row((size_t)width * 3);
+    bool ok = true;
+    for (int y = height - 1; y >= 0 && ok; --y) {  // GL rows are bottom to top
+        const uint8_t* src = rgba + (size_t)y * width * 4;
+        for (int x = 0; x < width; ++x)
+            for (int k = 0; k < 3; ++k) row[(size_t)3 * x + k] = src[(size_t)4 * x + k];
+        ok = std::fwrite(row.data(), 1, row.size(), f) == row.size();
+    }
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? SPH_OK : SPH_ERR_INVALID_ARG;
 }
 
 }  // extern "C"

@@ -10,10 +10,14 @@
 // Keys come from a script instead of GLFW: --keys "p@0,r@500,p@501" presses a key at a frame.
 // Every --report frames one JSON line goes to stdout: frame, steps, wall time per frame and the
 // FP64 diagnostics (sph_reduce). --scene dam_break runs the 1,048,576-particle dam break instead
-// of the reference's 10,000-particle lattice.
+// of the reference's 10,000-particle lattice. --render-every N draws the particles every N
+// frames (the toon pass of display(), Main.cpp:311-337, through sph_render) and writes
+// <prefix>_<frame>.ppm: the headless stand-in for the window and the video capture
+// (Main.cpp:377-384).
 //
 //   sph_headless [--frames N] [--keys "p@0"] [--report N] [--scene reference|dam_break]
 //                [--visc V] [--smoothing S] [--mass M] [--rest-rho R]
+//                [--render-every N] [--render-prefix P] [--size WxH]
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -33,6 +37,9 @@ struct Options {
     std::string scene = "reference";
     std::map<int, std::string> keys;  // frame -> keys pressed
     float visc = -1, smoothing = -1, mass = -1, rest_rho = -1;
+    int render_every = 0;
+    std::string render_prefix = "frame";
+    int width = 720, height = 720;  // init_window_width/height (Main.cpp:39-40)
 };
 
 bool parse(int argc, char** argv, Options& o) {
@@ -49,6 +56,11 @@ bool parse(int argc, char** argv, Options& o) {
         else if (a == "--smoothing") o.smoothing = (float)std::atof(next("--smoothing"));
         else if (a == "--mass") o.mass = (float)std::atof(next("--mass"));
         else if (a == "--rest-rho") o.rest_rho = (float)std::atof(next("--rest-rho"));
+        else if (a == "--render-every") o.render_every = std::atoi(next("--render-every"));
+        else if (a == "--render-prefix") o.render_prefix = next("--render-prefix");
+        else if (a == "--size") {
+            if (std::sscanf(next("--size"), "%dx%d", &o.width, &o.height) != 2) return false;
+        }
         else if (a == "--keys") {
             std::string s = next("--keys");
             size_t p = 0;
@@ -66,7 +78,8 @@ bool parse(int argc, char** argv, Options& o) {
             return false;
         }
     }
-    return o.frames >= 0 && o.report > 0 && (o.scene == "reference" || o.scene == "dam_break");
+    return o.frames >= 0 && o.report > 0 && o.render_every >= 0 && o.width > 0 && o.height > 0 &&
+           (o.scene == "reference" || o.scene == "dam_break");
 }
 
 // The scene the 'r' key re-creates.
@@ -104,11 +117,25 @@ void report(sph_ctx* ctx, int frame, double ms_per_frame) {
 
 }  // namespace
 
+// The view of a scene: the reference's initial camera for its own lattice; for the dam break a
+// camera that sees its 5.12 x 1.28 x 1.28 box.
+sph_view make_view(const Options& o) {
+    sph_view v;
+    sph_view_default(&v, o.width, o.height, 1.0f);
+    if (o.scene == "dam_break") {
+        const float eye[3] = {2.56f, 2.5f, 6.0f}, center[3] = {2.56f, 0.5f, 0.64f};
+        sph_view_camera(&v, 0.0f, 1.0f, eye, center);
+        v.point_size = 4.0f;
+    }
+    return v;
+}
+
 int main(int argc, char** argv) {
     Options o;
     if (!parse(argc, argv, o)) {
         std::fprintf(stderr, "usage: %s [--frames N] [--keys \"p@0,r@500\"] [--report N] "
-                             "[--scene reference|dam_break] [--visc V] [--smoothing S] [--mass M] [--rest-rho R]\n",
+                             "[--scene reference|dam_break] [--visc V] [--smoothing S] [--mass M] [--rest-rho R] "
+                             "[--render-every N] [--render-prefix P] [--size WxH]\n",
                      argv[0]);
         return 2;
     }
@@ -124,6 +151,8 @@ int main(int argc, char** argv) {
         std::fprintf(stderr, "upload: %s\n", sph_last_error(ctx));
         return 1;
     }
+    const sph_view view = make_view(o);
+    std::vector<uint8_t> image(o.render_every > 0 ? (size_t)o.width * o.height * 4 : 0);
     bool simulate = false;  // Main.cpp:87: a zero-initialised global, so the simulation starts paused
     auto t0 = std::chrono::steady_clock::now();
     int frames_since = 0;
@@ -151,6 +180,15 @@ int main(int argc, char** argv) {
         if (o.mass > 0) p.mass = o.mass;
         if (o.rest_rho > 0) p.resting_rho = o.rest_rho;
         if (sph_set_params(ctx, &p) != SPH_OK) std::fprintf(stderr, "uniforms: %s\n", sph_last_error(ctx));
+        if (o.render_every > 0 && (frame + 1) % o.render_every == 0) {
+            char name[4096];
+            std::snprintf(name, sizeof(name), "%s_%05d.ppm", o.render_prefix.c_str(), frame + 1);
+            if (sph_render(ctx, &view, 0, image.data(), 0) != SPH_OK ||
+                sph_image_write_ppm(name, image.data(), o.width, o.height) != SPH_OK) {
+                std::fprintf(stderr, "render: %s\n", sph_last_error(ctx));
+                return 1;
+            }
+        }
         ++frames_since;
         if ((frame + 1) % o.report == 0 || frame + 1 == o.frames) {
             if (sph_synchronize(ctx) != SPH_OK) {

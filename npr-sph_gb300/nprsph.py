@@ -74,6 +74,18 @@ class LearnedReport(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class View(C.Structure):
+    """sph_view: camera, light, material and image size of sph_render."""
+    _fields_ = [("model", C.c_float * 16), ("view", C.c_float * 16), ("proj", C.c_float * 16),
+                ("eye_w", C.c_float * 4), ("light_w", C.c_float * 4), ("dark", C.c_float * 4),
+                ("midtone", C.c_float * 4), ("highlight", C.c_float * 4), ("outline", C.c_float * 4),
+                ("clear_color", C.c_float * 4), ("shininess", C.c_float), ("point_size", C.c_float),
+                ("width", C.c_int32), ("height", C.c_int32)]
+
+
+assert C.sizeof(View) == 320
+
+
 # Every symbol of include/sph_gb300.h with its ctypes signature.
 _P = C.c_void_p
 _SIGS = {
@@ -121,6 +133,11 @@ _SIGS = {
     "sph_mpnn_train": (C.c_int32, [_P, C.c_uint32, C.c_float, C.c_uint64, _P]),
     "sph_learned_step": (C.c_int32, [_P, _P, C.c_int32, C.c_int32, C.c_float, C.c_float, C.POINTER(LearnedReport)]),
     "sph_refresh_density": (C.c_int32, [_P]),
+    "sph_view_default": (C.c_int32, [C.POINTER(View), C.c_int32, C.c_int32, C.c_float]),
+    "sph_view_camera": (C.c_int32, [C.POINTER(View), C.c_float, C.c_float, C.POINTER(C.c_float),
+                                    C.POINTER(C.c_float)]),
+    "sph_render": (C.c_int32, [_P, C.POINTER(View), C.c_uint32, _P, C.c_int32]),
+    "sph_image_write_ppm": (C.c_int32, [C.c_char_p, _P, C.c_int32, C.c_int32]),
     "sph_snapshot_save": (C.c_int32, [_P, C.c_char_p, C.c_uint64]),
     "sph_snapshot_info": (C.c_int32, [C.c_char_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32),
                                       C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
@@ -189,6 +206,25 @@ def grid_dims(p: Params) -> tuple[float, tuple[int, int, int]]:
 
 def empty_particles(n: int) -> np.ndarray:
     return np.zeros(n, dtype=PARTICLE_DTYPE)
+
+
+# ---- views and images (sph_render) -----------------------------------------------------------
+
+def view_default(width: int = 720, height: int = 720, model_scale: float = 1.0) -> View:
+    v = View()
+    _check(lib.sph_view_default(C.byref(v), width, height, model_scale), what="sph_view_default")
+    return v
+
+
+def view_camera(v: View, angle: float, scale: float, eye, center) -> View:
+    _check(lib.sph_view_camera(C.byref(v), angle, scale, _f3(eye), _f3(center)), what="sph_view_camera")
+    return v
+
+
+def write_ppm(path, rgba: np.ndarray) -> None:
+    rgba = np.ascontiguousarray(rgba, dtype=np.uint8)
+    h, w, _ = rgba.shape
+    _check(lib.sph_image_write_ppm(str(path).encode(), rgba.ctypes.data, w, h), what="sph_image_write_ppm")
 
 
 # ---- snapshot and trajectory files (format in include/sph_gb300.h) --------------------------
@@ -318,6 +354,18 @@ class Sim:
         _check(lib.sph_snapshot_load(str(path).encode(), s, C.byref(obj._ctx)), what="sph_snapshot_load")
         obj.n_scene = int(lib.sph_num_scenes(obj._ctx))
         return obj
+
+    def render(self, view: View, scene: int = 0, out: np.ndarray | None = None) -> np.ndarray:
+        """Toon render of the particles (sph_render): (height, width, 4) uint8, rows bottom to top."""
+        if out is None:
+            out = np.zeros((view.height, view.width, 4), dtype=np.uint8)
+        assert out.shape == (view.height, view.width, 4) and out.dtype == np.uint8 and out.flags.c_contiguous
+        _check(lib.sph_render(self._ctx, C.byref(view), int(scene), out.ctypes.data, 0), self._ctx)
+        return out
+
+    def render_device(self, view: View, dev_ptr: int, scene: int = 0) -> None:
+        """sph_render into a device buffer of width * height * 4 bytes."""
+        _check(lib.sph_render(self._ctx, C.byref(view), int(scene), C.c_void_p(dev_ptr), 1), self._ctx)
 
     def save(self, path, seed: int = 0) -> None:
         """Write a snapshot file (sph_snapshot_save)."""

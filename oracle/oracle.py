@@ -62,6 +62,8 @@ def lib() -> C.CDLL:
         L.oracle_mix64.restype = C.c_uint64
         L.oracle_mix64.argtypes = [C.c_uint64]
         L.oracle_max_threads.restype = C.c_int
+        L.oracle_render.restype = C.c_int
+        L.oracle_render.argtypes = [_P, _P, _I64, _P]
         _lib = L
     return _lib
 
@@ -197,3 +199,14 @@ def ref_shader_step(particles: np.ndarray, n_steps: int, constants=(0.02, 4.0, 3
     rc = R.ref_shader_step(a.ctypes.data, n_steps, c, u, lo, nthreads)
     assert rc == 0
     return a
+
+
+def render(view, pos4: np.ndarray) -> np.ndarray:
+    """CPU restatement of the particle draw (render_oracle.cpp): `view` is an sph_view
+    ctypes structure, pos4 the (n, 4) positions in record (draw) order. Returns the
+    (height, width, 4) RGBA8 image, rows bottom to top."""
+    pos4 = np.ascontiguousarray(pos4, dtype=np.float32)
+    out = np.zeros((view.height, view.width, 4), dtype=np.uint8)
+    rc = lib().oracle_render(C.addressof(view), pos4.ctypes.data, len(pos4), out.ctypes.data)
+    assert rc == 0
+    return out

@@ -43,3 +43,15 @@ def test_uniform_edits_take_effect(gpu):
     ka = json.loads(a.stdout.splitlines()[-1])["kinetic_energy"]
     kb = json.loads(b.stdout.splitlines()[-1])["kinetic_energy"]
     assert ka != kb
+
+
+@pytest.mark.gpu
+def test_render_frames_to_ppm(gpu, tmp_path):
+    prefix = tmp_path / "f"
+    r = run("--frames", "40", "--keys", "p@0", "--report", "40", "--render-every", "20",
+            "--render-prefix", str(prefix), "--size", "320x240")
+    assert r.returncode == 0, r.stderr
+    for k in (20, 40):
+        data = (tmp_path / f"f_{k:05d}.ppm").read_bytes()
+        assert data.startswith(b"P6\n320 240\n255\n")
+        assert len(data) == len(b"P6\n320 240\n255\n") + 320 * 240 * 3
