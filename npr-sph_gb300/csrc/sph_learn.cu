@@ -48,6 +48,9 @@ struct sph_mpnn {
     float2* ck_rhop = nullptr;
     float2 *snap_rhop = nullptr, *l_rhop = nullptr;
     float *rho_l = nullptr, *rho_p = nullptr;
+    float* Obuf = nullptr;    // [n][kOS] network outputs of a macro-step
+    double* osum = nullptr;   // [kSumBlocks][FO] partial sums of the outputs
+    float* ocorr = nullptr;   // [FO] momentum projection added to every output
     float4 *vel_l = nullptr, *vel_p = nullptr;
     double* cmp = nullptr;
     // host-frame scratch (sph_mpnn_loss_grad)
@@ -81,17 +84,51 @@ inline int nblk(long long n, int t = kT) { return (int)((n + t - 1) / t); }
 
 static_assert(M::K == kNbList, "the network reads the neighbour lists of launch_density_nb");
 
-// Macro-step update from the network output O (FP32 path), fused with the hash.
+constexpr int kSumBlocks = 256;
+
+// Momentum projection, step 1: FP64 partial sums of the outputs (fixed order: deterministic).
+__global__ void __launch_bounds__(kT) k_out_partial(const float* __restrict__ O, int n, double* __restrict__ part) {
+    __shared__ double sh[M::FO][kT];
+    double a[M::FO] = {};
+    for (int i = blockIdx.x * kT + threadIdx.x; i < n; i += gridDim.x * kT)
+#pragma unroll
+        for (int q = 0; q < M::FO; ++q) a[q] += (double)O[(size_t)i * M::kOS + q];
+#pragma unroll
+    for (int q = 0; q < M::FO; ++q) sh[q][threadIdx.x] = a[q];
+    __syncthreads();
+    for (int o = kT / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o)
+#pragma unroll
+            for (int q = 0; q < M::FO; ++q) sh[q][threadIdx.x] += sh[q][threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x < M::FO) part[blockIdx.x * M::FO + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+// Step 2: the shift that makes the mean of each head G/A. Pressure and viscosity forces are
+// pairwise antisymmetric (force_comp.glsl:59-60 with m_i = m_j), so over all particles the
+// sum of m a over the 4 sub-steps is N m G exactly: both target heads average G/A.
+__global__ void k_out_corr(const double* __restrict__ part, int blocks, int n, SceneDev S, float* __restrict__ corr) {
+    const int q = threadIdx.x;
+    if (q >= M::FO) return;
+    double s = 0.0;
+    for (int b = 0; b < blocks; ++b) s += part[b * M::FO + q];
+    const double ga = (double)S.g[q % 3] * (double)S.h / (double)S.gas_k;
+    corr[q] = (float)(ga - s / (double)n);
+}
+
+// Macro-step update from the network outputs O plus the projection corr, fused with the hash.
 __global__ void __launch_bounds__(kT) k_macro_integrate(const float4* __restrict__ pos_s, const float4* __restrict__ vel_s,
-                                                       const float* __restrict__ O, SceneDev S,
-                                                       float4* __restrict__ pos_out, float4* __restrict__ vel_out,
-                                                       int* __restrict__ key_out, int* __restrict__ rank_out,
-                                                       int* __restrict__ count, int n) {
+                                                       const float* __restrict__ O, const float* __restrict__ corr,
+                                                       SceneDev S, float4* __restrict__ pos_out,
+                                                       float4* __restrict__ vel_out, int* __restrict__ key_out,
+                                                       int* __restrict__ rank_out, int* __restrict__ count, int n) {
     const int t = blockIdx.x * kT + threadIdx.x;
     if (t >= n) return;
     float4 np, nv;
     const float* o = O + (size_t)t * M::kOS;
-    M::macro_update(S, o[0], o[1], o[2], o[3], o[4], o[5], pos_s[t], vel_s[t], np, nv);
+    M::macro_update(S, o[0] + corr[0], o[1] + corr[1], o[2] + corr[2], o[3] + corr[3], o[4] + corr[4],
+                    o[5] + corr[5], pos_s[t], vel_s[t], np, nv);
     pos_out[t] = np;
     vel_out[t] = nv;
     const int k = cell_key(S, np.x, np.y, np.z);
@@ -225,6 +262,7 @@ sph_status ensure_ctx_scratch(sph_mpnn* net, int n) {
     NCK(dal(&net->l_pos, m)); NCK(dal(&net->l_vel, m)); NCK(dal(&net->l_rhop, m));
     NCK(dal(&net->acc, m)); NCK(dal(&net->accx, m)); NCK(dal(&net->rho_l, m)); NCK(dal(&net->rho_p, m));
     NCK(dal(&net->vel_l, m)); NCK(dal(&net->vel_p, m)); NCK(dal(&net->cmp, (size_t)kCmpBlocks * 5));
+    NCK(dal(&net->Obuf, m * M::kOS)); NCK(dal(&net->osum, (size_t)kSumBlocks * M::FO)); NCK(dal(&net->ocorr, M::FO));
     net->cap = n;
     return SPH_OK;
 }
@@ -283,16 +321,21 @@ sph_status learned_macro(sph_ctx* ctx, sph_mpnn* net) {
     launch_nb_density(ctx, net->nb, net->cnt);
     M::Frame f{ctx->b.pos_s, ctx->b.vel_s, ctx->b.rhop, net->nb, net->cnt, nullptr, n,
                frame_const(ctx->s0, ctx->params[0].visc)};
+    const float* O = nullptr;
     if (net->precision == 1) {
         M::infer_round1(f, net->frags, net->H1b, net->Pperm, ctx->stream);
-        M::infer_round2(f, net->frags, M::trainer_params(net->tr), net->H1b, net->Pperm, ctx->s0, ctx->b.pos,
-                        ctx->b.vel, nullptr, ctx->b.key, ctx->b.rank, ctx->b.count, true, ctx->stream);
+        M::infer_round2(f, net->frags, M::trainer_params(net->tr), net->H1b, net->Pperm, ctx->s0, nullptr, nullptr,
+                        net->Obuf, nullptr, nullptr, nullptr, false, ctx->stream);
+        O = net->Obuf;
     } else {
         M::trainer_forward(net->inf, f, ctx->stream);
-        k_macro_integrate<<<nblk(n), kT, 0, ctx->stream>>>(ctx->b.pos_s, ctx->b.vel_s, M::trainer_out(net->inf),
-                                                           ctx->s0, ctx->b.pos, ctx->b.vel, ctx->b.key,
-                                                           ctx->b.rank, ctx->b.count, n);
+        O = M::trainer_out(net->inf);
     }
+    // momentum projection, then the update
+    k_out_partial<<<kSumBlocks, kT, 0, ctx->stream>>>(O, n, net->osum);
+    k_out_corr<<<1, 32, 0, ctx->stream>>>(net->osum, kSumBlocks, n, ctx->s0, net->ocorr);
+    k_macro_integrate<<<nblk(n), kT, 0, ctx->stream>>>(ctx->b.pos_s, ctx->b.vel_s, O, net->ocorr, ctx->s0, ctx->b.pos,
+                                                       ctx->b.vel, ctx->b.key, ctx->b.rank, ctx->b.count, n);
     ctx->need_hash = false;  // the integrate hashed the new positions
     ctx->steps += 4;
     ctx->stepped = true;
@@ -393,7 +436,7 @@ sph_status sph_mpnn_destroy(sph_mpnn* net) {
     for (auto& r : net->frames) cudaFree(r.arena);
     void* ptrs[] = {net->nb, net->cnt, net->snap_pos, net->snap_vel, net->snap_rhop, net->ck_pos, net->ck_vel,
                     net->ck_rhop, net->l_pos, net->l_vel,
-                    net->l_rhop, net->acc, net->accx, net->rho_l, net->rho_p, net->vel_l, net->vel_p, net->cmp, net->harena,
+                    net->l_rhop, net->acc, net->accx, net->Obuf, net->osum, net->ocorr, net->rho_l, net->rho_p, net->vel_l, net->vel_p, net->cmp, net->harena,
                     net->frags, net->H1b, net->Pperm};
     for (void* p : ptrs)
         if (p) cudaFree(p);

@@ -35,6 +35,7 @@ constexpr int kLd2 = 152;         // X2 tile row stride (144 used), bf16
 constexpr int kK1 = 80, kK2 = 144; // padded K of the two node layers (bias column at W+FN / 128)
 constexpr int kBias1 = W + FN;     // bias column of the round-1 node layer
 static_assert(kBias1 < kK1, "round-1 node input does not fit its padded K");
+static_assert(2 * W + 16 == kK2, "round-2 node input: [M2 H1], bias column, padding");
 static_assert(FO <= 8, "the output layer is one n-tile of 8 columns");
 
 // Fragment-ordered weights (u32 = 2 x bf16), built by k_prep_frags.
@@ -118,57 +119,91 @@ struct EdgeFrags {
     uint32_t a[4][4];  // [mt][reg]
 };
 
-// Round-1/2 edge layer of particle i: returns the per-lane sums over edges of relu(Z) for the
-// features (16 mt + g, 16 mt + g + 8), already reduced over the lane quad (all tq hold them).
+// Round-1/2 edge layer of a tile of 16 particles (rows of X), two groups of 8. An MMA n-tile
+// holds the same edge slot e of the group's 8 particles (column c = particle c): the loop over
+// edge slots has no per-particle branch, so the gathers of successive slots overlap. Lane
+// (g, tq) builds the features of particle g's edge e and accumulates relu(Z) for features
+// (16 mt + g, 16 mt + g + 8) of particles 2 tq and 2 tq + 1; padded edges have all-zero
+// features (bias included), so they add exactly zero. The sums / K go to X[:, 0:64].
 template <bool ROUND2>
-__device__ __forceinline__ void edge_layer(const EdgeFrags& A, int i, const float4* __restrict__ pos,
-                                           const float4* __restrict__ vel, const int* __restrict__ nb, int cnt,
-                                           float ih, float ic, const uint4* __restrict__ Pperm, float (&s)[4][2]) {
+__device__ __forceinline__ void edge_tile(const EdgeFrags& A, int base, int n, const float4* __restrict__ pos,
+                                          const float4* __restrict__ vel, const int* nb_s, const int* cnt_s,
+                                          float ih, float ic, const uint4* __restrict__ Pperm,
+                                          __nv_bfloat16* X, int ld) {
     const int lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
-    const float4 pi = pos[i], vi = vel[i];
+#pragma unroll 1
+    for (int grp = 0; grp < 2; ++grp) {
+        const int pc = grp * 8 + g;  // this lane's column particle (tile row)
+        const int i = base + pc;
+        const float4 pi = i < n ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 vi = i < n ? vel[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const int ci = cnt_s[pc];
+        const int c0 = cnt_s[grp * 8 + 2 * tq], c1 = cnt_s[grp * 8 + 2 * tq + 1];
+        int emax = ci;
 #pragma unroll
-    for (int mt = 0; mt < 4; ++mt) s[mt][0] = s[mt][1] = 0.0f;
+        for (int o = 16; o >= 4; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+        float s[4][2][2];
 #pragma unroll
-    for (int nt = 0; nt < 4; ++nt) {
-        if (nt * 8 >= cnt) break;  // warp-uniform: cnt is the particle's
-        const int e = nt * 8 + g;
-        const bool valid = e < cnt;
-        const int j = valid ? nb[(size_t)i * K + e] : i;
-        uint32_t b0, b1;
-        edge_b(pi, vi, pos[j], vel[j], ih, ic, tq, valid, b0, b1);
-        float c[4][4];
-        if constexpr (ROUND2) {
-            // accumulator starts at P_j for the two edge columns 2tq, 2tq+1 of this n-tile
-            const int e0 = nt * 8 + 2 * tq, e1 = e0 + 1;
-            uint4 p0 = make_uint4(0, 0, 0, 0), p1 = make_uint4(0, 0, 0, 0);
-            if (e0 < cnt) p0 = Pperm[(size_t)nb[(size_t)i * K + e0] * 8 + g];
-            if (e1 < cnt) p1 = Pperm[(size_t)nb[(size_t)i * K + e1] * 8 + g];
-            const uint32_t w0[4] = {p0.x, p0.y, p0.z, p0.w}, w1[4] = {p1.x, p1.y, p1.z, p1.w};
+        for (int mt = 0; mt < 4; ++mt) s[mt][0][0] = s[mt][0][1] = s[mt][1][0] = s[mt][1][1] = 0.0f;
+#pragma unroll 2
+        for (int e = 0; e < emax; ++e) {
+            const bool valid = e < ci;
+            const int j = valid ? nb_s[pc * K + e] : 0;
+            uint32_t b0, b1;
+            const float4 pj = valid ? pos[j] : pi, vj = valid ? vel[j] : vi;
+            edge_b(pi, vi, pj, vj, ih, ic, tq, valid, b0, b1);
+            float c[4][4];
+            if constexpr (ROUND2) {
+                // accumulators start at P_j of the two column particles 2 tq, 2 tq + 1
+                uint4 p0 = make_uint4(0, 0, 0, 0), p1 = make_uint4(0, 0, 0, 0);
+                if (e < c0) p0 = Pperm[(size_t)nb_s[(grp * 8 + 2 * tq) * K + e] * 8 + g];
+                if (e < c1) p1 = Pperm[(size_t)nb_s[(grp * 8 + 2 * tq + 1) * K + e] * 8 + g];
+                const uint32_t w0[4] = {p0.x, p0.y, p0.z, p0.w}, w1[4] = {p1.x, p1.y, p1.z, p1.w};
 #pragma unroll
-            for (int mt = 0; mt < 4; ++mt) {  // chunk word mt holds features (16 mt + g, 16 mt + g + 8)
-                c[mt][0] = bf16_lo(w0[mt]);
-                c[mt][1] = bf16_lo(w1[mt]);
-                c[mt][2] = bf16_hi(w0[mt]);
-                c[mt][3] = bf16_hi(w1[mt]);
+                for (int mt = 0; mt < 4; ++mt) {  // word mt holds features (16 mt + g, 16 mt + g + 8)
+                    c[mt][0] = bf16_lo(w0[mt]);
+                    c[mt][1] = bf16_lo(w1[mt]);
+                    c[mt][2] = bf16_hi(w0[mt]);
+                    c[mt][3] = bf16_hi(w1[mt]);
+                }
+            } else {
+#pragma unroll
+                for (int mt = 0; mt < 4; ++mt) c[mt][0] = c[mt][1] = c[mt][2] = c[mt][3] = 0.0f;
             }
-        } else {
 #pragma unroll
-            for (int mt = 0; mt < 4; ++mt) c[mt][0] = c[mt][1] = c[mt][2] = c[mt][3] = 0.0f;
+            for (int mt = 0; mt < 4; ++mt) {
+                mma(c[mt], A.a[mt], b0, b1);
+                s[mt][0][0] += fmaxf(c[mt][0], 0.0f);
+                s[mt][0][1] += fmaxf(c[mt][1], 0.0f);
+                s[mt][1][0] += fmaxf(c[mt][2], 0.0f);
+                s[mt][1][1] += fmaxf(c[mt][3], 0.0f);
+            }
         }
+        const float sc = 1.0f / K;
 #pragma unroll
-        for (int mt = 0; mt < 4; ++mt) {
-            mma(c[mt], A.a[mt], b0, b1);
-            s[mt][0] += fmaxf(c[mt][0], 0.0f) + fmaxf(c[mt][1], 0.0f);
-            s[mt][1] += fmaxf(c[mt][2], 0.0f) + fmaxf(c[mt][3], 0.0f);
-        }
+        for (int mt = 0; mt < 4; ++mt)
+#pragma unroll
+            for (int r = 0; r < 2; ++r)
+#pragma unroll
+                for (int cc = 0; cc < 2; ++cc)
+                    X[(grp * 8 + 2 * tq + cc) * ld + mt * 16 + g + 8 * r] = __float2bfloat16_rn(s[mt][r][cc] * sc);
     }
-#pragma unroll
-    for (int mt = 0; mt < 4; ++mt)
-#pragma unroll
-        for (int r = 0; r < 2; ++r) {
-            s[mt][r] += __shfl_xor_sync(0xffffffffu, s[mt][r], 1);
-            s[mt][r] += __shfl_xor_sync(0xffffffffu, s[mt][r], 2);
-        }
+}
+
+// Neighbour lists and counts of a tile into the warp's shared memory (rows past n: none).
+__device__ __forceinline__ void stage_tile_lists(int base, int n, const int* __restrict__ nb,
+                                                 const int* __restrict__ cnt, int* nb_s, int* cnt_s) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll 4
+    for (int q = lane; q < kTile * K; q += 32) {
+        const int i = base + q / K;
+        nb_s[q] = i < n ? nb[(size_t)base * K + q] : 0;
+    }
+    if (lane < kTile) {
+        const int i = base + lane;
+        cnt_s[lane] = i < n ? min(max(cnt[i], 0), K) : 0;
+    }
+    __syncwarp();
 }
 
 // A fragment of k-tile kt from a bf16 smem tile with row stride ld (16 rows).
@@ -200,17 +235,6 @@ __device__ __forceinline__ void node_gemm(const __nv_bfloat16* X, int ld, const 
     }
 }
 
-// Write 8 feature sums (or zeros) of particle row p into a tile: lanes tq == 0 own them.
-__device__ __forceinline__ void put_m(__nv_bfloat16* X, int ld, int p, const float (&s)[4][2], float scale) {
-    const int lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
-    if (tq != 0) return;
-#pragma unroll
-    for (int mt = 0; mt < 4; ++mt) {
-        X[p * ld + mt * 16 + g] = __float2bfloat16_rn(s[mt][0] * scale);
-        X[p * ld + mt * 16 + g + 8] = __float2bfloat16_rn(s[mt][1] * scale);
-    }
-}
-
 __device__ __forceinline__ void load_edge_frags(const uint32_t* __restrict__ fr, int base, EdgeFrags& A) {
     const int lane = threadIdx.x & 31;
 #pragma unroll
@@ -226,6 +250,8 @@ __global__ void __launch_bounds__(kThreads) k_infer_r1(const float4* __restrict_
                                                       const uint32_t* __restrict__ fr,
                                                       __nv_bfloat16* __restrict__ H1out, uint16_t* __restrict__ Pperm) {
     __shared__ __align__(16) __nv_bfloat16 xs[kWarps][kTile * kLd1];
+    __shared__ int nbs[kWarps][kTile * K];
+    __shared__ int cns[kWarps][kTile];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
     __nv_bfloat16* X = xs[warp];
     EdgeFrags A;
@@ -234,35 +260,28 @@ __global__ void __launch_bounds__(kThreads) k_infer_r1(const float4* __restrict_
     const int ntiles = (n + kTile - 1) / kTile;
     for (int tile = blockIdx.x * kWarps + warp; tile < ntiles; tile += gridDim.x * kWarps) {
         const int base = tile * kTile;
-        for (int p = 0; p < kTile; ++p) {
-            const int i = base + p;
-            float s[4][2];
+        stage_tile_lists(base, n, nb, cnt, nbs[warp], cns[warp]);
+        edge_tile<false>(A, base, n, pos, vel, nbs[warp], cns[warp], ih, ic, nullptr, X, kLd1);
+        // node features, bias column and padding (columns 64 .. 79) of the 16 rows
+        for (int q = lane; q < kTile * 16; q += 32) {
+            const int p = q >> 4, col = q & 15, i = base + p;
+            float v = 0.0f;
             if (i < n) {
-                const int c = min(max(cnt[i], 0), K);
-                edge_layer<false>(A, i, pos, vel, nb, c, ih, ic, nullptr, s);
-                put_m(X, kLd1, p, s, 1.0f / K);
-                if (lane < 16) {  // node features, bias column, padding (columns 64 .. 79)
-                    float v = 0.0f;
-                    const float4 vi = vel[i];
-                    const float rho = rhop[i].x;
-                    switch (lane) {
-                        case 0: v = vi.x * ic; break;
-                        case 1: v = vi.y * ic; break;
-                        case 2: v = vi.z * ic; break;
-                        case 3: v = rho / fc.rho_self - 1.0f; break;
-                        case 4: v = (rho - fc.rho0) / fc.rho_self; break;
-                        case 5: v = fc.log_mu; break;
-                        case 6: v = (float)c / K; break;
-                        case 7: v = 1.0f; break;
-                        case 8: v = fc.courant; break;
-                        case kBias1 - W: v = 1.0f; break;  // bias column
-                        default: v = 0.0f;
-                    }
-                    X[p * kLd1 + 64 + lane] = __float2bfloat16_rn(v);
+                switch (col) {
+                    case 0: v = vel[i].x * ic; break;
+                    case 1: v = vel[i].y * ic; break;
+                    case 2: v = vel[i].z * ic; break;
+                    case 3: v = rhop[i].x / fc.rho_self - 1.0f; break;
+                    case 4: v = (rhop[i].x - fc.rho0) / fc.rho_self; break;
+                    case 5: v = fc.log_mu; break;
+                    case 6: v = (float)cns[warp][p] / K; break;
+                    case 7: v = 1.0f; break;
+                    case 8: v = fc.courant; break;
+                    case kBias1 - W: v = 1.0f; break;  // bias column
+                    default: v = 0.0f;
                 }
-            } else {
-                for (int q = lane; q < kK1; q += 32) X[p * kLd1 + q] = __float2bfloat16_rn(0.0f);
             }
+            X[p * kLd1 + 64 + col] = __float2bfloat16_rn(v);
         }
         __syncwarp();
         float d[8][4];
@@ -318,6 +337,8 @@ __global__ void __launch_bounds__(kThreads) k_infer_r2(const float4* __restrict_
                                                       int* __restrict__ rank_out, int* __restrict__ count,
                                                       int integrate) {
     __shared__ __align__(16) __nv_bfloat16 xs[kWarps][kTile * kLd2];
+    __shared__ int nbs[kWarps][kTile * K];
+    __shared__ int cns[kWarps][kTile];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
     __nv_bfloat16* X = xs[warp];
     EdgeFrags A;
@@ -330,20 +351,14 @@ __global__ void __launch_bounds__(kThreads) k_infer_r2(const float4* __restrict_
     const int ntiles = (n + kTile - 1) / kTile;
     for (int tile = blockIdx.x * kWarps + warp; tile < ntiles; tile += gridDim.x * kWarps) {
         const int base = tile * kTile;
+        stage_tile_lists(base, n, nb, cnt, nbs[warp], cns[warp]);
+        edge_tile<true>(A, base, n, pos, vel, nbs[warp], cns[warp], ih, ic, Pperm, X, kLd2);
+        // H1 rows (columns 64 .. 127), bias column 128, padding to 143
         for (int p = 0; p < kTile; ++p) {
             const int i = base + p;
-            float s[4][2];
-            if (i < n) {
-                const int c = min(max(cnt[i], 0), K);
-                edge_layer<true>(A, i, pos, vel, nb, c, ih, ic, Pperm, s);
-                put_m(X, kLd2, p, s, 1.0f / K);
-                // H1 row (columns 64 .. 127), bias column 128, padding to 143
-                reinterpret_cast<uint32_t*>(X + p * kLd2 + 64)[lane] =
-                    reinterpret_cast<const uint32_t*>(H1 + (size_t)i * W)[lane];
-                if (lane < 16) X[p * kLd2 + 128 + lane] = __float2bfloat16_rn(lane == 0 ? 1.0f : 0.0f);
-            } else {
-                for (int q = lane; q < kK2; q += 32) X[p * kLd2 + q] = __float2bfloat16_rn(0.0f);
-            }
+            reinterpret_cast<uint32_t*>(X + p * kLd2 + 64)[lane] =
+                i < n ? reinterpret_cast<const uint32_t*>(H1 + (size_t)i * W)[lane] : 0u;
+            if (lane < 16) X[p * kLd2 + 128 + lane] = __float2bfloat16_rn(lane == 0 && i < n ? 1.0f : 0.0f);
         }
         __syncwarp();
         float d[8][4];

@@ -135,6 +135,21 @@ def test_trained_network_beats_the_macro_step_without_it(sph, trained):
     assert devs["trained"] < devs["zero"], devs
 
 
+def test_momentum_projection_conserves_momentum(sph, trained):
+    """Away from the walls plain SPH changes the momentum only by gravity (pressure and
+    viscosity are pairwise antisymmetric); the learned macro-step's projection makes the
+    network's heads average G/A, so its momentum matches plain SPH to rounding."""
+    net, _ = trained
+    p = sph.workload_params(lower=(0.0, 0.0, 0.0), upper=(1.0, 1.0, 1.0))
+    parts = sph.scene_ball(4000, (0.5, 0.5, 0.5), 0.5 * p.h, 0.01 * p.h, 31)
+    with sph.Sim(p, n_max=len(parts)) as sim:
+        sim.upload(parts)
+        sim.step(8)
+        rep = sim.learned_step(net, 1, judge_every=1, density_tol=1e30, momentum_tol=1e30)
+    assert rep.judged == 1 and rep.learned_macro_steps == 1
+    assert rep.last_momentum_dev < 2e-4, rep.last_momentum_dev
+
+
 def test_judge_rolls_back_to_plain(sph, trained):
     """With zero tolerance every learned interval fails: it is rolled back to its checkpoint and
     run by plain SPH, and after the second failure in a row one more interval runs plain. The
