@@ -266,6 +266,11 @@ sph_status sph_learned_step(sph_ctx* ctx, sph_mpnn* net, int32_t n_macro, int32_
                             float density_tol, float momentum_tol, sph_learned_report* report);
 /* Recompute rho and pres at the current positions (the state is re-sorted by cell). */
 sph_status sph_refresh_density(sph_ctx* ctx);
+/* The learned macro-step's input lists at the current positions, by particle id (record
+ * order): the <= 32 nearest neighbours j != i with r < h (FP32 canonical distance; ids, -1
+ * padded; nb_ids n x 32), their number, and rho (as the density pass computes it). The state
+ * is re-sorted by cell as by sph_refresh_density. */
+sph_status sph_neighbor_lists(sph_ctx* ctx, int32_t* nb_ids, int32_t* counts, float* rho);
 
 /* ---- diagnostics without allocation -------------------------------------
  * No counterpart in the reference.

@@ -203,6 +203,24 @@ __global__ void __launch_bounds__(kT) k_by_id(const float4* __restrict__ vel, co
     vel_id[id] = v;
 }
 
+// Neighbour lists (sorted slots) to particle ids, by particle id, with the count and density.
+__global__ void __launch_bounds__(kT) k_lists_by_id(const float4* __restrict__ vel_s, const int* __restrict__ nb,
+                                                   const int* __restrict__ cnt, const float2* __restrict__ rhop, int n,
+                                                   int* __restrict__ nb_id, int* __restrict__ cnt_id,
+                                                   float* __restrict__ rho_id) {
+    const int s = blockIdx.x * kT + threadIdx.x;
+    if (s >= n) return;
+    const int id = id_of(vel_s[s]);
+    if (id < 0 || id >= n) return;
+    const int c = min(max(cnt[s], 0), M::K);
+    for (int q = 0; q < M::K; ++q) {
+        const int j = q < c ? nb[(size_t)s * M::K + q] : -1;
+        nb_id[(size_t)id * M::K + q] = (j >= 0 && j < n) ? id_of(vel_s[j]) : -1;
+    }
+    cnt_id[id] = c;
+    rho_id[id] = rhop[s].x;
+}
+
 // FP64 partials of the judge: sum |rho_l - rho_p| / rho_p, sum (v_l - v_p) (3), sum |v_p|.
 __global__ void __launch_bounds__(kT) k_compare(const float* __restrict__ rl, const float* __restrict__ rp,
                                                const float4* __restrict__ vl, const float4* __restrict__ vp, int n,
@@ -651,6 +669,35 @@ sph_status sph_mpnn_train(sph_mpnn* net, uint32_t steps, float lr, uint64_t seed
         NCK(cudaMemcpyAsync(M::trainer_params(net->inf), M::trainer_params(net->tr), sizeof(float) * M::kParams,
                             cudaMemcpyDeviceToDevice, net->stream));
     return SPH_OK;
+}
+
+sph_status sph_neighbor_lists(sph_ctx* ctx, int32_t* nb_ids, int32_t* counts, float* rho) {
+    if (!ctx || !nb_ids || !counts || !rho) return SPH_ERR_INVALID_ARG;
+    if (!ctx->have_state) return fail(ctx, SPH_ERR_NOT_READY, "no particles uploaded");
+    cudaSetDevice(ctx->device);
+    const int n = ctx->b.n;
+    const size_t m = (size_t)n;
+    char* buf = nullptr;
+    const size_t bytes = m * M::K * 4 * 2 + m * 4 * 2 + m * 4;
+    if (cudaMalloc(&buf, bytes) != cudaSuccess) return fail(ctx, SPH_ERR_OUT_OF_MEMORY, "neighbour-list scratch");
+    int* nb = reinterpret_cast<int*>(buf);
+    int* cnt = nb + m * M::K;
+    int* nb_id = cnt + m;
+    int* cnt_id = nb_id + m * M::K;
+    float* rho_id = reinterpret_cast<float*>(cnt_id + m);
+    engine::sort_state(ctx);
+    launch_nb_density(ctx, nb, cnt);
+    k_lists_by_id<<<nblk(n), kT, 0, ctx->stream>>>(ctx->b.vel_s, nb, cnt, ctx->b.rhop, n, nb_id, cnt_id, rho_id);
+    // the sorted copy becomes the state, so rhop lines up with it (as after sph_refresh_density)
+    cudaMemcpyAsync(ctx->b.pos, ctx->b.pos_s, m * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->stream);
+    cudaMemcpyAsync(ctx->b.vel, ctx->b.vel_s, m * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->stream);
+    cudaError_t e = cudaMemcpyAsync(nb_ids, nb_id, m * M::K * 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(counts, cnt_id, m * 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(rho, rho_id, m * 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(buf);
+    if (e != cudaSuccess) return fail(ctx, SPH_ERR_CUDA, std::string("neighbour lists: ") + cudaGetErrorString(e));
+    return engine::check_device_error(ctx);
 }
 
 sph_status sph_refresh_density(sph_ctx* ctx) {

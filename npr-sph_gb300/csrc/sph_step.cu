@@ -488,11 +488,14 @@ __global__ void __launch_bounds__(BLOCK) k_density_nb(const float4* __restrict__
                 const float2 npz = make_float2(-p.z, -p.z);
                 const float2 h2v = make_float2(h2, h2);
                 float2 s2 = make_float2(0.f, 0.f), c2 = make_float2(0.f, 0.f);
+                // the particle's own staged index: its row's centre segment (dy = dz = 0) holds it
+                const int cseg = lrow * G::kSegPerRow + R * G::kSide + R;
+                const int self_j = T.seg_off[cseg] + (t - T.seg_gbeg[cseg]);
 #pragma unroll 1
                 for (int r = 0; r < G::kSegPerRow; ++r) {
                     int a, b;
                     seg_range<R, BLOCK>(T, lrow * G::kSegPerRow + r, cx, S.dim[0], start, a, b);
-#pragma unroll 1
+#pragma unroll 2
                     for (int j = a; j < b; j += 2) {
                         const float2 d2 = pair_d2(st, j, npx, npy, npz);
                         float2 w = __fadd2_rn(h2v, make_float2(-d2.x, -d2.y));
@@ -504,8 +507,8 @@ __global__ void __launch_bounds__(BLOCK) k_density_nb(const float4* __restrict__
                         const float2 lost = __fadd2_rn(tt, make_float2(-s2.x, -s2.y));
                         c2 = __fadd2_rn(lost, make_float2(-y.x, -y.y));
                         s2 = tt;
-                        if (d2.x < cut && st.slot[j] != t) lst[BLOCK * c++] = (unsigned short)j;
-                        if (d2.y < cut && st.slot[j + 1] != t) lst[BLOCK * c++] = (unsigned short)(j + 1);
+                        if (d2.x < cut && j != self_j) lst[BLOCK * c++] = (unsigned short)j;
+                        if (d2.y < cut && j + 1 != self_j) lst[BLOCK * c++] = (unsigned short)(j + 1);
                         if (c > kNbCapForce - 2) prune_nearest<BLOCK>(lst, c, st, p.x, p.y, p.z);
                     }
                 }

@@ -133,6 +133,7 @@ _SIGS = {
     "sph_mpnn_train": (C.c_int32, [_P, C.c_uint32, C.c_float, C.c_uint64, _P]),
     "sph_learned_step": (C.c_int32, [_P, _P, C.c_int32, C.c_int32, C.c_float, C.c_float, C.POINTER(LearnedReport)]),
     "sph_refresh_density": (C.c_int32, [_P]),
+    "sph_neighbor_lists": (C.c_int32, [_P, _P, _P, _P]),
     "sph_view_default": (C.c_int32, [C.POINTER(View), C.c_int32, C.c_int32, C.c_float]),
     "sph_view_camera": (C.c_int32, [C.POINTER(View), C.c_float, C.c_float, C.POINTER(C.c_float),
                                     C.POINTER(C.c_float)]),
@@ -474,6 +475,15 @@ class Sim:
         _check(lib.sph_autotune(self._ctx, trial_steps, C.byref(ms)), self._ctx)
         return float(ms.value)
 
+
+    def neighbor_lists(self):
+        """(nb (n, 32) ids, counts (n,), rho (n,)) by particle id (sph_neighbor_lists)."""
+        n = self.n
+        nb = np.zeros((n, 32), np.int32)
+        cnt = np.zeros(n, np.int32)
+        rho = np.zeros(n, np.float32)
+        _check(lib.sph_neighbor_lists(self._ctx, nb.ctypes.data, cnt.ctypes.data, rho.ctypes.data), self._ctx)
+        return nb, cnt, rho
 
     def refresh_density(self) -> None:
         """rho and pres at the current positions (sph_refresh_density)."""

@@ -95,3 +95,42 @@ def test_batched_neighbours(sph, orc, gpu):
         seg = state[offs[i]:offs[i + 1]]
         co, _ = orc.neighbors(p, seg, np.arange(len(seg)), backend="grid")
         np.testing.assert_array_equal(cg[offs[i]:offs[i + 1]], co)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("steps", [0, 150])
+def test_nearest_32_lists_against_brute_force(sph, orc, gpu, steps):
+    """The learned macro-step's input (sph_neighbor_lists): per particle the <= 32 nearest
+    neighbours j != i with r < h. Against the brute-force oracle lists, compared as multisets
+    of FP32 canonical distances (ties may pick either particle); the density equals the plain
+    density pass bit for bit."""
+    sc = sph.dam_break(16, 32, 32, seed=41)
+    with sph.Sim(sc.params, n_max=len(sc.particles)) as sim:
+        sim.upload(sc.particles)
+        sim.step(steps)
+        state = sim.download()
+        nb, cnt, rho = sim.neighbor_lists()
+        sim.refresh_density()
+        rho_plain = sim.download()["extras"][:, 0]
+    assert np.array_equal(rho, rho_plain)
+    pos = np.ascontiguousarray(state["pos"][:, :3], dtype=np.float32)
+    off, items = orc.neighbor_lists(sc.params, state, backend="brute")
+
+    def d2(i, js):
+        d = pos[js] - pos[i]
+        return (d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2]
+
+    n = len(pos)
+    over = 0
+    for i in range(n):
+        ref = items[off[i]:off[i + 1]]
+        ref = ref[ref != i]
+        k = min(len(ref), 32)
+        over += len(ref) > 32
+        assert cnt[i] == k, (i, cnt[i], len(ref))
+        got = nb[i, :k]
+        assert np.all(nb[i, k:] == -1)
+        assert np.all(np.isin(got, ref)) and len(np.unique(got)) == k
+        assert np.array_equal(np.sort(d2(i, got)), np.sort(d2(i, ref))[:k])
+    if steps == 0:
+        assert over > 0  # the dense lattice exercises the nearest-32 selection
