@@ -266,6 +266,76 @@ def render_workload(stream, frames: int = 20) -> dict:
 WEIGHTS = REPO / "npr-sph_gb300" / "weights" / "mpnn_w64.npy"
 
 
+def slosh_study(args, stream) -> dict:
+    """Learned vs plain on the 16,777,216-particle slosh (256^3 lattice at 0.5h in a 2:1:1 box,
+    v_x = 0.5 sin(pi x / L)): 2,000 dt-equivalents each from the same state. Every 200 dt: the
+    FP64 GPU reductions of both runs (momentum, energy, density drift from t = 0) and the
+    learned run's density deviation from the plain run by particle id (mean and max)."""
+    import torch
+    import nprsph as S
+
+    if not WEIGHTS.exists():
+        return {"unavailable": f"no trained weights at {WEIGHTS.relative_to(REPO)}"}
+    params = np.load(WEIGHTS).astype(np.float32)
+    sc = S.slosh_block(256, seed=5)
+    n = len(sc.particles)
+    every, total = 200, 2000
+
+    def diag(sim):
+        d = sim.reduce()
+        e = d.kinetic_energy + d.potential_energy
+        return {"momentum": list(d.momentum), "energy": e, "mean_rho": d.mean_rho, "max_rho": d.max_rho,
+                "nonfinite": int(d.nonfinite)}
+
+    rows, reps = [], []
+    t_plain = t_learned = 0.0
+    with S.Net(16, stream=stream.cuda_stream) as net, \
+            S.Sim(sc.params, n_max=n, stream=stream.cuda_stream) as plain, \
+            S.Sim(sc.params, n_max=n, stream=stream.cuda_stream) as learned:
+        net.set_params(params)
+        for sim in (plain, learned):
+            sim.upload(sc.particles)
+            sim.refresh_density()
+        d0p, d0l = diag(plain), diag(learned)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for k in range(total // every):
+            torch.cuda.synchronize()
+            a.record(stream)
+            plain.step(every)
+            b.record(stream)
+            torch.cuda.synchronize()
+            t_plain += a.elapsed_time(b) / 1e3
+            a.record(stream)
+            reps.append(learned.learned_step(net, every // 4, 8, 0.01, 0.01))
+            b.record(stream)
+            torch.cuda.synchronize()
+            t_learned += a.elapsed_time(b) / 1e3
+            plain.refresh_density()
+            learned.refresh_density()
+            dp, dl = diag(plain), diag(learned)
+            rp = plain.download()["extras"][:, 0].astype(np.float64)
+            rl = learned.download()["extras"][:, 0].astype(np.float64)
+            dev = np.abs(rl - rp) / rp
+            m0 = np.linalg.norm(d0p["momentum"]) + 1e-30
+            rows.append({
+                "dt": (k + 1) * every,
+                "learned_vs_plain_density_dev": {"mean": float(dev.mean()), "max": float(dev.max())},
+                "plain": {"momentum_drift": float(np.linalg.norm(np.subtract(dp["momentum"], d0p["momentum"])) / m0),
+                          "energy_drift": (dp["energy"] - d0p["energy"]) / abs(d0p["energy"]),
+                          "mean_rho": dp["mean_rho"], "nonfinite": dp["nonfinite"]},
+                "learned": {"momentum_drift": float(np.linalg.norm(np.subtract(dl["momentum"], d0l["momentum"])) / m0),
+                            "energy_drift": (dl["energy"] - d0l["energy"]) / abs(d0l["energy"]),
+                            "mean_rho": dl["mean_rho"], "nonfinite": dl["nonfinite"]},
+            })
+    nl = sum(r.learned_macro_steps for r in reps)
+    npl = sum(r.plain_macro_steps for r in reps)
+    return {"workload": "slosh 256^3 = 16,777,216 particles, 2:1:1 box, v_x = 0.5 sin(pi x / L), 2,000 dt-equivalents",
+            "particles": n, "plain_updates_per_s": n * total / t_plain, "learned_updates_per_s": n * total / t_learned,
+            "learned_macro_steps": nl, "plain_macro_steps": npl, "judged": sum(r.judged for r in reps),
+            "fallbacks": sum(r.fallbacks for r in reps), "checkpoints": rows,
+            "drift_reference": "FP64 GPU reductions (sph_reduce) of each run against its own t = 0"}
+
+
 def learned_workload(args, stream, flush) -> dict:
     """The learned macro-step on the same dam break: units of 8 macro-steps (32 dt, one judged
     against plain SPH), each timed with CUDA events, L2 flushed between units; plain SPH timed
@@ -417,6 +487,8 @@ def run_ours(args) -> None:
         return
     extra = extra_workloads(args, stream) if args.extra_steps > 0 else {}
     learned = learned_workload(args, stream, flush) if args.learned else {"skipped": "--no-learned"}
+    if args.study:
+        learned["slosh_16m_study"] = slosh_study(args, stream)
     peaks, src = measured_peaks()
     hbm = float(peaks["hbm_gbs"])
     value = world * n * args.steps / total_s
@@ -473,6 +545,8 @@ def main() -> None:
                     help="keep the default launch shape instead of timing the candidates first")
     ap.add_argument("--no-learned", dest="learned", action="store_false",
                     help="skip the learned macro-step measurement")
+    ap.add_argument("--study", action="store_true",
+                    help="also run the 16M-particle slosh study of learned vs plain (2,000 dt-equivalents)")
     ap.add_argument("--extra-steps", type=int, default=100,
                     help="steps of the batched-scenes and 10k reference-scene measurements (0: skip)")
     args = ap.parse_args()

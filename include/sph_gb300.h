@@ -361,13 +361,16 @@ sph_status sph_image_write_ppm(const char* path, const uint8_t* rgba, int32_t wi
  * and the step count, with a checksum. A trajectory file is the same header
  * followed by frames appended during a run. Format (little-endian):
  *   64-byte header: magic "NPRSPHS1" (snapshot) / "NPRSPHT1" (trajectory),
- *     u32 version 1, u32 header bytes 64, u64 particles, u32 scenes, u32 0,
+ *     u32 version 1, u32 header bytes 64, u64 particles, u32 scenes, u32 flags,
  *     u64 step count (trajectory: 0), u64 seed (a caller tag), u64 checksum
  *     (snapshot: of all bytes after the header; trajectory: of the scene
  *     table), u64 0;
  *   scene table: scenes x sph_params, scenes x u32 counts, zero padding to a
  *     multiple of 64 bytes;
- *   snapshot: particles x sph_particle;
+ *   snapshot: particles x sph_particle; then, when flags bit 0 is set, particles x
+ *     u32: the record index at each slot of the device state (the within-cell order
+ *     the next neighbour sort keeps; restoring it makes a resumed run repeat the
+ *     original bit for bit; sph_snapshot_save always writes it);
  *   trajectory frames: u64 step, u64 particles, u64 checksum of the records,
  *     u64 0, particles x sph_particle.
  * Checksum: FNV-1a 64 over the 64-bit little-endian words of the bytes (a final

@@ -55,6 +55,10 @@ void sort_state(sph_ctx* ctx);
 // n plain steps (graph replay, or eager with per-pass timing).
 sph_status run_steps(sph_ctx* ctx, int n);
 sph_status check_device_error(sph_ctx* ctx);
+// The record index at each slot of the current state (the within-cell order that the next
+// sort keeps), and its restore after an upload: resuming with it repeats a run bit for bit.
+sph_status slot_order(sph_ctx* ctx, uint32_t* host_order);
+sph_status apply_order(sph_ctx* ctx, const uint32_t* host_order);
 
 }  // namespace engine
 }  // namespace sphgb

@@ -31,6 +31,66 @@ sph_status fail(sph_ctx* c, sph_status code, const std::string& msg) {
 }  // namespace engine
 }  // namespace sphgb
 
+namespace {
+
+// State in record order -> the given slot order (order[s] = record at slot s).
+__global__ void __launch_bounds__(256) k_apply_order(const float4* __restrict__ pos, const float4* __restrict__ vel,
+                                                     const uint32_t* __restrict__ order, int n,
+                                                     float4* __restrict__ pos_out, float4* __restrict__ vel_out) {
+    const int s = blockIdx.x * 256 + threadIdx.x;
+    if (s >= n) return;
+    const uint32_t id = order[s];
+    if (id < (uint32_t)n) {
+        pos_out[s] = pos[id];
+        vel_out[s] = vel[id];
+    }
+}
+
+}  // namespace
+
+namespace sphgb {
+namespace engine {
+
+sph_status slot_order(sph_ctx* ctx, uint32_t* host_order) {
+    const size_t n = (size_t)ctx->b.n;
+    std::vector<float4> v(n);
+    cudaError_t e = cudaMemcpyAsync(v.data(), ctx->b.vel, n * sizeof(float4), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return fail(ctx, SPH_ERR_CUDA, std::string("slot order: ") + cudaGetErrorString(e));
+    for (size_t s = 0; s < n; ++s) std::memcpy(&host_order[s], &v[s].w, 4);
+    return SPH_OK;
+}
+
+sph_status apply_order(sph_ctx* ctx, const uint32_t* host_order) {
+    const int n = ctx->b.n;
+    std::vector<char> seen((size_t)n, 0);
+    for (int s = 0; s < n; ++s) {
+        if (host_order[s] >= (uint32_t)n || seen[host_order[s]])
+            return fail(ctx, SPH_ERR_INVALID_ARG, "slot order is not a permutation");
+        seen[host_order[s]] = 1;
+    }
+    uint32_t* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, sizeof(uint32_t) * (size_t)n);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d, host_order, sizeof(uint32_t) * (size_t)n, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) {
+        k_apply_order<<<(n + 255) / 256, 256, 0, ctx->stream>>>(ctx->b.pos, ctx->b.vel, d, n, ctx->b.pos_s, ctx->b.vel_s);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ctx->b.pos, ctx->b.pos_s, sizeof(float4) * (size_t)n, cudaMemcpyDeviceToDevice, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ctx->b.vel, ctx->b.vel_s, sizeof(float4) * (size_t)n, cudaMemcpyDeviceToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (d) cudaFree(d);
+    if (e != cudaSuccess) return fail(ctx, SPH_ERR_CUDA, std::string("slot order: ") + cudaGetErrorString(e));
+    ctx->need_hash = true;
+    return SPH_OK;
+}
+
+}  // namespace engine
+}  // namespace sphgb
+
 using sphgb::engine::fail;
 
 namespace {

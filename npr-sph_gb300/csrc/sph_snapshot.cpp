@@ -13,7 +13,7 @@
 //   12      4      header bytes (64)
 //   16      8      particles n
 //   24      4      scenes
-//   28      4      reserved (0)
+//   28      4      flags: bit 0 = snapshot carries the slot order
 //   32      8      step count (snapshot) / 0 (trajectory)
 //   40      8      seed: a caller tag kept with the data
 //   48      8      checksum of the payload (snapshot: everything after the
@@ -21,7 +21,10 @@
 //   56      8      reserved (0)
 //   64             scene table: scenes x sph_params (96 B), scenes x u32 counts,
 //                  zero padding to a multiple of 64 bytes
-//   then           snapshot: n x 64 B records
+//   then           snapshot: n x 64 B records, then (flag bit 0) n x u32: the
+//                  record index at each slot of the state, i.e. the within-cell
+//                  order that the next neighbour sort keeps; restoring it makes
+//                  the resumed run repeat the original bit for bit
 //                  trajectory: frames of {u64 step, u64 n, u64 checksum of the
 //                  records, u64 0, n x 64 B records}
 // Checksum: FNV-1a 64 over the little-endian 64-bit words of the bytes (a
@@ -48,7 +51,7 @@ struct Header {
     char magic[8];
     uint32_t version, header_bytes;
     uint64_t n;
-    uint32_t scenes, reserved0;
+    uint32_t scenes, flags;
     uint64_t steps, seed, checksum, reserved1;
 };
 static_assert(sizeof(Header) == 64, "header layout");
@@ -101,7 +104,7 @@ sph_status read_head(FILE* f, const char* magic, Header& h, std::vector<sph_para
     if (std::fread(&h, sizeof(h), 1, f) != 1) return SPH_ERR_INVALID_ARG;
     if (std::memcmp(h.magic, magic, 8) != 0 || h.version != kVersion || h.header_bytes != kHeader)
         return SPH_ERR_INVALID_ARG;
-    if (h.scenes == 0 || h.scenes > (1u << 20) || h.n > (1ull << 30)) return SPH_ERR_INVALID_ARG;
+    if (h.scenes == 0 || h.scenes > (1u << 20) || h.n > (1ull << 30) || (h.flags & ~1u)) return SPH_ERR_INVALID_ARG;
     table.assign(table_bytes(h.scenes), 0);
     if (std::fread(table.data(), 1, table.size(), f) != table.size()) return SPH_ERR_INVALID_ARG;
     params.resize(h.scenes);
@@ -133,15 +136,20 @@ sph_status sph_snapshot_save(sph_ctx* ctx, const char* path, uint64_t seed) {
         std::vector<sph_particle> recs(n);
         sph_status st = sph_download_aos(ctx, recs.data(), (uint32_t)n);
         if (st) return st;
+        std::vector<uint32_t> order(n);
+        st = sphgb::engine::slot_order(ctx, order.data());
+        if (st) return st;
         const std::vector<unsigned char> table = scene_table(ctx);
         uint64_t sum = fnv_words(table.data(), table.size());
         sum = fnv_words(recs.data(), n * sizeof(sph_particle), sum);
+        sum = fnv_words(order.data(), n * 4, sum);
         Header h{};
         std::memcpy(h.magic, kMagicSnap, 8);
         h.version = kVersion;
         h.header_bytes = kHeader;
         h.n = n;
         h.scenes = (uint32_t)ctx->params.size();
+        h.flags = 1;
         h.steps = ctx->steps;
         h.seed = seed;
         h.checksum = sum;
@@ -149,7 +157,8 @@ sph_status sph_snapshot_save(sph_ctx* ctx, const char* path, uint64_t seed) {
         if (!out.f) return fail(ctx, SPH_ERR_INVALID_ARG, std::string("cannot open ") + path + " for writing");
         if (std::fwrite(&h, sizeof(h), 1, out.f) != 1 ||
             std::fwrite(table.data(), 1, table.size(), out.f) != table.size() ||
-            std::fwrite(recs.data(), sizeof(sph_particle), n, out.f) != n)
+            std::fwrite(recs.data(), sizeof(sph_particle), n, out.f) != n ||
+            std::fwrite(order.data(), 4, n, out.f) != n)
             return fail(ctx, SPH_ERR_INVALID_ARG, std::string("short write to ") + path);
         return SPH_OK;
     } catch (const std::bad_alloc&) {
@@ -193,6 +202,11 @@ sph_status sph_snapshot_verify(const char* path) {
         std::vector<sph_particle> recs(h.n);
         if (std::fread(recs.data(), sizeof(sph_particle), h.n, in.f) != h.n) return SPH_ERR_INVALID_ARG;
         sum = fnv_words(recs.data(), h.n * sizeof(sph_particle), sum);
+        if (h.flags & 1u) {
+            std::vector<uint32_t> order(h.n);
+            if (std::fread(order.data(), 4, h.n, in.f) != h.n) return SPH_ERR_INVALID_ARG;
+            sum = fnv_words(order.data(), h.n * 4, sum);
+        }
         return sum == h.checksum ? SPH_OK : SPH_ERR_INVALID_ARG;
     } catch (const std::bad_alloc&) {
         return SPH_ERR_OUT_OF_MEMORY;
@@ -215,12 +229,19 @@ sph_status sph_snapshot_load(const char* path, void* stream, sph_ctx** out) {
         if (std::fread(recs.data(), sizeof(sph_particle), h.n, in.f) != h.n) return SPH_ERR_INVALID_ARG;
         uint64_t sum = fnv_words(table.data(), table.size());
         sum = fnv_words(recs.data(), h.n * sizeof(sph_particle), sum);
+        std::vector<uint32_t> order;
+        if (h.flags & 1u) {
+            order.resize(h.n);
+            if (std::fread(order.data(), 4, h.n, in.f) != h.n) return SPH_ERR_INVALID_ARG;
+            sum = fnv_words(order.data(), h.n * 4, sum);
+        }
         if (sum != h.checksum) return SPH_ERR_INVALID_ARG;
         sph_ctx* ctx = nullptr;
         st = h.scenes == 1 ? sph_create(params.data(), (uint32_t)h.n, stream, &ctx)
                            : sph_create_batch(params.data(), counts.data(), h.scenes, stream, &ctx);
         if (st) return st;
         st = sph_upload_aos(ctx, recs.data(), (uint32_t)h.n);
+        if (!st && !order.empty()) st = sphgb::engine::apply_order(ctx, order.data());
         if (st) {
             sph_destroy(ctx);
             return st;

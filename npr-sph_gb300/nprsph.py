@@ -231,7 +231,7 @@ def write_ppm(path, rgba: np.ndarray) -> None:
 # ---- snapshot and trajectory files (format in include/sph_gb300.h) --------------------------
 
 _HEADER_DTYPE = np.dtype([("magic", "S8"), ("version", "<u4"), ("header_bytes", "<u4"), ("n", "<u8"),
-                          ("scenes", "<u4"), ("reserved0", "<u4"), ("steps", "<u8"), ("seed", "<u8"),
+                          ("scenes", "<u4"), ("flags", "<u4"), ("steps", "<u8"), ("seed", "<u8"),
                           ("checksum", "<u8"), ("reserved1", "<u8")])
 _FRAME_HEAD = np.dtype([("step", "<u8"), ("n", "<u8"), ("checksum", "<u8"), ("reserved", "<u8")])
 
@@ -273,8 +273,13 @@ def read_snapshot(path) -> dict:
     recs = raw[off:off + 64 * n].view(PARTICLE_DTYPE)
     if len(recs) != n:
         raise ValueError("truncated snapshot")
+    order = None
+    if int(h["flags"]) & 1:
+        order = raw[off + 64 * n:off + 68 * n].view("<u4")
+        if len(order) != n:
+            raise ValueError("truncated snapshot")
     return {"n": n, "steps": int(h["steps"]), "seed": int(h["seed"]), "checksum": int(h["checksum"]),
-            "params": params, "counts": counts, "particles": recs}
+            "params": params, "counts": counts, "particles": recs, "slot_order": order}
 
 
 def read_trajectory(path) -> dict:

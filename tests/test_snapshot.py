@@ -19,14 +19,15 @@ def fnv_words(b: bytes) -> int:
     return h
 
 
-def write_snapshot(path, params_list, counts, particles, steps, seed):
+def write_snapshot(path, params_list, counts, particles, steps, seed, order=None):
     """An independent writer of the documented format."""
     table = b"".join(bytes(p) for p in params_list) + np.asarray(counts, "<u4").tobytes()
     table += bytes((-len(table)) % 64)
-    recs = particles.tobytes()
+    recs = particles.tobytes() + (np.asarray(order, "<u4").tobytes() if order is not None else b"")
     head = np.zeros(1, dtype=[("magic", "S8"), ("version", "<u4"), ("hb", "<u4"), ("n", "<u8"), ("sc", "<u4"),
                               ("r0", "<u4"), ("steps", "<u8"), ("seed", "<u8"), ("sum", "<u8"), ("r1", "<u8")])
     head["magic"], head["version"], head["hb"] = b"NPRSPHS1", 1, 64
+    head["r0"] = 1 if order is not None else 0  # flags: bit 0 = slot order present
     head["n"], head["sc"], head["steps"], head["seed"] = len(particles), len(params_list), steps, seed
     head["sum"] = fnv_words(table + recs)
     with open(path, "wb") as f:
@@ -50,6 +51,21 @@ def test_library_reads_a_file_written_to_the_format(sph, tmp_path):
     assert r["steps"] == 17 and r["seed"] == 99 and list(r["counts"]) == [512]
     assert bytes(r["params"][0]) == bytes(sc.params)
     assert np.array_equal(r["particles"], sc.particles)
+
+
+def test_slot_order_section(sph, tmp_path):
+    sc = sph.dam_break(8, 8, 8, seed=4)
+    order = np.random.default_rng(1).permutation(len(sc.particles)).astype(np.uint32)
+    path = tmp_path / "o.snap"
+    write_snapshot(path, [sc.params], [len(sc.particles)], sc.particles, steps=3, seed=1, order=order)
+    assert sph.snapshot_verify(path)
+    r = sph.read_snapshot(path)
+    assert np.array_equal(r["slot_order"], order) and np.array_equal(r["particles"], sc.particles)
+    raw = bytearray(path.read_bytes())
+    raw[-3] ^= 0x10  # the order section is covered by the checksum
+    bad = tmp_path / "bad.snap"
+    bad.write_bytes(bytes(raw))
+    assert not sph.snapshot_verify(bad)
 
 
 def test_corrupt_or_truncated_files_are_refused(sph, tmp_path):
@@ -85,6 +101,7 @@ def test_save_load_continues_bit_for_bit(sph, gpu, tmp_path):
         steps_a = a.steps
     assert sph.snapshot_verify(path)
     assert sph.snapshot_info(path)["steps"] == 25
+    assert sph.read_snapshot(path)["slot_order"] is not None
     with sph.Sim.from_snapshot(path) as b:
         assert b.steps == 25
         b.step(25)
