@@ -32,13 +32,18 @@ inline int nblk(long long n, int t = kT) { return (int)((n + t - 1) / t); }
 // Edge and node features (the header of sph_mpnn.h states them).
 __device__ __forceinline__ void edge_feat(float4 pi, float4 vi, float4 pj, float4 vj, const FrameConst& fc,
                                           float* e) {
-    const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
-    const float r = sqrtf(dx * dx + dy * dy + dz * dz);
     const float ih = 1.0f / fc.h, ic = 1.0f / fc.c;
-    e[0] = dx * ih; e[1] = dy * ih; e[2] = dz * ih;
-    e[3] = (vj.x - vi.x) * ic; e[4] = (vj.y - vi.y) * ic; e[5] = (vj.z - vi.z) * ic;
-    e[6] = r * ih;
-    e[7] = 1.0f - r * ih;
+    const float dx = (pj.x - pi.x) * ih, dy = (pj.y - pi.y) * ih, dz = (pj.z - pi.z) * ih;
+    const float ux = (vj.x - vi.x) * ic, uy = (vj.y - vi.y) * ic, uz = (vj.z - vi.z) * ic;
+    const float r = sqrtf(dx * dx + dy * dy + dz * dz);
+    const float q = 1.0f - r;
+    const float sg = r > 0.0f ? q * q / r : 0.0f;
+    e[0] = dx; e[1] = dy; e[2] = dz;
+    e[3] = ux; e[4] = uy; e[5] = uz;
+    e[6] = r;
+    e[7] = q;
+    e[8] = sg * dx; e[9] = sg * dy; e[10] = sg * dz;
+    e[11] = q * ux; e[12] = q * uy; e[13] = q * uz;
 }
 
 __device__ __forceinline__ void node_feat(float4 vi, float rho, int cnt, const FrameConst& fc, float* nf) {

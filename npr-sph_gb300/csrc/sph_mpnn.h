@@ -5,7 +5,9 @@
 // The network (no counterpart in the reference) predicts, for every particle,
 // the mean accelerations over a macro-step of 4*dt from its <= 32 nearest
 // neighbours:
-//   e_ij = [(x_j-x_i)/h, (v_j-v_i)/c, r/h, 1-r/h]                                 8 edge features
+//   e_ij = [d, u, r/h, q, q^2 d/(r/h), q u]    d = (x_j-x_i)/h, u = (v_j-v_i)/c, q = 1-r/h
+//          (the last two are the shapes of the spiky gradient and of the viscosity
+//          Laplacian, force_comp.glsl:59-60; the first at r = 0 is zero)        14 edge features
 //   n_i  = [v_i/c, rho_i/rho_self-1, (rho_i-rho0)/rho_self, log10(mu)/4, cnt/K, 1, c dt/h]   9
 //   round 1: M1 = sum_j relu(e_ij We1 + be1)/K;  H1 = relu([M1 n] Wn1 + bn1);  P = H1 Wp
 //   round 2: M2 = sum_j relu(e_ij We2 + P_j + be2)/K;  H2 = relu([M2 H1] Wn2 + bn2)
@@ -31,7 +33,7 @@ namespace mpnn {
 
 constexpr int K = 32;   // neighbours per particle
 constexpr int W = 64;   // hidden width
-constexpr int FE = 8;   // edge features
+constexpr int FE = 14;  // edge features (the bias column FE of the 16-wide MMA k-tile is 1)
 constexpr int FN = 9;   // node features
 constexpr int FO = 6;   // outputs: O_v (3), O_x (3)
 constexpr int kOS = 8;  // stride of an output / target row (floats)

@@ -74,7 +74,7 @@ __global__ void k_prep_frags(const float* __restrict__ prm, uint32_t* __restrict
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= kFragTotal) return;
     int r = t;
-    if (r < kFragWn1) {  // edge layers, transposed: A[o][k] = W[k][o]; bias row 8
+    if (r < kFragWn1) {  // edge layers, transposed: A[o][k] = W[k][o]; bias row FE
         const bool second = r >= kFragWe2;
         if (second) r -= kFragWe2;
         const float* Wm = prm + (second ? kWe2 : kWe1);
@@ -83,7 +83,7 @@ __global__ void k_prep_frags(const float* __restrict__ prm, uint32_t* __restrict
         const int g = lane >> 2, tq = lane & 3;
         const int o = mt * 16 + g + ((q & 1) ? 8 : 0);
         const int k = 2 * tq + ((q & 2) ? 8 : 0);
-        fr[t] = pack_bf16(wel(Wm, FE, W, b, 8, k, o), wel(Wm, FE, W, b, 8, k + 1, o));
+        fr[t] = pack_bf16(wel(Wm, FE, W, b, FE, k, o), wel(Wm, FE, W, b, FE, k + 1, o));
         return;
     }
     // node layers: B[k][o], b0 rows k0, k0+1; b1 rows k0+8, k0+9
@@ -102,17 +102,23 @@ __global__ void k_prep_frags(const float* __restrict__ prm, uint32_t* __restrict
     fr[t] = pack_bf16(wel(Wm, kin, nout, b, brow, k, o), wel(Wm, kin, nout, b, brow, k + 1, o));
 }
 
-// Edge features 2t, 2t+1 of the edge (i -> j) as bf16x2 (B fragment row pair), and the bias pair.
+// B fragment of the edge (i -> j): lane tq holds features (2 tq, 2 tq + 1) in b0 and
+// (8 + 2 tq, 9 + 2 tq) in b1 as bf16 pairs; feature FE (= 14) is the bias column (1) and 15 is
+// zero. Every lane computes all features and selects its pairs (no divergence).
+static_assert(FE == 14, "edge_b is written for 14 edge features plus the bias column");
 __device__ __forceinline__ void edge_b(float4 pi, float4 vi, float4 pj, float4 vj, float ih, float ic, int tq,
                                        bool valid, uint32_t& b0, uint32_t& b1) {
-    const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
-    float f0, f1;
-    if (tq == 0) { f0 = dx * ih; f1 = dy * ih; }
-    else if (tq == 1) { f0 = dz * ih; f1 = (vj.x - vi.x) * ic; }
-    else if (tq == 2) { f0 = (vj.y - vi.y) * ic; f1 = (vj.z - vi.z) * ic; }
-    else { const float r = sqrtf(dx * dx + dy * dy + dz * dz) * ih; f0 = r; f1 = 1.0f - r; }
-    b0 = valid ? pack_bf16(f0, f1) : 0u;
-    b1 = (valid && tq == 0) ? pack_bf16(1.0f, 0.0f) : 0u;
+    const float dx = (pj.x - pi.x) * ih, dy = (pj.y - pi.y) * ih, dz = (pj.z - pi.z) * ih;
+    const float ux = (vj.x - vi.x) * ic, uy = (vj.y - vi.y) * ic, uz = (vj.z - vi.z) * ic;
+    const float r = sqrtf(dx * dx + dy * dy + dz * dz);
+    const float q = 1.0f - r;
+    const float sg = r > 0.0f ? q * q / r : 0.0f;
+    const float a0 = tq == 0 ? dx : tq == 1 ? dz : tq == 2 ? uy : r;
+    const float a1 = tq == 0 ? dy : tq == 1 ? ux : tq == 2 ? uz : q;
+    const float c0 = tq == 0 ? sg * dx : tq == 1 ? sg * dz : tq == 2 ? q * uy : 1.0f;
+    const float c1 = tq == 0 ? sg * dy : tq == 1 ? q * ux : tq == 2 ? q * uz : 0.0f;
+    b0 = valid ? pack_bf16(a0, a1) : 0u;
+    b1 = valid ? pack_bf16(c0, c1) : 0u;
 }
 
 struct EdgeFrags {

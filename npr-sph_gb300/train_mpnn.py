@@ -114,7 +114,7 @@ def main() -> None:
 def init_params(seed: int) -> np.ndarray:
     """He-style initial parameters in the library's flat layout (sph_mpnn_set_params)."""
     rng = np.random.default_rng(seed)
-    W, FE, FN, FO = 64, 8, 9, 6
+    W, FE, FN, FO = 64, 14, 9, 6
     shapes = [("We1", (FE, W)), ("be1", (W,)), ("Wn1", (W + FN, W)), ("bn1", (W,)), ("Wp", (W, W)),
               ("We2", (FE, W)), ("be2", (W,)), ("Wn2", (2 * W, W)), ("bn2", (W,)), ("Wo", (W, FO)), ("bo", (FO,))]
     out = []

@@ -9,7 +9,9 @@ The network has no counterpart in the reference (NPR-SPH has no learned componen
 predicts, per particle, the mean accelerations of the next 4 plain steps (a macro-step of
 4*dt) from the particle's neighbourhood:
 
-  edge features  e_ij = [ (x_j-x_i)/h (3), (v_j-v_i)/c (3), r/h, 1-r/h ]          (8)
+  edge features  e_ij = [ d (3), u (3), r/h, q, q^2 d / (r/h) (3), q u (3) ]        (14)
+                 d = (x_j-x_i)/h, u = (v_j-v_i)/c, q = 1 - r/h; the spiky-gradient and
+                 viscosity-Laplacian shapes of force_comp.glsl:59-60 (the first is 0 at r = 0)
   node features  n_i  = [ v_i/c (3), rho_i/rho_self - 1, (rho_i-rho0)/rho_self,
                           log10(mu)/4, cnt_i/K, 1, c*dt/h ]                         (9)
   round 1   Z1_ij = e_ij We1 + be1,  M1_i = sum_j relu(Z1_ij) / K
@@ -31,7 +33,7 @@ import numpy as np
 
 K = 32
 W = 64
-FE = 8
+FE = 14
 FN = 9
 FO = 6
 
@@ -72,16 +74,18 @@ def init_params(seed: int = 0) -> np.ndarray:
 
 
 def features(pos, vel, rho, nb, cnt, h, c, rho_self, rho0, mu, dt):
-    """Edge features e (n, K, 8) with padded edges zeroed, edge mask (n, K), node features (n, 9)."""
+    """Edge features e (n, K, 14) with padded edges zeroed, edge mask (n, K), node features (n, 9)."""
     pos = np.asarray(pos, np.float64)
     vel = np.asarray(vel, np.float64)
     n = len(pos)
     mask = np.arange(K)[None, :] < np.asarray(cnt)[:, None]
     j = np.where(mask, nb, 0)
-    d = pos[j] - pos[:, None, :]
-    dv = vel[j] - vel[:, None, :]
+    d = (pos[j] - pos[:, None, :]) / h
+    u = (vel[j] - vel[:, None, :]) / c
     r = np.sqrt((d * d).sum(-1))
-    e = np.concatenate([d / h, dv / c, (r / h)[..., None], (1.0 - r / h)[..., None]], axis=-1)
+    q = 1.0 - r
+    sg = np.where(r > 0.0, q * q / np.where(r > 0.0, r, 1.0), 0.0)
+    e = np.concatenate([d, u, r[..., None], q[..., None], sg[..., None] * d, q[..., None] * u], axis=-1)
     e = np.where(mask[..., None], e, 0.0)
     rho = np.asarray(rho, np.float64)
     nf = np.zeros((n, FN))

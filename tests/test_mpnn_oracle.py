@@ -29,14 +29,18 @@ def small_frame(seed: int, n: int = 40):
 
 def test_layout_size():
     assert MO.n_params() == len(MO.init_params(0))
-    assert MO.FO == 6 and MO.FN == 9 and MO.FE == 8
+    assert MO.FO == 6 and MO.FN == 9 and MO.FE == 14
 
 
 def test_features():
     e, mask, nf, nb, _ = small_frame(1)
     assert np.all(e[~mask] == 0.0)
     r = e[..., 6]
-    assert np.all(r[mask] < 1.0) and np.allclose(e[..., 7][mask], 1.0 - r[mask])
+    q = e[..., 7]
+    assert np.all(r[mask] < 1.0) and np.allclose(q[mask], 1.0 - r[mask])
+    # the spiky-gradient shape: |q^2 d / r| = q^2; the Laplacian shape: q u
+    assert np.allclose(np.linalg.norm(e[..., 8:11], axis=-1)[mask], (q * q)[mask])
+    assert np.allclose(e[..., 11:14][mask], (q[..., None] * e[..., 3:6])[mask])
     assert np.allclose(nf[:, 7], 1.0)
     assert np.allclose(nf[:, 8], 44.72 * 1e-4 / 0.02)
 
