@@ -70,6 +70,18 @@ def barrier(world: int) -> None:
         dist.barrier()
 
 
+def profiled_traffic(kernel: str):
+    """DRAM bytes (read + write) per launch of `kernel` from the committed ncu summary of the
+    dam break (a line `traffic_bytes_per_launch <kernel>: <bytes>`), or None."""
+    import re
+
+    prof = REPO / "profiles" / "pair_kernels_dam_break_1m.md"
+    if not prof.exists():
+        return None
+    m = re.search(rf"^traffic_bytes_per_launch {re.escape(kernel)}: (\d+)", prof.read_text(), re.M)
+    return int(m.group(1)) if m else None
+
+
 def measured_peaks() -> tuple[dict, str]:
     p = REPO / "MEASURED_PEAKS.json"
     if p.exists():
@@ -497,10 +509,7 @@ def run_ours(args) -> None:
     achieved = B_ALG["force_integrate"] * n / (fi_ms * 1e-3) / 1e9
     step_achieved = B_ALG_STEP * n * args.steps / local_s / 1e9
     cpu = cpu_oracle_rate(args.cpu_seconds) if args.cpu_seconds > 0 else None
-    traffic = None
-    prof = REPO / "profiles" / "force_integrate_traffic.json"
-    if prof.exists():
-        traffic = json.loads(prof.read_text()).get("bytes_per_launch_1m")
+    traffic = profiled_traffic("k_force_integrate")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,

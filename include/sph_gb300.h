@@ -286,9 +286,8 @@ sph_status sph_neighbor_lists(sph_ctx* ctx, int32_t* nb_ids, int32_t* counts, fl
  *
  * It exists for callers that cannot allocate device memory at the point they
  * need it: a render or game loop that reserves its GPU memory up front and
- * must not allocate per frame, a plugin host that owns every buffer, code that
- * records its work into a CUDA graph (where cudaMalloc would break the
- * capture). It calls no cudaMalloc/cudaFree: its scratch is a fixed 96 KiB
+ * must not allocate per frame, or a plugin host that owns every buffer and
+ * hands the library only pointers. It calls no cudaMalloc/cudaFree: its scratch is a fixed 96 KiB
  * array in device memory, which every GPU that loads this library holds until
  * the process exits.
  *   - n <= 4,194,304 records; larger n returns SPH_ERR_CAPACITY.

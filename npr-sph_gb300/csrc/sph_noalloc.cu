@@ -3,9 +3,8 @@
 //
 // Some callers of this library cannot allocate device memory when they need
 // the diagnostics: a renderer or game loop that reserves its GPU memory budget
-// up front and must not allocate per frame, a plugin host that owns every
-// buffer, or code that records its GPU work into a CUDA graph, where a
-// cudaMalloc would break the capture. They hold the particles in their own
+// up front and must not allocate per frame, or a plugin host that owns every
+// buffer and hands the library only pointers. They hold the particles in their own
 // device buffer (the reference keeps them in an SSBO, Main.cpp:524-527) and
 // pass that buffer and an output buffer in.
 //

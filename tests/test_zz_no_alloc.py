@@ -1,8 +1,7 @@
 """sph_reduce_aos_noalloc: FP64 diagnostics of a caller-owned device buffer with no allocation.
 
 Callers that cannot allocate device memory when they need the diagnostics (a frame loop
-with a fixed GPU memory budget, a plugin host that owns every buffer, work recorded into
-a CUDA graph) pass their particle buffer and an output buffer; the scratch of the
+with a fixed GPU memory budget, a plugin host that owns every buffer) pass their particle buffer and an output buffer; the scratch of the
 reduction is a fixed device array inside the library. This checks it through the C ABI
 against the context-based sph_reduce on the same state, on two calls in a row.
 
