@@ -398,6 +398,16 @@ def learned_workload(args, stream, flush) -> dict:
         learned.refresh_density()
         plain.refresh_density()
         a, b = learned.download(), plain.download()
+        # What the network gains: one judged macro-step from the same state (the plain run's
+        # end state) with the trained network and with a zero network (v' = v, x' = x + 4 dt v,
+        # then the momentum projection adds gravity).
+        gain = {}
+        with S.Net(16, stream=stream.cuda_stream) as zero:
+            zero.set_params(np.zeros(int(S.lib.sph_mpnn_num_params()), np.float32))
+            for name, nn in (("trained", net), ("zero_network", zero)):
+                learned.upload(b)
+                r = learned.learned_step(nn, 1, 1, 1e30, 1e30)
+                gain[name] = {"density_dev": r.last_density_dev, "momentum_dev": r.last_momentum_dev}
     rl, rp = a["extras"][:, 0].astype(np.float64), b["extras"][:, 0].astype(np.float64)
     judged = sum(r.judged for r in reps)
     n_learned = sum(r.learned_macro_steps for r in reps)
@@ -413,6 +423,7 @@ def learned_workload(args, stream, flush) -> dict:
         "judged_mean_density_dev": sum(r.sum_density_dev for r in reps) / max(judged, 1),
         "judged_max_density_dev": max((r.max_density_dev for r in reps), default=0.0),
         "end_state_mean_density_dev_vs_plain_run": float(np.mean(np.abs(rl - rp) / rp)),
+        "one_macro_step_vs_4_plain_steps": gain,
         "precision": "BF16 weights/activations, FP32 accumulate (mma.sync m16n8k16)",
         "weights": str(WEIGHTS.relative_to(REPO)),
     })

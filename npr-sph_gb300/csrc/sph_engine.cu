@@ -33,16 +33,19 @@ sph_status fail(sph_ctx* c, sph_status code, const std::string& msg) {
 
 namespace {
 
-// State in record order -> the given slot order (order[s] = record at slot s).
+// State in record order -> the given slot order (order[s] = record at slot s): positions,
+// velocities and the uploaded (rho, pres), which live in slot order like the rest.
 __global__ void __launch_bounds__(256) k_apply_order(const float4* __restrict__ pos, const float4* __restrict__ vel,
-                                                     const uint32_t* __restrict__ order, int n,
-                                                     float4* __restrict__ pos_out, float4* __restrict__ vel_out) {
+                                                     const float2* __restrict__ rhop, const uint32_t* __restrict__ order,
+                                                     int n, float4* __restrict__ pos_out, float4* __restrict__ vel_out,
+                                                     float2* __restrict__ rhop_out) {
     const int s = blockIdx.x * 256 + threadIdx.x;
     if (s >= n) return;
     const uint32_t id = order[s];
     if (id < (uint32_t)n) {
         pos_out[s] = pos[id];
         vel_out[s] = vel[id];
+        rhop_out[s] = rhop[id];
     }
 }
 
@@ -70,19 +73,25 @@ sph_status apply_order(sph_ctx* ctx, const uint32_t* host_order) {
         seen[host_order[s]] = 1;
     }
     uint32_t* d = nullptr;
+    float2* rh = nullptr;
     cudaError_t e = cudaMalloc(&d, sizeof(uint32_t) * (size_t)n);
+    if (e == cudaSuccess) e = cudaMalloc(&rh, sizeof(float2) * (size_t)n);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(d, host_order, sizeof(uint32_t) * (size_t)n, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess) {
-        k_apply_order<<<(n + 255) / 256, 256, 0, ctx->stream>>>(ctx->b.pos, ctx->b.vel, d, n, ctx->b.pos_s, ctx->b.vel_s);
+        k_apply_order<<<(n + 255) / 256, 256, 0, ctx->stream>>>(ctx->b.pos, ctx->b.vel, ctx->b.rhop, d, n, ctx->b.pos_s,
+                                                                ctx->b.vel_s, rh);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(ctx->b.pos, ctx->b.pos_s, sizeof(float4) * (size_t)n, cudaMemcpyDeviceToDevice, ctx->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(ctx->b.vel, ctx->b.vel_s, sizeof(float4) * (size_t)n, cudaMemcpyDeviceToDevice, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ctx->b.rhop, rh, sizeof(float2) * (size_t)n, cudaMemcpyDeviceToDevice, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (d) cudaFree(d);
+    if (rh) cudaFree(rh);
     if (e != cudaSuccess) return fail(ctx, SPH_ERR_CUDA, std::string("slot order: ") + cudaGetErrorString(e));
     ctx->need_hash = true;
     return SPH_OK;

@@ -96,6 +96,7 @@ def test_save_load_continues_bit_for_bit(sph, gpu, tmp_path):
         a.upload(sc.particles)
         a.step(25)
         a.save(path, seed=6)
+        saved = a.download()
         a.step(25)
         end_a = a.download()
         steps_a = a.steps
@@ -104,6 +105,7 @@ def test_save_load_continues_bit_for_bit(sph, gpu, tmp_path):
     assert sph.read_snapshot(path)["slot_order"] is not None
     with sph.Sim.from_snapshot(path) as b:
         assert b.steps == 25
+        assert np.array_equal(b.download(), saved)  # every field, rho and pres included
         b.step(25)
         end_b = b.download()
         assert b.steps == steps_a
