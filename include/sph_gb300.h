@@ -210,12 +210,18 @@ sph_status sph_tile_stats(sph_ctx* ctx, uint32_t out[2]);
  * kernels, on frames recorded from the plain step itself.
  * Judge: the macro-steps run in intervals of judge_every. Each learned interval
  * starts from a checkpoint; its last macro-step is judged: from the same state a
- * learned macro-step and 4 plain steps are compared by particle id. When the mean
- * relative density deviation exceeds density_tol, or the momentum difference
- * (relative to sum m|v| + M |G| 4 dt) exceeds momentum_tol, the interval is rolled
- * back to its checkpoint and run by plain SPH, and after the k-th failure in a row
- * plain SPH also runs the next 2^(k-1) - 1 intervals (at most 7). This judge state
- * lives in the context across sph_learned_step calls; an upload clears it. */
+ * learned macro-step and 4 plain steps are compared with FP64 reductions. When the
+ * density deviation exceeds density_tol, or the momentum difference (relative to
+ * sum m|v| + M |G| 4 dt) exceeds momentum_tol, the interval is rolled back to its
+ * checkpoint and run by plain SPH, and after the k-th failure in a row plain SPH
+ * also runs the next 2^(k-1) - 1 intervals (at most 7). The density deviation is
+ * (sph_learned_set_judge):
+ *   SPH_JUDGE_MEAN_DENSITY (default): the deviation of the mean density,
+ *     |sum rho_learned - sum rho_plain| / sum rho_plain;
+ *   SPH_JUDGE_PARTICLE_DENSITY: the mean over particles (by id) of
+ *     |rho_learned - rho_plain| / rho_plain, a much stricter bound.
+ * Both are reported whichever decides. This judge state lives in the context
+ * across sph_learned_step calls; an upload clears it (the metric setting stays). */
 typedef struct sph_mpnn sph_mpnn;
 
 typedef struct sph_learned_report {
@@ -223,12 +229,17 @@ typedef struct sph_learned_report {
     uint64_t plain_macro_steps;    /* macro-steps (4 plain steps each) run by plain SPH */
     uint64_t judged;
     uint64_t fallbacks;            /* judged intervals that failed and were rolled back */
-    double last_density_dev;       /* mean |rho_learned - rho_plain| / rho_plain at the last judge */
+    double last_density_dev;       /* mean over particles of |rho_learned - rho_plain| / rho_plain at the last judge */
     double last_momentum_dev;
     double max_density_dev;
     double sum_density_dev;        /* over all judges */
     uint64_t discarded_macro_steps;/* learned macro-steps thrown away by roll-backs */
+    double last_mean_rho_dev;      /* |sum rho_learned - sum rho_plain| / sum rho_plain at the last judge */
+    double max_mean_rho_dev;
 } sph_learned_report;
+
+#define SPH_JUDGE_MEAN_DENSITY      0
+#define SPH_JUDGE_PARTICLE_DENSITY  1
 
 uint32_t sph_mpnn_num_params(void);
 /* Network with a training workspace for frames of up to n_frame particles. */
@@ -264,6 +275,9 @@ sph_status sph_mpnn_train(sph_mpnn* net, uint32_t steps, float lr, uint64_t seed
  * (judge_every = 0: never). */
 sph_status sph_learned_step(sph_ctx* ctx, sph_mpnn* net, int32_t n_macro, int32_t judge_every,
                             float density_tol, float momentum_tol, sph_learned_report* report);
+/* The density deviation the judge of sph_learned_step compares with density_tol:
+ * SPH_JUDGE_MEAN_DENSITY (default) or SPH_JUDGE_PARTICLE_DENSITY. */
+sph_status sph_learned_set_judge(sph_ctx* ctx, int32_t metric);
 /* Recompute rho and pres at the current positions (the state is re-sorted by cell). */
 sph_status sph_refresh_density(sph_ctx* ctx);
 /* The learned macro-step's input lists at the current positions, by particle id (record
@@ -298,6 +312,43 @@ sph_status sph_neighbor_lists(sph_ctx* ctx, int32_t* nb_ids, int32_t* counts, fl
  *     streams without ordering between them) race and give wrong sums. */
 sph_status sph_reduce_aos_noalloc(const sph_particle* dev_particles, uint32_t n, const sph_params* p,
                                   double* dev_sums, void* stream);
+
+/* ---- static obstacles (new; the reference lists "objects to collide with" as
+ * future work, README.md:59, and loads its meshes with LoadMesh, LoadMesh.cpp:16-55)
+ * An obstacle is a signed distance field sampled on a regular grid: sample
+ * (i, j, k) at origin + spacing * (i, j, k), stored x fastest, negative inside.
+ * Every step, after the wall clamp of integrate_comp.glsl:45-77, a particle at
+ * x with phi(x) < 0 (phi: trilinear interpolation of the samples; no obstacle
+ * outside the sampled box) is moved out along n = g / |g|, g the trilinear
+ * interpolation of the samples' central-difference gradients (one-sided on the
+ * grid's faces), and its velocity's normal component gets the walls' rule,
+ * v_n *= -damping:
+ *   x -= phi(x) n;   if v.n < 0: v -= (1 + damping) (v.n) n;
+ * then the position is clamped into the box again (velocity unchanged). The
+ * learned macro-step applies the same rule after its update. One obstacle per
+ * context; in a batch it applies to every scene, in each scene's coordinates. */
+
+/* Set (sdf non-NULL) or remove (sdf NULL) the obstacle. dims >= 2 per axis, at most
+ * 2^28 samples; spacing > 0. The samples are copied to the device. */
+sph_status sph_set_obstacle(sph_ctx* ctx, const float* sdf, const int32_t dims[3], const float origin[3],
+                            float spacing);
+
+/* Signed distance field of a closed triangle mesh on the grid above, computed on the
+ * current device: |phi| = the distance to the nearest triangle, negative where the
+ * generalised winding number of the mesh exceeds 1/2 (the sum over triangles of their
+ * solid angles, Van Oosterom and Strackee's formula, over 4 pi). verts: nv x 3 floats,
+ * tris: nt x 3 vertex indices (counter-clockwise seen from outside), sdf_out: host array
+ * of dims[0] * dims[1] * dims[2] floats. */
+sph_status sph_sdf_from_mesh(const float* verts, uint32_t nv, const uint32_t* tris, uint32_t nt,
+                             const int32_t dims[3], const float origin[3], float spacing, float* sdf_out);
+
+/* Vertices and triangles of a Wavefront OBJ file (no GPU needed): `v x y z` and `f`
+ * lines (vertex index forms a, a/b, a/b/c, a//c; negative indices count from the end;
+ * polygons are split into a fan of triangles); other lines are ignored. In: *nv, *nt
+ * the capacities of verts (nv x 3 floats) and tris (nt x 3); out: the file's counts.
+ * With verts or tris NULL only the counts are returned. SPH_ERR_CAPACITY when the
+ * arrays are too small, SPH_ERR_INVALID_ARG for a missing file or a bad index. */
+sph_status sph_obj_read(const char* path, float* verts, uint32_t* nv, uint32_t* tris, uint32_t* nt);
 
 /* ---- headless toon rendering of the particles ----------------------------
  * The reference draws the particles after the step (Main.cpp:311-337, SPH

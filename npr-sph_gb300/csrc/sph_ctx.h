@@ -29,6 +29,7 @@ struct sph_ctx {
     // judge state of the learned macro-step, kept across sph_learned_step calls (cleared by uploads)
     int judge_failures = 0;  // failed judges in a row
     int judge_backoff = 0;   // plain intervals still to run before the next learned attempt
+    int judge_metric = SPH_JUDGE_MEAN_DENSITY;  // density deviation the judge decides on
     long long cell_cap = 0;
     int tile_cap = 0;
     double* diag_dev = nullptr;
@@ -40,6 +41,11 @@ struct sph_ctx {
     uint32_t* q_cnt = nullptr;
     unsigned long long* q_dig = nullptr;
     int q_cap = 0;
+    // static obstacle (sph_set_obstacle): signed distance samples on the device, or null
+    float* sdf_dev = nullptr;
+    int sdf_dims[3] = {0, 0, 0};
+    float sdf_org[3] = {0.f, 0.f, 0.f};
+    float sdf_inv = 0.f;
     // render scratch (sph_render): depth/id keys, positions by id, a device image for host output
     void* render_buf = nullptr;
     size_t render_cap = 0;

@@ -8,6 +8,7 @@
 //   density                     (rho_pres_comp.glsl)
 //   force + integrate + hash    (force_comp.glsl + integrate_comp.glsl)
 // captured once into a CUDA graph and replayed per step.
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -142,6 +143,12 @@ sph_status rebuild_geometry(sph_ctx* ctx) {
     for (size_t i = 0; i < sc.size(); ++i) {
         sc[i] = make_scene_dev(ctx->params[i], ctx->cfg.stencil, (int)cell, (int)first, (int)ctx->counts[i], keep);
         sc[i].row_base = (int)rows;
+        sc[i].sdf = ctx->sdf_dev;
+        for (int a = 0; a < 3; ++a) {
+            sc[i].sdim[a] = ctx->sdf_dims[a];
+            sc[i].sorg[a] = ctx->sdf_org[a];
+        }
+        sc[i].sinv = ctx->sdf_inv;
         cell += (long long)sc[i].dim[0] * sc[i].dim[1] * sc[i].dim[2];
         rows += (long long)sc[i].dim[1] * sc[i].dim[2];
         first += ctx->counts[i];
@@ -435,7 +442,7 @@ sph_status sph_destroy(sph_ctx* ctx) {
     void* ptrs[] = {b.pos, b.vel, b.pos_s, b.vel_s, b.rhop, b.force_s, b.force_up, b.aux, b.aos, b.key, b.rank,
                     b.perm, b.count, b.start, b.scan_state, b.scan_ticket, b.slot_of_id, b.err, b.partials,
                     b.scenes, b.tile_stats, ctx->diag_dev, ctx->scene_first_dev, ctx->q_ids, ctx->q_cnt, ctx->q_dig,
-                    ctx->render_buf};
+                    ctx->render_buf, ctx->sdf_dev};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (auto& e : ctx->ev)
@@ -446,6 +453,49 @@ sph_status sph_destroy(sph_ctx* ctx) {
 }
 
 const char* sph_last_error(const sph_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+sph_status sph_set_obstacle(sph_ctx* ctx, const float* sdf, const int32_t dims[3], const float origin[3],
+                            float spacing) {
+    if (!ctx) return SPH_ERR_INVALID_ARG;
+    GUARD_BEGIN
+    CK(cudaSetDevice(ctx->device));
+    if (!sdf) {  // remove
+        if (ctx->sdf_dev) {
+            CK(cudaStreamSynchronize(ctx->stream));
+            CK(cudaFree(ctx->sdf_dev));
+        }
+        ctx->sdf_dev = nullptr;
+        ctx->sdf_dims[0] = ctx->sdf_dims[1] = ctx->sdf_dims[2] = 0;
+        ctx->sdf_inv = 0.0f;
+        return rebuild_geometry(ctx);
+    }
+    if (!dims || !origin) return fail(ctx, SPH_ERR_INVALID_ARG, "obstacle: null dims or origin");
+    long long total = 1;
+    for (int a = 0; a < 3; ++a) {
+        if (dims[a] < 2 || dims[a] > (1 << 20)) return fail(ctx, SPH_ERR_INVALID_ARG, "obstacle: dims must be >= 2");
+        if (!std::isfinite(origin[a])) return fail(ctx, SPH_ERR_INVALID_ARG, "obstacle: origin not finite");
+        total *= dims[a];
+    }
+    if (total > (1ll << 28)) return fail(ctx, SPH_ERR_INVALID_ARG, "obstacle: more than 2^28 samples");
+    if (!(spacing > 0.0f) || !std::isfinite(spacing)) return fail(ctx, SPH_ERR_INVALID_ARG, "obstacle: spacing");
+    float* d = nullptr;
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMalloc(&d, sizeof(float) * (size_t)total));
+    cudaError_t e = cudaMemcpy(d, sdf, sizeof(float) * (size_t)total, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(d);
+        return fail(ctx, SPH_ERR_CUDA, std::string("obstacle upload: ") + cudaGetErrorString(e));
+    }
+    if (ctx->sdf_dev) cudaFree(ctx->sdf_dev);
+    ctx->sdf_dev = d;
+    for (int a = 0; a < 3; ++a) {
+        ctx->sdf_dims[a] = dims[a];
+        ctx->sdf_org[a] = origin[a];
+    }
+    ctx->sdf_inv = 1.0f / spacing;
+    return rebuild_geometry(ctx);
+    GUARD_END
+}
 
 sph_status sph_set_params(sph_ctx* ctx, const sph_params* p) {
     if (!ctx || !p) return SPH_ERR_INVALID_ARG;

@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -344,3 +345,60 @@ sph_status sph_image_write_ppm(const char* path, const uint8_t* rgba, int32_t wi
 }
 
 }  // extern "C"
+
+// ---- Wavefront OBJ reader (the mesh input of sph_sdf_from_mesh) ---------------------------
+// Reads `v x y z` and `f i j k ...` lines; a face vertex is "a", "a/b", "a/b/c" or "a//c"
+// (1-based, negative = counted back from the last vertex read so far); a polygon with m
+// vertices becomes the m - 2 triangles (v0, v_k, v_k+1). Other lines are skipped.
+extern "C" sph_status sph_obj_read(const char* path, float* verts, uint32_t* nv, uint32_t* tris, uint32_t* nt) {
+    if (!path || !nv || !nt) return SPH_ERR_INVALID_ARG;
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return SPH_ERR_INVALID_ARG;
+    std::vector<float> v;
+    std::vector<uint32_t> t;
+    sph_status st = SPH_OK;
+    char line[4096];
+    std::vector<long long> poly;
+    while (st == SPH_OK && std::fgets(line, sizeof line, f)) {
+        const char* s = line;
+        while (*s == ' ' || *s == '\t') ++s;
+        if (s[0] == 'v' && (s[1] == ' ' || s[1] == '\t')) {
+            float x, y, z;
+            if (std::sscanf(s + 2, "%f %f %f", &x, &y, &z) != 3) { st = SPH_ERR_INVALID_ARG; break; }
+            v.push_back(x); v.push_back(y); v.push_back(z);
+        } else if (s[0] == 'f' && (s[1] == ' ' || s[1] == '\t')) {
+            poly.clear();
+            const char* q = s + 2;
+            const long long nvert = (long long)(v.size() / 3);
+            while (true) {
+                while (*q == ' ' || *q == '\t') ++q;
+                if (*q == '\0' || *q == '\n' || *q == '\r' || *q == '#') break;
+                char* end = nullptr;
+                const long long idx = std::strtoll(q, &end, 10);
+                if (end == q) { st = SPH_ERR_INVALID_ARG; break; }
+                const long long k = idx > 0 ? idx - 1 : nvert + idx;  // idx == 0 is invalid
+                if (idx == 0 || k < 0 || k >= nvert) { st = SPH_ERR_INVALID_ARG; break; }
+                poly.push_back(k);
+                q = end;
+                while (*q && *q != ' ' && *q != '\t' && *q != '\n' && *q != '\r') ++q;  // skip /vt/vn
+            }
+            if (st == SPH_OK && poly.size() < 3) st = SPH_ERR_INVALID_ARG;
+            for (size_t k = 1; st == SPH_OK && k + 1 < poly.size(); ++k) {
+                t.push_back((uint32_t)poly[0]);
+                t.push_back((uint32_t)poly[k]);
+                t.push_back((uint32_t)poly[k + 1]);
+            }
+        }
+    }
+    std::fclose(f);
+    if (st != SPH_OK) return st;
+    const uint32_t cv = (uint32_t)(v.size() / 3), ct = (uint32_t)(t.size() / 3);
+    const uint32_t cap_v = *nv, cap_t = *nt;
+    *nv = cv;
+    *nt = ct;
+    if (!verts || !tris) return SPH_OK;
+    if (cap_v < cv || cap_t < ct) return SPH_ERR_CAPACITY;
+    std::memcpy(verts, v.data(), sizeof(float) * v.size());
+    std::memcpy(tris, t.data(), sizeof(uint32_t) * t.size());
+    return SPH_OK;
+}

@@ -41,6 +41,11 @@ struct SceneDev {
     int keep_force;
     int row_base;     // first cell row (y, z) of this scene in the global row numbering
     int pad_;
+    // Static obstacle (sph_set_obstacle): signed distance samples, null when there is none.
+    const float* sdf; // [sdim z][sdim y][sdim x], device memory, negative inside
+    int sdim[3];
+    float sorg[3];    // position of sample (0, 0, 0)
+    float sinv;       // 1 / sample spacing
 };
 
 // Device buffers of one engine (single scene or a batch of scenes).

@@ -10,9 +10,10 @@
 //   accelerations), then the wall clamp of integrate_comp.glsl:45-77 with the
 //   damping, then the cell hash.
 // Judge (every judge_every macro-steps): from the same state, one learned
-// macro-step and 4 plain steps; the mean relative density deviation between
-// the two results and their momentum difference decide. Above the bounds the
-// plain result is kept and plain SPH runs the next judge_every macro-steps.
+// macro-step and 4 plain steps; the density deviation between the two results
+// (of the mean density, or per particle: sph_learned_set_judge) and their
+// momentum difference decide. Above the bounds the interval is rolled back and
+// run by plain SPH.
 #include <cmath>
 #include <cstring>
 #include <random>
@@ -129,6 +130,12 @@ __global__ void __launch_bounds__(kT) k_macro_integrate(const float4* __restrict
     const float* o = O + (size_t)t * M::kOS;
     M::macro_update(S, o[0] + corr[0], o[1] + corr[1], o[2] + corr[2], o[3] + corr[3], o[4] + corr[4],
                     o[5] + corr[5], pos_s[t], vel_s[t], np, nv);
+    if (S.sdf) {  // the static obstacle's rule, after the wall clamp as in the plain step
+        float x[3] = {np.x, np.y, np.z}, u[3] = {nv.x, nv.y, nv.z};
+        obstacle_response(S, x, u);
+        np = make_float4(x[0], x[1], x[2], np.w);
+        nv = make_float4(u[0], u[1], u[2], nv.w);
+    }
     pos_out[t] = np;
     vel_out[t] = nv;
     const int k = cell_key(S, np.x, np.y, np.z);
@@ -221,28 +228,32 @@ __global__ void __launch_bounds__(kT) k_lists_by_id(const float4* __restrict__ v
     rho_id[id] = rhop[s].x;
 }
 
-// FP64 partials of the judge: sum |rho_l - rho_p| / rho_p, sum (v_l - v_p) (3), sum |v_p|.
+// FP64 partials of the judge: sum |rho_l - rho_p| / rho_p, sum (v_l - v_p) (3), sum |v_p|,
+// sum rho_l, sum rho_p.
+constexpr int kCmpFields = 7;
 __global__ void __launch_bounds__(kT) k_compare(const float* __restrict__ rl, const float* __restrict__ rp,
                                                const float4* __restrict__ vl, const float4* __restrict__ vp, int n,
                                                double* __restrict__ out) {
-    __shared__ double sh[5][kT];
-    double a[5] = {0, 0, 0, 0, 0};
+    __shared__ double sh[kCmpFields][kT];
+    double a[kCmpFields] = {0, 0, 0, 0, 0, 0, 0};
     for (int i = blockIdx.x * kT + threadIdx.x; i < n; i += gridDim.x * kT) {
         a[0] += fabs((double)rl[i] - (double)rp[i]) / (double)rp[i];
         a[1] += (double)vl[i].x - (double)vp[i].x;
         a[2] += (double)vl[i].y - (double)vp[i].y;
         a[3] += (double)vl[i].z - (double)vp[i].z;
         a[4] += sqrt((double)vp[i].x * vp[i].x + (double)vp[i].y * vp[i].y + (double)vp[i].z * vp[i].z);
+        a[5] += (double)rl[i];
+        a[6] += (double)rp[i];
     }
-    for (int f = 0; f < 5; ++f) sh[f][threadIdx.x] = a[f];
+    for (int f = 0; f < kCmpFields; ++f) sh[f][threadIdx.x] = a[f];
     __syncthreads();
     for (int o = kT / 2; o > 0; o >>= 1) {
         if (threadIdx.x < o)
-            for (int f = 0; f < 5; ++f) sh[f][threadIdx.x] += sh[f][threadIdx.x + o];
+            for (int f = 0; f < kCmpFields; ++f) sh[f][threadIdx.x] += sh[f][threadIdx.x + o];
         __syncthreads();
     }
     if (threadIdx.x == 0)
-        for (int f = 0; f < 5; ++f) out[blockIdx.x * 5 + f] = sh[f][0];
+        for (int f = 0; f < kCmpFields; ++f) out[blockIdx.x * kCmpFields + f] = sh[f][0];
 }
 
 constexpr int kCmpBlocks = 256;
@@ -279,7 +290,7 @@ sph_status ensure_ctx_scratch(sph_mpnn* net, int n) {
     NCK(dal(&net->ck_pos, m)); NCK(dal(&net->ck_vel, m)); NCK(dal(&net->ck_rhop, m));
     NCK(dal(&net->l_pos, m)); NCK(dal(&net->l_vel, m)); NCK(dal(&net->l_rhop, m));
     NCK(dal(&net->acc, m)); NCK(dal(&net->accx, m)); NCK(dal(&net->rho_l, m)); NCK(dal(&net->rho_p, m));
-    NCK(dal(&net->vel_l, m)); NCK(dal(&net->vel_p, m)); NCK(dal(&net->cmp, (size_t)kCmpBlocks * 5));
+    NCK(dal(&net->vel_l, m)); NCK(dal(&net->vel_p, m)); NCK(dal(&net->cmp, (size_t)kCmpBlocks * kCmpFields));
     NCK(dal(&net->Obuf, m * M::kOS)); NCK(dal(&net->osum, (size_t)kSumBlocks * M::FO)); NCK(dal(&net->ocorr, M::FO));
     net->cap = n;
     return SPH_OK;
@@ -394,7 +405,7 @@ void restore_state(sph_ctx* ctx, const Saved& s) {
 // from that state, compared by particle id. Returns the mean relative density deviation and
 // the momentum difference; the learned result is left in (l_pos, l_vel, l_rhop) and the plain
 // one in the context.
-sph_status judge_macro(sph_ctx* ctx, sph_mpnn* net, double& dev, double& mom) {
+sph_status judge_macro(sph_ctx* ctx, sph_mpnn* net, double& dev, double& mom, double& mdev) {
     const int n = ctx->b.n;
     const Saved s0 = save_state(ctx, net->snap_pos, net->snap_vel, net->snap_rhop);
     if (!ctx->need_hash) cudaMemsetAsync(ctx->b.count, 0, sizeof(int) * (size_t)ctx->b.ncell, ctx->stream);
@@ -410,14 +421,15 @@ sph_status judge_macro(sph_ctx* ctx, sph_mpnn* net, double& dev, double& mom) {
     if (st) return st;
     k_by_id<<<nblk(n), kT, 0, ctx->stream>>>(ctx->b.vel, ctx->b.rhop, n, net->rho_p, net->vel_p);
     k_compare<<<kCmpBlocks, kT, 0, ctx->stream>>>(net->rho_l, net->rho_p, net->vel_l, net->vel_p, n, net->cmp);
-    std::vector<double> h((size_t)kCmpBlocks * 5);
+    std::vector<double> h((size_t)kCmpBlocks * kCmpFields);
     if (cudaMemcpyAsync(h.data(), net->cmp, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, ctx->stream) ||
         cudaStreamSynchronize(ctx->stream))
         return fail(ctx, SPH_ERR_CUDA, "judge readback");
-    double sum[5] = {0, 0, 0, 0, 0};
+    double sum[kCmpFields] = {0, 0, 0, 0, 0, 0, 0};
     for (int b = 0; b < kCmpBlocks; ++b)
-        for (int f = 0; f < 5; ++f) sum[f] += h[(size_t)b * 5 + f];
+        for (int f = 0; f < kCmpFields; ++f) sum[f] += h[(size_t)b * kCmpFields + f];
     dev = sum[0] / n;
+    mdev = sum[6] > 0.0 ? std::fabs(sum[5] - sum[6]) / sum[6] : INFINITY;
     const double g = std::sqrt((double)ctx->s0.g[0] * ctx->s0.g[0] + (double)ctx->s0.g[1] * ctx->s0.g[1] +
                                (double)ctx->s0.g[2] * ctx->s0.g[2]);
     mom = std::sqrt(sum[1] * sum[1] + sum[2] * sum[2] + sum[3] * sum[3]) / (sum[4] + n * g * 4.0 * ctx->s0.dt);
@@ -709,6 +721,14 @@ sph_status sph_refresh_density(sph_ctx* ctx) {
     return engine::check_device_error(ctx);
 }
 
+sph_status sph_learned_set_judge(sph_ctx* ctx, int32_t metric) {
+    if (!ctx) return SPH_ERR_INVALID_ARG;
+    if (metric != SPH_JUDGE_MEAN_DENSITY && metric != SPH_JUDGE_PARTICLE_DENSITY)
+        return fail(ctx, SPH_ERR_INVALID_ARG, "unknown judge metric");
+    ctx->judge_metric = metric;
+    return SPH_OK;
+}
+
 sph_status sph_learned_step(sph_ctx* ctx, sph_mpnn* net, int32_t n_macro, int32_t judge_every, float density_tol,
                             float momentum_tol, sph_learned_report* rep) {
     if (!ctx || !net) return SPH_ERR_INVALID_ARG;
@@ -755,15 +775,18 @@ sph_status sph_learned_step(sph_ctx* ctx, sph_mpnn* net, int32_t n_macro, int32_
             st = learned_macro(ctx, net);
             if (st) return st;
         }
-        double dev = 0.0, mom = 0.0;
-        st = judge_macro(ctx, net, dev, mom);
+        double dev = 0.0, mom = 0.0, mdev = 0.0;
+        st = judge_macro(ctx, net, dev, mom, mdev);
         if (st) return st;
         ++r.judged;
         r.last_density_dev = dev;
         r.last_momentum_dev = mom;
         r.max_density_dev = std::max(r.max_density_dev, dev);
         r.sum_density_dev += dev;
-        if (dev <= density_tol && mom <= momentum_tol) {
+        r.last_mean_rho_dev = mdev;
+        r.max_mean_rho_dev = std::max(r.max_mean_rho_dev, mdev);
+        const double crit = ctx->judge_metric == SPH_JUDGE_PARTICLE_DENSITY ? dev : mdev;
+        if (crit <= density_tol && mom <= momentum_tol) {
             copy_state(ctx, ctx->b.pos, ctx->b.vel, ctx->b.rhop, net->l_pos, net->l_vel, net->l_rhop);
             cudaMemsetAsync(ctx->b.count, 0, sizeof(int) * (size_t)ctx->b.ncell, ctx->stream);
             ctx->need_hash = true;

@@ -38,6 +38,7 @@
 // plain FP32 with contraction allowed (only the predicate is pinned bit-exact).
 // For i != j at r == 0 the pressure term is skipped (the shader's
 // normalize(0) is NaN, force_comp.glsl:59); the viscosity term is kept.
+#include <algorithm>
 #include <climits>
 #include <type_traits>
 
@@ -424,10 +425,13 @@ __global__ void __launch_bounds__(BLOCK) k_force_integrate(const float4* __restr
             pos_out[t] = make_float4(np[0], np[1], np[2], p.w);
             vel_out[t] = make_float4(nv[0], nv[1], nv[2], v.w);
             if (force_out) force_out[t] = make_float4(Fx, Fy, Fz, 0.0f);
-            // Hash of the new position: the next step's sort starts from here.
-            const int c = cell_key(S, np[0], np[1], np[2]);
-            key_out[t] = c;
-            rank_out[t] = atomicAdd(&count[c], 1);
+            // Hash of the new position: the next step's sort starts from here (with an obstacle,
+            // k_obstacle_hash hashes after moving the particles out of it).
+            if (key_out) {
+                const int c = cell_key(S, np[0], np[1], np[2]);
+                key_out[t] = c;
+                rank_out[t] = atomicAdd(&count[c], 1);
+            }
         }
         if (!tiled && threadIdx.x == 0 && stats) atomicAdd(&stats[1], 1u);
         __syncthreads();  // the next chunk reuses the tile
@@ -585,8 +589,33 @@ void force_impl(const Buffers& b, const SceneDev& s0, float4* force_out, cudaStr
     auto k = k_force_integrate<B, R, BLOCK>;
     constexpr size_t sm = force_smem<R, BLOCK>();
     k<<<grid_size(k, BLOCK, sm, b.n), BLOCK, sm, st>>>(b.pos_s, b.vel_s, b.rhop, b.start, s0, b.scenes, b.nscene,
-                                                       b.pos, b.vel, force_out, b.key, b.rank, b.count, b.n,
-                                                       b.tile_stats);
+                                                       b.pos, b.vel, force_out, s0.sdf ? nullptr : b.key, b.rank,
+                                                       b.count, b.n, b.tile_stats);
+}
+
+// The static obstacle's rule (sph_set_obstacle) on the integrated state, then the cell hash of
+// the final positions (the force kernel leaves the hash to this kernel when there is an
+// obstacle). One thread per slot.
+template <bool BATCHED>
+__global__ void __launch_bounds__(256) k_obstacle_hash(float4* __restrict__ pos, float4* __restrict__ vel, SceneDev s0,
+                                                       const SceneDev* __restrict__ scenes, int nscene,
+                                                       int* __restrict__ key_out, int* __restrict__ rank_out,
+                                                       int* __restrict__ count, int n) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const float4 p = pos[t], v = vel[t];
+        int sc = 0;
+        if constexpr (BATCHED) sc = min(max(scene_of(p), 0), nscene - 1);
+        const SceneDev& S = scene_params<BATCHED>(s0, scenes, sc);
+        float x[3] = {p.x, p.y, p.z}, u[3] = {v.x, v.y, v.z};
+        obstacle_response(S, x, u);
+        if (x[0] != p.x || x[1] != p.y || x[2] != p.z || u[0] != v.x || u[1] != v.y || u[2] != v.z) {
+            pos[t] = make_float4(x[0], x[1], x[2], p.w);
+            vel[t] = make_float4(u[0], u[1], u[2], v.w);
+        }
+        const int c = cell_key(S, x[0], x[1], x[2]);
+        key_out[t] = c;
+        rank_out[t] = atomicAdd(&count[c], 1);
+    }
 }
 
 template <bool B, int R>
@@ -653,6 +682,14 @@ void launch_force_integrate(const Buffers& b, const SceneDev& s0, bool batched, 
         dispatch(c.block, c.stencil, [&](auto R, auto BL) { force_impl<true, R.value, BL.value>(b, s0, f, st); });
     else
         dispatch(c.block, c.stencil, [&](auto R, auto BL) { force_impl<false, R.value, BL.value>(b, s0, f, st); });
+    if (s0.sdf) {
+        const int blocks = std::min((b.n + 255) / 256, device_sm_count() * 8);
+        if (batched)
+            k_obstacle_hash<true><<<blocks, 256, 0, st>>>(b.pos, b.vel, s0, b.scenes, b.nscene, b.key, b.rank, b.count,
+                                                          b.n);
+        else
+            k_obstacle_hash<false><<<blocks, 256, 0, st>>>(b.pos, b.vel, s0, b.scenes, 1, b.key, b.rank, b.count, b.n);
+    }
 }
 
 void launch_density_nb(const Buffers& b, const SceneDev& s0, bool batched, const LaunchCfg& c, int* nb, int* cnt,

@@ -18,6 +18,11 @@
 //   sph_headless [--frames N] [--keys "p@0"] [--report N] [--scene reference|dam_break]
 //                [--visc V] [--smoothing S] [--mass M] [--rest-rho R]
 //                [--render-every N] [--render-prefix P] [--size WxH]
+//                [--obstacle mesh.obj] [--obstacle-spacing S]
+// --obstacle loads a Wavefront OBJ mesh (the reference's LoadMesh, LoadMesh.cpp:16-55) and makes
+// it a static obstacle of the step: its signed distance field sampled over the box
+// (sph_sdf_from_mesh), handed to sph_set_obstacle.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -40,6 +45,8 @@ struct Options {
     int render_every = 0;
     std::string render_prefix = "frame";
     int width = 720, height = 720;  // init_window_width/height (Main.cpp:39-40)
+    std::string obstacle;           // OBJ mesh to collide with (README.md:59; meshes load in LoadMesh.cpp:16-55)
+    float obstacle_spacing = 0.0f;  // SDF sample spacing; 0: h / 2
 };
 
 bool parse(int argc, char** argv, Options& o) {
@@ -58,6 +65,8 @@ bool parse(int argc, char** argv, Options& o) {
         else if (a == "--rest-rho") o.rest_rho = (float)std::atof(next("--rest-rho"));
         else if (a == "--render-every") o.render_every = std::atoi(next("--render-every"));
         else if (a == "--render-prefix") o.render_prefix = next("--render-prefix");
+        else if (a == "--obstacle") o.obstacle = next("--obstacle");
+        else if (a == "--obstacle-spacing") o.obstacle_spacing = (float)std::atof(next("--obstacle-spacing"));
         else if (a == "--size") {
             if (std::sscanf(next("--size"), "%dx%d", &o.width, &o.height) != 2) return false;
         }
@@ -117,6 +126,37 @@ void report(sph_ctx* ctx, int frame, double ms_per_frame) {
 
 }  // namespace
 
+// The mesh of --obstacle as a static obstacle: its signed distance field sampled over the box
+// (sph_sdf_from_mesh on the GPU), handed to sph_set_obstacle.
+bool load_obstacle(sph_ctx* ctx, const Options& o, const sph_params& p) {
+    uint32_t nv = 0, nt = 0;
+    if (sph_obj_read(o.obstacle.c_str(), nullptr, &nv, nullptr, &nt) != SPH_OK || nt == 0) {
+        std::fprintf(stderr, "cannot read the mesh %s\n", o.obstacle.c_str());
+        return false;
+    }
+    std::vector<float> v(3ull * nv);
+    std::vector<uint32_t> t(3ull * nt);
+    if (sph_obj_read(o.obstacle.c_str(), v.data(), &nv, t.data(), &nt) != SPH_OK) return false;
+    const float sp = o.obstacle_spacing > 0 ? o.obstacle_spacing : 0.5f * p.smoothing_coeff * p.particle_radius;
+    int32_t dims[3];
+    float org[3];
+    size_t total = 1;
+    for (int a = 0; a < 3; ++a) {
+        org[a] = p.lower[a];
+        dims[a] = std::max(2, (int)std::ceil((p.upper[a] - p.lower[a]) / sp) + 1);
+        total *= (size_t)dims[a];
+    }
+    std::vector<float> sdf(total);
+    if (sph_sdf_from_mesh(v.data(), nv, t.data(), nt, dims, org, sp, sdf.data()) != SPH_OK ||
+        sph_set_obstacle(ctx, sdf.data(), dims, org, sp) != SPH_OK) {
+        std::fprintf(stderr, "obstacle: %s\n", sph_last_error(ctx));
+        return false;
+    }
+    std::fprintf(stderr, "obstacle %s: %u triangles, %d x %d x %d samples at %g\n", o.obstacle.c_str(), nt, dims[0],
+                 dims[1], dims[2], sp);
+    return true;
+}
+
 // The view of a scene: the reference's initial camera for its own lattice; for the dam break a
 // camera that sees its 5.12 x 1.28 x 1.28 box.
 sph_view make_view(const Options& o) {
@@ -135,7 +175,8 @@ int main(int argc, char** argv) {
     if (!parse(argc, argv, o)) {
         std::fprintf(stderr, "usage: %s [--frames N] [--keys \"p@0,r@500\"] [--report N] "
                              "[--scene reference|dam_break] [--visc V] [--smoothing S] [--mass M] [--rest-rho R] "
-                             "[--render-every N] [--render-prefix P] [--size WxH]\n",
+                             "[--render-every N] [--render-prefix P] [--size WxH] [--obstacle mesh.obj] "
+                             "[--obstacle-spacing S]\n",
                      argv[0]);
         return 2;
     }
@@ -151,6 +192,7 @@ int main(int argc, char** argv) {
         std::fprintf(stderr, "upload: %s\n", sph_last_error(ctx));
         return 1;
     }
+    if (!o.obstacle.empty() && !load_obstacle(ctx, o, p)) return 1;
     const sph_view view = make_view(o);
     std::vector<uint8_t> image(o.render_every > 0 ? (size_t)o.width * o.height * 4 : 0);
     bool simulate = false;  // Main.cpp:87: a zero-initialised global, so the simulation starts paused

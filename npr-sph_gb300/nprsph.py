@@ -27,6 +27,7 @@ PARTICLE_DTYPE = np.dtype([("pos", "<f4", 4), ("vel", "<f4", 4), ("force", "<f4"
 assert PARTICLE_DTYPE.itemsize == 64
 
 FLAG_KEEP_FORCE = 0x1
+JUDGE_MEAN_DENSITY, JUDGE_PARTICLE_DENSITY = 0, 1
 
 OK, ERR_INVALID_ARG, ERR_CUDA, ERR_OUT_OF_MEMORY, ERR_CAPACITY, ERR_NOT_READY, ERR_DEVICE, ERR_UNSUPPORTED = (
     0, -1, -2, -3, -4, -5, -6, -7)
@@ -68,7 +69,8 @@ class LearnedReport(C.Structure):
     _fields_ = [("learned_macro_steps", C.c_uint64), ("plain_macro_steps", C.c_uint64), ("judged", C.c_uint64),
                 ("fallbacks", C.c_uint64), ("last_density_dev", C.c_double), ("last_momentum_dev", C.c_double),
                 ("max_density_dev", C.c_double), ("sum_density_dev", C.c_double),
-                ("discarded_macro_steps", C.c_uint64)]
+                ("discarded_macro_steps", C.c_uint64), ("last_mean_rho_dev", C.c_double),
+                ("max_mean_rho_dev", C.c_double)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -133,6 +135,7 @@ _SIGS = {
     "sph_mpnn_train": (C.c_int32, [_P, C.c_uint32, C.c_float, C.c_uint64, _P]),
     "sph_learned_step": (C.c_int32, [_P, _P, C.c_int32, C.c_int32, C.c_float, C.c_float, C.POINTER(LearnedReport)]),
     "sph_refresh_density": (C.c_int32, [_P]),
+    "sph_learned_set_judge": (C.c_int32, [_P, C.c_int32]),
     "sph_neighbor_lists": (C.c_int32, [_P, _P, _P, _P]),
     "sph_view_default": (C.c_int32, [C.POINTER(View), C.c_int32, C.c_int32, C.c_float]),
     "sph_view_camera": (C.c_int32, [C.POINTER(View), C.c_float, C.c_float, C.POINTER(C.c_float),
@@ -154,6 +157,10 @@ _SIGS = {
                                    C.c_float, C.c_uint64]),
     "sph_scene_ball": (C.c_int32, [_P, C.c_uint32, C.POINTER(C.c_float), C.c_float, C.c_float, C.c_uint64]),
     "sph_scene_slosh": (C.c_int32, [_P, C.c_uint32, C.c_float, C.c_float, C.c_float]),
+    "sph_set_obstacle": (C.c_int32, [_P, _P, C.POINTER(C.c_int32), C.POINTER(C.c_float), C.c_float]),
+    "sph_sdf_from_mesh": (C.c_int32, [_P, C.c_uint32, _P, C.c_uint32, C.POINTER(C.c_int32), C.POINTER(C.c_float),
+                                      C.c_float, _P]),
+    "sph_obj_read": (C.c_int32, [C.c_char_p, _P, C.POINTER(C.c_uint32), _P, C.POINTER(C.c_uint32)]),
 }
 
 
@@ -373,6 +380,16 @@ class Sim:
         """sph_render into a device buffer of width * height * 4 bytes."""
         _check(lib.sph_render(self._ctx, C.byref(view), int(scene), C.c_void_p(dev_ptr), 1), self._ctx)
 
+    def set_obstacle(self, sdf: np.ndarray | None, origin=(0.0, 0.0, 0.0), spacing: float = 1.0) -> None:
+        """Static obstacle from signed distance samples sdf[z, y, x] (sph_set_obstacle); None removes it."""
+        if sdf is None:
+            _check(lib.sph_set_obstacle(self._ctx, None, None, None, C.c_float(0.0)), self._ctx)
+            return
+        a = np.ascontiguousarray(sdf, dtype=np.float32)
+        assert a.ndim == 3
+        dims = (C.c_int32 * 3)(a.shape[2], a.shape[1], a.shape[0])
+        _check(lib.sph_set_obstacle(self._ctx, a.ctypes.data, dims, _f3(origin), C.c_float(spacing)), self._ctx)
+
     def save(self, path, seed: int = 0) -> None:
         """Write a snapshot file (sph_snapshot_save)."""
         _check(lib.sph_snapshot_save(self._ctx, str(path).encode(), int(seed)), self._ctx)
@@ -494,6 +511,10 @@ class Sim:
         """rho and pres at the current positions (sph_refresh_density)."""
         _check(lib.sph_refresh_density(self._ctx), self._ctx)
 
+    def set_judge(self, metric: int) -> None:
+        """Density deviation of the learned step's judge: JUDGE_MEAN_DENSITY or JUDGE_PARTICLE_DENSITY."""
+        _check(lib.sph_learned_set_judge(self._ctx, metric), self._ctx)
+
     def learned_step(self, net: "Net", n_macro: int, judge_every: int = 8, density_tol: float = 0.01,
                      momentum_tol: float = 0.01) -> LearnedReport:
         rep = LearnedReport()
@@ -614,6 +635,66 @@ def scene_slosh(a: np.ndarray, amplitude: float, x0: float, length: float) -> np
     _check(lib.sph_scene_slosh(_ptr(a), len(a), C.c_float(amplitude), C.c_float(x0), C.c_float(length)),
            what="sph_scene_slosh")
     return a
+
+
+def sdf_from_mesh(verts: np.ndarray, tris: np.ndarray, dims, origin, spacing: float) -> np.ndarray:
+    """Signed distance samples [z, y, x] of a closed triangle mesh on a grid (sph_sdf_from_mesh, GPU)."""
+    v = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 3)
+    t = np.ascontiguousarray(tris, dtype=np.uint32).reshape(-1, 3)
+    nx, ny, nz = (int(d) for d in dims)
+    out = np.zeros((nz, ny, nx), dtype=np.float32)
+    _check(lib.sph_sdf_from_mesh(v.ctypes.data, len(v), t.ctypes.data, len(t), (C.c_int32 * 3)(nx, ny, nz),
+                                 _f3(origin), C.c_float(spacing), out.ctypes.data), what="sph_sdf_from_mesh")
+    return out
+
+
+def obj_read(path) -> tuple[np.ndarray, np.ndarray]:
+    """Vertices (n, 3) float32 and triangles (m, 3) uint32 of a Wavefront OBJ file (sph_obj_read)."""
+    nv, nt = C.c_uint32(0), C.c_uint32(0)
+    _check(lib.sph_obj_read(str(path).encode(), None, C.byref(nv), None, C.byref(nt)), what="sph_obj_read")
+    v = np.zeros((nv.value, 3), dtype=np.float32)
+    t = np.zeros((nt.value, 3), dtype=np.uint32)
+    _check(lib.sph_obj_read(str(path).encode(), v.ctypes.data, C.byref(nv), t.ctypes.data, C.byref(nt)),
+           what="sph_obj_read")
+    return v, t
+
+
+def icosphere(radius: float = 1.0, center=(0.0, 0.0, 0.0), subdivisions: int = 2) -> tuple[np.ndarray, np.ndarray]:
+    """A closed triangle mesh of a sphere (an icosahedron with each face split in 4, `subdivisions`
+    times, vertices pushed onto the sphere), counter-clockwise seen from outside."""
+    t = (1.0 + 5 ** 0.5) / 2.0
+    v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+         (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    f = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2), (10, 7, 6),
+         (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10),
+         (8, 6, 7), (9, 8, 1)]
+    verts = [np.array(p, dtype=np.float64) / np.linalg.norm(p) for p in v]
+    for _ in range(subdivisions):
+        mid: dict = {}
+
+        def midpoint(a: int, b: int) -> int:
+            key = (min(a, b), max(a, b))
+            if key not in mid:
+                m = verts[a] + verts[b]
+                verts.append(m / np.linalg.norm(m))
+                mid[key] = len(verts) - 1
+            return mid[key]
+
+        nf = []
+        for a, b, c in f:
+            ab, bc, ca = midpoint(a, b), midpoint(b, c), midpoint(c, a)
+            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        f = nf
+    return (radius * np.array(verts) + np.asarray(center, dtype=np.float64)).astype(np.float32), \
+        np.array(f, dtype=np.uint32)
+
+
+def write_obj(path, verts: np.ndarray, tris: np.ndarray) -> None:
+    with open(path, "w") as fh:
+        for x, y, z in verts:
+            fh.write(f"v {x:.9g} {y:.9g} {z:.9g}\n")
+        for a, b, c in tris:
+            fh.write(f"f {a + 1} {b + 1} {c + 1}\n")
 
 
 def workload_params(gravity_y: float = -9.81, dt: float = 1e-4, lower=None, upper=None, k=None, mu=None,

@@ -55,6 +55,8 @@ def lib() -> C.CDLL:
         L.oracle_step_f32_aos.argtypes = [_P, _P, _I64, C.c_int, C.c_int, C.c_int, C.c_int]
         L.oracle_neighbors.restype = C.c_int
         L.oracle_neighbors.argtypes = [_P, _I64, _P, _I64, _P, C.c_int, C.c_int, _P, _P]
+        L.oracle_obstacle_f64.restype = C.c_int
+        L.oracle_obstacle_f64.argtypes = [_P, _P, _P, _P, C.c_double, _I64, _P, _P, _P]
         L.oracle_neighbor_lists.restype = C.c_int64
         L.oracle_neighbor_lists.argtypes = [_P, _I64, _P, C.c_int, _P, _P, _I64]
         L.oracle_cutoff_d2.restype = C.c_float
@@ -210,3 +212,67 @@ def render(view, pos4: np.ndarray) -> np.ndarray:
     rc = lib().oracle_render(C.addressof(view), pos4.ctypes.data, len(pos4), out.ctypes.data)
     assert rc == 0
     return out
+
+
+def obstacle_f64(params, sdf: np.ndarray, origin, spacing: float, pos: np.ndarray, vel: np.ndarray):
+    """The obstacle rule (FP64) on copies of pos/vel (n x 3) that already went through the wall
+    clamp; sdf[z, y, x] as given to sph_set_obstacle. Returns (pos, vel, phi at the input)."""
+    a = np.ascontiguousarray(sdf, dtype=np.float32)
+    dims = np.array([a.shape[2], a.shape[1], a.shape[0]], dtype=np.int32)
+    org = np.ascontiguousarray(origin, dtype=np.float64)
+    x = np.array(pos, dtype=np.float64, order="C")
+    v = np.array(vel, dtype=np.float64, order="C")
+    phi = np.zeros(len(x))
+    rc = lib().oracle_obstacle_f64(_pp(params), a.ctypes.data, dims.ctypes.data, org.ctypes.data, float(spacing),
+                                   len(x), x.ctypes.data, v.ctypes.data, phi.ctypes.data)
+    assert rc == 0
+    return x, v, phi
+
+
+def _tri_dist2(p: np.ndarray, a: np.ndarray, b: np.ndarray, c: np.ndarray) -> np.ndarray:
+    """Squared distance from points p (m x 3) to triangle (a, b, c): the closest point by Voronoi
+    region (Ericson, Real-Time Collision Detection, 2005, section 5.1.5), vectorised over p."""
+    ab, ac = b - a, c - a
+    ap, bp, cp = p - a, p - b, p - c
+    d1, d2 = ap @ ab, ap @ ac
+    d3, d4 = bp @ ab, bp @ ac
+    d5, d6 = cp @ ab, cp @ ac
+    va, vb, vc = d3 * d6 - d5 * d4, d5 * d2 - d1 * d6, d1 * d4 - d3 * d2
+    with np.errstate(divide="ignore", invalid="ignore"):
+        den = va + vb + vc
+        q = a + np.outer(vb / den, ab) + np.outer(vc / den, ac)                              # face
+        e_bc = (va <= 0) & (d4 - d3 >= 0) & (d5 - d6 >= 0)
+        q = np.where(e_bc[:, None], b + np.outer((d4 - d3) / ((d4 - d3) + (d5 - d6)), c - b), q)
+        e_ac = (vb <= 0) & (d2 >= 0) & (d6 <= 0)
+        q = np.where(e_ac[:, None], a + np.outer(d2 / (d2 - d6), ac), q)
+        v_c = (d6 >= 0) & (d5 <= d6)
+        q = np.where(v_c[:, None], c, q)
+        e_ab = (vc <= 0) & (d1 >= 0) & (d3 <= 0)
+        q = np.where(e_ab[:, None], a + np.outer(d1 / (d1 - d3), ab), q)
+        v_b = (d3 >= 0) & (d4 <= d3)
+        q = np.where(v_b[:, None], b, q)
+        v_a = (d1 <= 0) & (d2 <= 0)
+        q = np.where(v_a[:, None], a, q)
+    d = p - q
+    return np.einsum("ij,ij->i", d, d)
+
+
+def mesh_sdf(verts: np.ndarray, tris: np.ndarray, points: np.ndarray) -> np.ndarray:
+    """FP64 signed distance of points (m x 3) to a closed triangle mesh: the distance to the
+    nearest triangle, negative where the winding number (sum of solid angles by Van Oosterom
+    and Strackee's formula, over 4 pi) exceeds 1/2. The restatement of sph_sdf_from_mesh."""
+    v = np.asarray(verts, dtype=np.float64)
+    p = np.asarray(points, dtype=np.float64)
+    best = np.full(len(p), np.inf)
+    omega = np.zeros(len(p))
+    for ia, ib, ic in np.asarray(tris, dtype=np.int64):
+        a, b, c = v[ia], v[ib], v[ic]
+        best = np.minimum(best, _tri_dist2(p, a, b, c))
+        x, y, z = a - p, b - p, c - p
+        lx, ly, lz = (np.linalg.norm(t, axis=1) for t in (x, y, z))
+        num = np.einsum("ij,ij->i", x, np.cross(y, z))
+        den = lx * ly * lz + np.einsum("ij,ij->i", x, y) * lz + np.einsum("ij,ij->i", x, z) * ly + \
+            np.einsum("ij,ij->i", y, z) * lx
+        omega += 2.0 * np.arctan2(num, den)
+    d = np.sqrt(best)
+    return np.where(omega / (4.0 * np.pi) > 0.5, -d, d)

@@ -451,6 +451,66 @@ int64_t oracle_neighbor_lists(const sph_params* P, int64_t n, const float* pos4,
     return total;
 }
 
+// Static obstacle rule of the library (sph_set_obstacle; no reference counterpart), in FP64,
+// applied to states that already went through the wall clamp: phi = trilinear interpolation of
+// the samples (sample (i, j, k) at origin + spacing (i, j, k), x fastest; none outside the
+// sampled box); where phi < 0: x -= phi n, n = g / |g| with g the trilinear interpolant of the
+// samples' central-difference gradients;
+// v -= (1 + damping)(v.n) n if v.n < 0; then x is clamped into [lower, upper]. phi_out[i]
+// receives phi at the input position (NaN outside the sampled box).
+int oracle_obstacle_f64(const sph_params* P, const float* sdf, const int32_t* dims, const double* origin,
+                        double spacing, int64_t n, double* pos, double* vel, double* phi_out) {
+    if (!P || !sdf || !dims || !origin || !pos || !vel || !(spacing > 0.0)) return -1;
+    const double inv = 1.0 / spacing, damp = P->damping;
+    const int64_t sy = dims[0], sz = (int64_t)dims[0] * dims[1];
+    for (int64_t q = 0; q < n; ++q) {
+        double* x = pos + 3 * q;
+        double* v = vel + 3 * q;
+        const double u[3] = {(x[0] - origin[0]) * inv, (x[1] - origin[1]) * inv, (x[2] - origin[2]) * inv};
+        bool in = true;
+        for (int a = 0; a < 3; ++a) in = in && u[a] >= 0.0 && u[a] <= (double)(dims[a] - 1);
+        if (phi_out) phi_out[q] = NAN;
+        if (!in) continue;
+        int c[3];
+        double t[3];
+        for (int a = 0; a < 3; ++a) {
+            c[a] = std::min((int)std::floor(u[a]), dims[a] - 2);
+            t[a] = u[a] - c[a];
+        }
+        auto S = [&](const int* q) { return (double)sdf[q[2] * sz + q[1] * sy + q[0]]; };
+        // phi: the trilinear interpolant; g: the trilinear interpolant of the samples'
+        // central-difference gradients (one-sided on the grid's faces)
+        double phi = 0.0, g[3] = {0.0, 0.0, 0.0};
+        for (int corner = 0; corner < 8; ++corner) {
+            const int o[3] = {corner & 1, (corner >> 1) & 1, (corner >> 2) & 1};
+            int q[3];
+            double w = 1.0;
+            for (int a = 0; a < 3; ++a) {
+                w *= o[a] ? t[a] : 1.0 - t[a];
+                q[a] = c[a] + o[a];
+            }
+            phi += w * S(q);
+            for (int a = 0; a < 3; ++a) {
+                int qh[3] = {q[0], q[1], q[2]}, ql[3] = {q[0], q[1], q[2]};
+                qh[a] = std::min(q[a] + 1, dims[a] - 1);
+                ql[a] = std::max(q[a] - 1, 0);
+                g[a] += w * (S(qh) - S(ql)) / (double)(qh[a] - ql[a]) * inv;
+            }
+        }
+        if (phi_out) phi_out[q] = phi;
+        const double gl = std::sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+        if (!(phi < 0.0) || !(gl > 0.0)) continue;
+        const double nrm[3] = {g[0] / gl, g[1] / gl, g[2] / gl};
+        const double vn = v[0] * nrm[0] + v[1] * nrm[1] + v[2] * nrm[2];
+        for (int a = 0; a < 3; ++a) {
+            x[a] -= phi * nrm[a];
+            if (vn < 0.0) v[a] -= (1.0 + damp) * vn * nrm[a];
+            x[a] = std::min(std::max(x[a], (double)P->lower[a]), (double)P->upper[a]);
+        }
+    }
+    return 0;
+}
+
 int oracle_max_threads(void) { return omp_get_max_threads(); }
 
 }  // extern "C"

@@ -185,3 +185,30 @@ def test_learned_run_stays_finite(sph, trained):
     assert d.nonfinite == 0
     lo, hi = np.array(sc.params.lower[:3]), np.array(sc.params.upper[:3])
     assert np.all(out["pos"][:, :3] >= lo) and np.all(out["pos"][:, :3] <= hi)
+
+
+def test_judge_metric_selects_the_density_deviation(sph, trained):
+    """Both density deviations of a judged macro-step are reported and the selected one
+    decides. The deviation of the mean density is far below the mean per-particle deviation,
+    so a tolerance between the two keeps the learned interval under JUDGE_MEAN_DENSITY (the
+    default) and rolls it back under JUDGE_PARTICLE_DENSITY."""
+    net, _ = trained
+    sc = sph.dam_break(16, 32, 32, seed=24)
+    out = {}
+    with sph.Sim(sc.params, n_max=len(sc.particles)) as sim:
+        sim.upload(sc.particles)
+        sim.step(8)
+        start = sim.download()
+        probe = sim.learned_step(net, 1, 1, 1e30, 1e30)
+        assert probe.judged == 1 and probe.learned_macro_steps == 1
+        assert 0.0 <= probe.last_mean_rho_dev < 0.5 * probe.last_density_dev
+        tol = 0.5 * (probe.last_mean_rho_dev + probe.last_density_dev)
+        for metric in (sph.JUDGE_MEAN_DENSITY, sph.JUDGE_PARTICLE_DENSITY):
+            sim.upload(start)
+            sim.set_judge(metric)
+            out[metric] = sim.learned_step(net, 1, 1, tol, 1e30)
+        with pytest.raises(sph.SphError):
+            sim.set_judge(7)
+    mean, part = out[sph.JUDGE_MEAN_DENSITY], out[sph.JUDGE_PARTICLE_DENSITY]
+    assert (mean.learned_macro_steps, mean.fallbacks) == (1, 0)
+    assert (part.learned_macro_steps, part.fallbacks) == (0, 1)

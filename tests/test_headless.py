@@ -55,3 +55,20 @@ def test_render_frames_to_ppm(gpu, tmp_path):
         data = (tmp_path / f"f_{k:05d}.ppm").read_bytes()
         assert data.startswith(b"P6\n320 240\n255\n")
         assert len(data) == len(b"P6\n320 240\n255\n") + 320 * 240 * 3
+
+
+@pytest.mark.gpu
+def test_obstacle_mesh(sph, gpu, tmp_path):
+    """--obstacle: an icosphere OBJ through the reference's lattice becomes a static obstacle (the
+    particles inside it are moved out in the first step); the run stays finite and its state
+    differs from the same run without the mesh."""
+    v, t = sph.icosphere(0.03, (0.02, 0.25, 0.02), 2)
+    sph.write_obj(tmp_path / "ball.obj", v, t)
+    a = run("--frames", "30", "--keys", "p@0", "--report", "30", "--obstacle", str(tmp_path / "ball.obj"))
+    b = run("--frames", "30", "--keys", "p@0", "--report", "30")
+    assert a.returncode == 0 and b.returncode == 0, (a.stderr, b.stderr)
+    assert "320 triangles" in a.stderr
+    la, lb = json.loads(a.stdout.splitlines()[-1]), json.loads(b.stdout.splitlines()[-1])
+    assert la["nonfinite"] == 0 and la["steps"] == 30
+    assert la["kinetic_energy"] != lb["kinetic_energy"]
+    assert run("--obstacle", str(tmp_path / "missing.obj"), "--frames", "1").returncode == 1
