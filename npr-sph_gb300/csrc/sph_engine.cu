@@ -166,7 +166,6 @@ sph_status rebuild_geometry(sph_ctx* ctx) {
         CK(dalloc(&ctx->b.start, (size_t)cap + 1));
         CK(dalloc(&ctx->b.scan_state, (size_t)tiles));
         CK(cudaMemsetAsync(ctx->b.scan_state, 0, sizeof(unsigned long long) * tiles, ctx->stream));
-        CK(cudaMemsetAsync(ctx->b.scan_ticket, 0, sizeof(int) * 2, ctx->stream));
         ctx->cell_cap = cap;
         ctx->tile_cap = tiles;
     }
@@ -222,7 +221,7 @@ sph_status check_device_error(sph_ctx* ctx) {
     if (e) {
         CK(cudaMemsetAsync(ctx->b.err, 0, sizeof(uint32_t), ctx->stream));
         char buf[128];
-        std::snprintf(buf, sizeof(buf), "device error word 0x%x (1: scan look-back timeout, 4: slot out of range)", e);
+        std::snprintf(buf, sizeof(buf), "device error word 0x%x (2: cell key out of range, 4: slot out of range)", e);
         return fail(ctx, SPH_ERR_DEVICE, buf);
     }
     return SPH_OK;
@@ -298,13 +297,12 @@ sph_status create_impl(const sph_params* params, const uint32_t* counts, uint32_
     if (dalloc(&b.pos, n) || dalloc(&b.vel, n) || dalloc(&b.pos_s, n) || dalloc(&b.vel_s, n) ||
         dalloc(&b.rhop, n) || dalloc(&b.force_s, n) || dalloc(&b.force_up, n) || dalloc(&b.aux, n) ||
         dalloc(&b.key, n) || dalloc(&b.rank, n) || dalloc(&b.perm, n) || dalloc(&b.slot_of_id, n) ||
-        dalloc(&b.err, 1) || dalloc(&b.scan_ticket, 2) || dalloc(&b.scenes, nscene) || dalloc(&b.tile_stats, 2) ||
+        dalloc(&b.err, 1) || dalloc(&b.scenes, nscene) || dalloc(&b.tile_stats, 2) ||
         dalloc(&b.partials, reduce_partials_doubles((int)nscene)) ||
         dalloc(&ctx->diag_dev, (size_t)nscene * kDiagFields) || dalloc(&ctx->scene_first_dev, nscene + 1))
         return bail(SPH_ERR_OUT_OF_MEMORY);
     if (cudaMemsetAsync(b.err, 0, sizeof(uint32_t), ctx->stream) ||
-        cudaMemsetAsync(b.tile_stats, 0, sizeof(uint32_t) * 2, ctx->stream) ||
-        cudaMemsetAsync(b.scan_ticket, 0, sizeof(int) * 2, ctx->stream))
+        cudaMemsetAsync(b.tile_stats, 0, sizeof(uint32_t) * 2, ctx->stream))
         return bail(SPH_ERR_CUDA);
     for (auto& e : ctx->ev)
         if (cudaEventCreate(&e) != cudaSuccess) return bail(SPH_ERR_CUDA);
@@ -440,7 +438,7 @@ sph_status sph_destroy(sph_ctx* ctx) {
     free_graph(ctx);
     Buffers& b = ctx->b;
     void* ptrs[] = {b.pos, b.vel, b.pos_s, b.vel_s, b.rhop, b.force_s, b.force_up, b.aux, b.aos, b.key, b.rank,
-                    b.perm, b.count, b.start, b.scan_state, b.scan_ticket, b.slot_of_id, b.err, b.partials,
+                    b.perm, b.count, b.start, b.scan_state, b.slot_of_id, b.err, b.partials,
                     b.scenes, b.tile_stats, ctx->diag_dev, ctx->scene_first_dev, ctx->q_ids, ctx->q_cnt, ctx->q_dig,
                     ctx->render_buf, ctx->sdf_dev};
     for (void* p : ptrs)

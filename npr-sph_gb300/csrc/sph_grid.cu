@@ -6,8 +6,8 @@
 //   hash     key = linearised cell of pos, rank = atomicAdd(count[key], 1)
 //            (fused into the integrate epilogue of the previous step; this
 //            kernel only runs after an upload or a neighbour query)
-//   scan     start = exclusive prefix sum of count (single pass, decoupled
-//            look-back); zeroes count for the next step
+//   scan     start = exclusive prefix sum of count (tile sums, then each tile
+//            adds the sums before it); zeroes count for the next step
 //   scatter  perm[start[key] + rank] = s
 //   gather   stable: within a cell, particles keep their previous slot order,
 //            so the sort is deterministic; copies pos/vel into sorted order.
@@ -43,134 +43,97 @@ __global__ void __launch_bounds__(kThreads) k_hash(const float4* __restrict__ po
     }
 }
 
-// Tile descriptor of the single-pass scan: [flag:2][unused:30][value:32].
-constexpr unsigned long long kFlagAgg = 1ull << 62;     // tile aggregate available
-constexpr unsigned long long kFlagPrefix = 2ull << 62;  // inclusive prefix available
-constexpr int kSpinLimit = 1 << 20;
-
-__device__ __forceinline__ unsigned long long ld_volatile(const unsigned long long* p) {
-    return *reinterpret_cast<const volatile unsigned long long*>(p);
-}
-__device__ __forceinline__ void st_volatile(unsigned long long* p, unsigned long long v) {
-    *reinterpret_cast<volatile unsigned long long*>(p) = v;
-}
-
-// Exclusive scan of count[0, ncell) into start[0, ncell], start[ncell] = total,
-// count zeroed on the way. Tiles are claimed in order from a ticket, so every
-// predecessor of a tile is already running: the look-back always makes
-// progress. Its spin is still bounded: on timeout the tile raises
-// ERR_SCAN_SPIN and goes on with a wrong prefix, which later kernels clamp.
-// The last tile to finish resets the descriptors and the ticket.
-__global__ void __launch_bounds__(kScanThreads) k_scan(int* __restrict__ count, int* __restrict__ start,
-                                                       int ncell, unsigned long long* state, int* ticket,
-                                                       uint32_t* err) {
-    __shared__ int s_tile, s_prefix, s_last;
-    __shared__ int s_warp[kScanThreads / 32];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (threadIdx.x == 0) s_tile = atomicAdd(&ticket[0], 1);
-    __syncthreads();
-    const int tile = s_tile;
-    const int ntiles = (ncell + kScanTile - 1) / kScanTile;
-    const long long base = (long long)tile * kScanTile + (long long)threadIdx.x * kScanItems;
-
-    int v[kScanItems];
-    int sum = 0;
+// Exclusive scan of count[0, ncell) into start[0, ncell], start[ncell] = total, count
+// zeroed on the way, in two launches over tiles of kScanTile cells (tile = blockIdx.x):
+//   k_scan_tiles  the sum of each tile's counts -> tile_sum[tile]
+//   k_scan_apply  each tile adds up the sums of the tiles before it (at most a few thousand
+//                 ints, read by the whole CTA), scans its own counts and writes start.
+// No tile waits for another, so nothing can spin; the counts are read twice, the second
+// time from L2 (4 bytes per cell).
+__device__ __forceinline__ void load_tile_counts(const int* __restrict__ count, long long base, int ncell,
+                                                 int (&v)[kScanItems]) {
     if (base + kScanItems <= ncell && ((base & 3) == 0)) {
         const int4* c4 = reinterpret_cast<const int4*>(count + base);
 #pragma unroll
         for (int k = 0; k < kScanItems / 4; ++k) {
-            int4 q = c4[k];
+            const int4 q = c4[k];
             v[4 * k] = q.x; v[4 * k + 1] = q.y; v[4 * k + 2] = q.z; v[4 * k + 3] = q.w;
         }
+    } else {
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) v[k] = base + k < ncell ? count[base + k] : 0;
+    }
+}
+
+// Block-wide sum of one int per thread (every thread gets the total).
+__device__ __forceinline__ int block_sum(int x, int* s_warp) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) s_warp[warp] = x;
+    __syncthreads();
+    int t = 0;
+#pragma unroll
+    for (int w = 0; w < kScanThreads / 32; ++w) t += s_warp[w];
+    __syncthreads();
+    return t;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const int* __restrict__ count, int ncell,
+                                                             int* __restrict__ tile_sum) {
+    __shared__ int s_warp[kScanThreads / 32];
+    const long long base = (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanItems;
+    int v[kScanItems];
+    load_tile_counts(count, base, ncell, v);
+    int sum = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) sum += v[k];
+    const int total = block_sum(sum, s_warp);
+    if (threadIdx.x == 0) tile_sum[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_apply(int* __restrict__ count, int* __restrict__ start, int ncell,
+                                                             const int* __restrict__ tile_sum) {
+    __shared__ int s_warp[kScanThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int tile = blockIdx.x;
+    int before = 0;
+    for (int t = threadIdx.x; t < tile; t += kScanThreads) before += tile_sum[t];
+    const int prefix = block_sum(before, s_warp);
+    const long long base = (long long)tile * kScanTile + (long long)threadIdx.x * kScanItems;
+    int v[kScanItems];
+    load_tile_counts(count, base, ncell, v);
+    if (base + kScanItems <= ncell && ((base & 3) == 0)) {
         int4* z4 = reinterpret_cast<int4*>(count + base);
 #pragma unroll
         for (int k = 0; k < kScanItems / 4; ++k) z4[k] = make_int4(0, 0, 0, 0);
     } else {
 #pragma unroll
-        for (int k = 0; k < kScanItems; ++k) {
-            long long idx = base + k;
-            v[k] = idx < ncell ? count[idx] : 0;
-            if (idx < ncell) count[idx] = 0;
-        }
+        for (int k = 0; k < kScanItems; ++k)
+            if (base + k < ncell) count[base + k] = 0;
     }
+    int sum = 0;
 #pragma unroll
     for (int k = 0; k < kScanItems; ++k) sum += v[k];
-
-    // Block-wide exclusive scan of the per-thread sums.
+    // block-wide exclusive scan of the per-thread sums
     int incl = sum;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        int t = __shfl_up_sync(0xffffffffu, incl, o);
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= o) incl += t;
     }
     if (lane == 31) s_warp[warp] = incl;
     __syncthreads();
-    if (warp == 0) {
-        int w = lane < kScanThreads / 32 ? s_warp[lane] : 0;
+    int warp_excl = 0;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            int t = __shfl_up_sync(0xffffffffu, w, o);
-            if (lane >= o) w += t;
-        }
-        if (lane < kScanThreads / 32) s_warp[lane] = w;  // inclusive warp totals
-    }
-    __syncthreads();
-    const int warp_excl = warp > 0 ? s_warp[warp - 1] : 0;
-    const int tile_total = s_warp[kScanThreads / 32 - 1];
-    const int thread_excl = warp_excl + incl - sum;
-
-    // Look-back by warp 0: each probe reads the 32 nearest predecessors at once and
-    // sums back to the nearest one whose inclusive prefix is published.
-    if (warp == 0) {
-        int excl = 0;
-        if (tile == 0) {
-            if (lane == 0) st_volatile(&state[0], kFlagPrefix | (unsigned)tile_total);
-        } else {
-            if (lane == 0) st_volatile(&state[tile], kFlagAgg | (unsigned)tile_total);
-            for (int t = tile - 1;; t -= 32) {
-                const int idx = t - lane;  // lane 0 = nearest predecessor
-                unsigned long long d = idx >= 0 ? ld_volatile(&state[idx]) : kFlagPrefix;
-                int spins = 0;
-                while (true) {
-                    const bool missing = (d >> 62) == 0;
-                    if (!__any_sync(0xffffffffu, missing) || ++spins > kSpinLimit) break;
-                    if (missing) {
-                        __nanosleep(64);
-                        d = ld_volatile(&state[idx]);
-                    }
-                }
-                if (__any_sync(0xffffffffu, (d >> 62) == 0)) {  // gave up: flag it, go on with what we have
-                    if (lane == 0) raise_err(err, ERR_SCAN_SPIN);
-                    break;
-                }
-                const unsigned pmask = __ballot_sync(0xffffffffu, (d >> 62) == 2);
-                const int first_p = pmask ? __ffs(pmask) - 1 : 32;
-                int val = lane <= first_p ? (int)(unsigned)(d & 0xffffffffull) : 0;
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
-                excl += val;
-                if (pmask) break;
-            }
-            if (lane == 0) st_volatile(&state[tile], kFlagPrefix | (unsigned)(excl + tile_total));
-        }
-        if (lane == 0) {
-            s_prefix = excl;
-            __threadfence();
-            s_last = (atomicAdd(&ticket[1], 1) == ntiles - 1);
-        }
-    }
-    __syncthreads();
-    int run = s_prefix + thread_excl;
+    for (int w = 0; w < kScanThreads / 32; ++w) warp_excl += w < warp ? s_warp[w] : 0;
+    int run = prefix + warp_excl + incl - sum;
 #pragma unroll
     for (int k = 0; k < kScanItems; ++k) {
-        long long idx = base + k;
+        const long long idx = base + k;
         if (idx < ncell) start[idx] = run;
         run += v[k];
         if (idx == ncell - 1) start[ncell] = run;
-    }
-    if (s_last) {  // every tile has finished its look-back: reset for the next scan
-        for (int t = threadIdx.x; t < ntiles; t += blockDim.x) state[t] = 0ull;
-        if (threadIdx.x == 0) { ticket[0] = 0; ticket[1] = 0; }
     }
 }
 
@@ -341,8 +304,10 @@ void launch_hash(const Buffers& b, const SceneDev& s0, bool batched, cudaStream_
 }
 
 void launch_scan(const Buffers& b, cudaStream_t st) {
-    int ntiles = (b.ncell + kScanTile - 1) / kScanTile;
-    k_scan<<<ntiles, kScanThreads, 0, st>>>(b.count, b.start, b.ncell, b.scan_state, b.scan_ticket, b.err);
+    const int ntiles = (b.ncell + kScanTile - 1) / kScanTile;
+    int* tile_sum = reinterpret_cast<int*>(b.scan_state);  // ntiles 8-byte slots, used as ints
+    k_scan_tiles<<<ntiles, kScanThreads, 0, st>>>(b.count, b.ncell, tile_sum);
+    k_scan_apply<<<ntiles, kScanThreads, 0, st>>>(b.count, b.start, b.ncell, tile_sum);
 }
 
 void launch_scatter(const Buffers& b, cudaStream_t st) {

@@ -11,7 +11,6 @@ namespace sphgb {
 
 // Error bits of the device error word (ORed by kernels, read by the host).
 enum : uint32_t {
-    ERR_SCAN_SPIN = 1u << 0,   // a scan tile gave up waiting for its predecessor
     ERR_BAD_CELL = 1u << 1,    // a cell key fell outside its scene's cell range
     ERR_BAD_SLOT = 1u << 2,    // a slot/rank outside [0, n)
 };
@@ -66,8 +65,7 @@ struct Buffers {
     int* perm = nullptr;       // sorted slot -> state slot (before stabilising)
     int* count = nullptr;      // particles per cell (zero between steps)
     int* start = nullptr;      // first sorted slot of each cell; start[ncell] = n
-    unsigned long long* scan_state = nullptr;  // decoupled look-back tile descriptors
-    int* scan_ticket = nullptr;                // dynamic tile counter
+    unsigned long long* scan_state = nullptr;  // per-tile sums of the scan (one 8-byte slot per tile)
     int* slot_of_id = nullptr; // id -> sorted slot (neighbour queries)
     uint32_t* err = nullptr;   // device error word
     double* partials = nullptr;// reduction partials

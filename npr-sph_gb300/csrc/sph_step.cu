@@ -50,11 +50,13 @@ namespace {
 
 // BLOCK threads per CTA = target particles per chunk (128 or 256, autotuned).
 // A chunk stages about (2R+1)^2 * (BLOCK + 2R * cell occupancy * rows in the chunk)
-// candidates: ~9.7 * BLOCK for a lattice at 0.5h spacing; 16 * BLOCK leaves room for
-// compression and for chunks that straddle rows.
+// candidates: at most 9.6 * BLOCK (mean 9.4) over the chunks of the 1M dam break's 0.5h
+// lattice, its densest state. 12 * BLOCK leaves room for compression and for chunks that
+// straddle rows, and keeps the tiles small enough for 9 density / 5 force CTAs of 128 per SM;
+// a chunk that needs more takes the global-memory path.
 // With R = 2 (cells of h/2, 25 neighbour rows) a chunk stages ~26 * BLOCK.
-template <int R, int BLOCK> constexpr int stage_cap() { return (R == 1 ? 16 : 30) * BLOCK; }
-constexpr int kNbCapForce = 64;         // force list entries per thread (staged index, u16)
+template <int R, int BLOCK> constexpr int stage_cap() { return (R == 1 ? 12 : 30) * BLOCK; }
+constexpr int kNbCapForce = 48;         // force list entries per thread (staged index, u16)
 constexpr float kSentinel = 1e30f;      // staged padding: its distance to any particle is +inf
 
 template <int R>
