@@ -29,7 +29,7 @@ constexpr int kMaxDevices = 64;
 // row it later reads, so nothing has to be cleared between calls. All calls
 // share it: calls whose kernels overlap on the GPU (on different streams
 // without ordering between them) race on it.
-__device__ __align__(256) double g_noalloc_partials[kNoAllocMaxBlocks * kDiagFields];
+static __device__ __align__(256) double g_noalloc_partials[kNoAllocMaxBlocks * kDiagFields];
 
 // Device address of g_noalloc_partials, looked up once per device. In host
 // code the array's name is only a host-side stand-in, not a device address.

@@ -162,3 +162,34 @@ def test_set_obstacle_arguments_and_removal(sph, gpu):
         b.step(7)
         assert np.array_equal(a.download()["pos"], b.download()["pos"])
     assert not np.array_equal(sa["pos"], sb["pos"])  # the obstacle did act
+
+
+def test_obstacle_in_a_batch(sph, gpu):
+    """In a batch the obstacle applies to every scene in its own coordinates: after one step two
+    identical scenes match each other and the same scene stepped alone with the obstacle up to
+    FP32 rounding (a batch places row segments at other shared-memory offsets, so the packed
+    density lanes differ; see test_batched_matches_single_scenes), and after six steps no
+    particle of either scene is inside the sphere."""
+    p = sph.workload_params(lower=(0.0, 0.0, 0.0), upper=(0.3, 0.3, 0.3))
+    parts = sph.scene_fill(3000, (0.05, 0.05, 0.05), (0.25, 0.2, 0.25), 0.5 * p.h, 0.01 * p.h, 9)
+    sdf = sphere_sdf(16, 0.02, (0.15, 0.1, 0.15), 0.05)
+    n = len(parts)
+    counts = np.array([n, n], dtype=np.uint32)
+
+    def depth(x):
+        return 0.05 - np.linalg.norm(x[:, :3].astype(np.float64) - (0.15, 0.1, 0.15), axis=1)
+
+    assert (depth(parts["pos"]) > 0.0).sum() > 100  # the lattice starts partly inside
+    with sph.Sim([p, p], counts=counts) as b, sph.Sim(p, n_max=n) as one:
+        b.upload(np.concatenate([parts, parts]))
+        one.upload(parts)
+        for sim in (b, one):
+            sim.set_obstacle(sdf, (0.0, 0.0, 0.0), 0.02)
+            sim.step(1)
+        out, ref = b.download(), one.download()
+        for g in (out["pos"][:n], out["pos"][n:]):
+            np.testing.assert_allclose(g[:, :3], ref["pos"][:, :3], rtol=0, atol=1e-6)
+        b.step(5)
+        out = b.download()
+    for x in (out["pos"][:n], out["pos"][n:]):  # within the sampling error of a 0.02 grid on r = 0.05
+        assert depth(x).max() < 5e-3

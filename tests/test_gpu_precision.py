@@ -77,5 +77,5 @@ def test_crop_fp32_and_learned_against_fp64(sph, orc, gpu):
     assert out["plain_fp32"]["density_err_mean"] < 1e-3
     assert out["plain_fp32"]["momentum_diff_rel"] < 1e-3
     if "learned_bf16" in out:  # the trained network beats the macro-step without it (v' = v, x' = x + 4 dt v)
-        assert out["learned_bf16"]["density_err_mean"] < out["zero_network"]["density_err_mean"]
-        assert out["learned_bf16"]["momentum_diff_rel"] < 0.05
+        for k in ("density_err_mean", "momentum_diff_rel", "kinetic_energy_diff_rel"):
+            assert out["learned_bf16"][k] < out["zero_network"][k], k
