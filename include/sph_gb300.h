@@ -236,6 +236,8 @@ typedef struct sph_learned_report {
     uint64_t discarded_macro_steps;/* learned macro-steps thrown away by roll-backs */
     double last_mean_rho_dev;      /* |sum rho_learned - sum rho_plain| / sum rho_plain at the last judge */
     double max_mean_rho_dev;
+    double last_max_rho_dev;       /* |max rho_learned - max rho_plain| / max rho_plain at the last judge */
+    double max_max_rho_dev;
 } sph_learned_report;
 
 #define SPH_JUDGE_MEAN_DENSITY      0
@@ -278,6 +280,11 @@ sph_status sph_learned_step(sph_ctx* ctx, sph_mpnn* net, int32_t n_macro, int32_
 /* The density deviation the judge of sph_learned_step compares with density_tol:
  * SPH_JUDGE_MEAN_DENSITY (default) or SPH_JUDGE_PARTICLE_DENSITY. */
 sph_status sph_learned_set_judge(sph_ctx* ctx, int32_t metric);
+/* A further bound of the judge: the interval also fails when the maximum density deviates by
+ * more than tol, |max rho_learned - max rho_plain| / max rho_plain (default: no bound). The
+ * mean density can stay within 1% while a network packs particles into clusters; the
+ * maximum density shows that. */
+sph_status sph_learned_set_max_density_tol(sph_ctx* ctx, float tol);
 /* Recompute rho and pres at the current positions (the state is re-sorted by cell). */
 sph_status sph_refresh_density(sph_ctx* ctx);
 /* The learned macro-step's input lists at the current positions, by particle id (record

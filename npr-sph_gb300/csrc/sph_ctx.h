@@ -2,6 +2,7 @@
 // engine helpers that the learned macro-step (sph_learn.cu) reuses.
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -30,6 +31,7 @@ struct sph_ctx {
     int judge_failures = 0;  // failed judges in a row
     int judge_backoff = 0;   // plain intervals still to run before the next learned attempt
     int judge_metric = SPH_JUDGE_MEAN_DENSITY;  // density deviation the judge decides on
+    double judge_max_rho_tol = INFINITY;        // bound on the deviation of the maximum density
     long long cell_cap = 0;
     int tile_cap = 0;
     double* diag_dev = nullptr;

@@ -229,13 +229,13 @@ __global__ void __launch_bounds__(kT) k_lists_by_id(const float4* __restrict__ v
 }
 
 // FP64 partials of the judge: sum |rho_l - rho_p| / rho_p, sum (v_l - v_p) (3), sum |v_p|,
-// sum rho_l, sum rho_p.
-constexpr int kCmpFields = 7;
+// sum rho_l, sum rho_p, max rho_l, max rho_p (fields 7 and 8 combine by max).
+constexpr int kCmpFields = 9;
 __global__ void __launch_bounds__(kT) k_compare(const float* __restrict__ rl, const float* __restrict__ rp,
                                                const float4* __restrict__ vl, const float4* __restrict__ vp, int n,
                                                double* __restrict__ out) {
     __shared__ double sh[kCmpFields][kT];
-    double a[kCmpFields] = {0, 0, 0, 0, 0, 0, 0};
+    double a[kCmpFields] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     for (int i = blockIdx.x * kT + threadIdx.x; i < n; i += gridDim.x * kT) {
         a[0] += fabs((double)rl[i] - (double)rp[i]) / (double)rp[i];
         a[1] += (double)vl[i].x - (double)vp[i].x;
@@ -244,12 +244,16 @@ __global__ void __launch_bounds__(kT) k_compare(const float* __restrict__ rl, co
         a[4] += sqrt((double)vp[i].x * vp[i].x + (double)vp[i].y * vp[i].y + (double)vp[i].z * vp[i].z);
         a[5] += (double)rl[i];
         a[6] += (double)rp[i];
+        a[7] = fmax(a[7], (double)rl[i]);
+        a[8] = fmax(a[8], (double)rp[i]);
     }
     for (int f = 0; f < kCmpFields; ++f) sh[f][threadIdx.x] = a[f];
     __syncthreads();
     for (int o = kT / 2; o > 0; o >>= 1) {
         if (threadIdx.x < o)
-            for (int f = 0; f < kCmpFields; ++f) sh[f][threadIdx.x] += sh[f][threadIdx.x + o];
+            for (int f = 0; f < kCmpFields; ++f)
+                sh[f][threadIdx.x] = f >= 7 ? fmax(sh[f][threadIdx.x], sh[f][threadIdx.x + o])
+                                            : sh[f][threadIdx.x] + sh[f][threadIdx.x + o];
         __syncthreads();
     }
     if (threadIdx.x == 0)
@@ -405,7 +409,7 @@ void restore_state(sph_ctx* ctx, const Saved& s) {
 // from that state, compared by particle id. Returns the mean relative density deviation and
 // the momentum difference; the learned result is left in (l_pos, l_vel, l_rhop) and the plain
 // one in the context.
-sph_status judge_macro(sph_ctx* ctx, sph_mpnn* net, double& dev, double& mom, double& mdev) {
+sph_status judge_macro(sph_ctx* ctx, sph_mpnn* net, double& dev, double& mom, double& mdev, double& xdev) {
     const int n = ctx->b.n;
     const Saved s0 = save_state(ctx, net->snap_pos, net->snap_vel, net->snap_rhop);
     if (!ctx->need_hash) cudaMemsetAsync(ctx->b.count, 0, sizeof(int) * (size_t)ctx->b.ncell, ctx->stream);
@@ -425,11 +429,15 @@ sph_status judge_macro(sph_ctx* ctx, sph_mpnn* net, double& dev, double& mom, do
     if (cudaMemcpyAsync(h.data(), net->cmp, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, ctx->stream) ||
         cudaStreamSynchronize(ctx->stream))
         return fail(ctx, SPH_ERR_CUDA, "judge readback");
-    double sum[kCmpFields] = {0, 0, 0, 0, 0, 0, 0};
+    double sum[kCmpFields] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     for (int b = 0; b < kCmpBlocks; ++b)
-        for (int f = 0; f < kCmpFields; ++f) sum[f] += h[(size_t)b * kCmpFields + f];
+        for (int f = 0; f < kCmpFields; ++f) {
+            const double x = h[(size_t)b * kCmpFields + f];
+            sum[f] = f >= 7 ? std::max(sum[f], x) : sum[f] + x;
+        }
     dev = sum[0] / n;
     mdev = sum[6] > 0.0 ? std::fabs(sum[5] - sum[6]) / sum[6] : INFINITY;
+    xdev = sum[8] > 0.0 ? std::fabs(sum[7] - sum[8]) / sum[8] : INFINITY;
     const double g = std::sqrt((double)ctx->s0.g[0] * ctx->s0.g[0] + (double)ctx->s0.g[1] * ctx->s0.g[1] +
                                (double)ctx->s0.g[2] * ctx->s0.g[2]);
     mom = std::sqrt(sum[1] * sum[1] + sum[2] * sum[2] + sum[3] * sum[3]) / (sum[4] + n * g * 4.0 * ctx->s0.dt);
@@ -729,6 +737,13 @@ sph_status sph_learned_set_judge(sph_ctx* ctx, int32_t metric) {
     return SPH_OK;
 }
 
+sph_status sph_learned_set_max_density_tol(sph_ctx* ctx, float tol) {
+    if (!ctx) return SPH_ERR_INVALID_ARG;
+    if (!(tol >= 0.0f)) return fail(ctx, SPH_ERR_INVALID_ARG, "max-density tolerance must be >= 0");
+    ctx->judge_max_rho_tol = tol;
+    return SPH_OK;
+}
+
 sph_status sph_learned_step(sph_ctx* ctx, sph_mpnn* net, int32_t n_macro, int32_t judge_every, float density_tol,
                             float momentum_tol, sph_learned_report* rep) {
     if (!ctx || !net) return SPH_ERR_INVALID_ARG;
@@ -775,8 +790,8 @@ sph_status sph_learned_step(sph_ctx* ctx, sph_mpnn* net, int32_t n_macro, int32_
             st = learned_macro(ctx, net);
             if (st) return st;
         }
-        double dev = 0.0, mom = 0.0, mdev = 0.0;
-        st = judge_macro(ctx, net, dev, mom, mdev);
+        double dev = 0.0, mom = 0.0, mdev = 0.0, xdev = 0.0;
+        st = judge_macro(ctx, net, dev, mom, mdev, xdev);
         if (st) return st;
         ++r.judged;
         r.last_density_dev = dev;
@@ -785,8 +800,10 @@ sph_status sph_learned_step(sph_ctx* ctx, sph_mpnn* net, int32_t n_macro, int32_
         r.sum_density_dev += dev;
         r.last_mean_rho_dev = mdev;
         r.max_mean_rho_dev = std::max(r.max_mean_rho_dev, mdev);
+        r.last_max_rho_dev = xdev;
+        r.max_max_rho_dev = std::max(r.max_max_rho_dev, xdev);
         const double crit = ctx->judge_metric == SPH_JUDGE_PARTICLE_DENSITY ? dev : mdev;
-        if (crit <= density_tol && mom <= momentum_tol) {
+        if (crit <= density_tol && mom <= momentum_tol && xdev <= ctx->judge_max_rho_tol) {
             copy_state(ctx, ctx->b.pos, ctx->b.vel, ctx->b.rhop, net->l_pos, net->l_vel, net->l_rhop);
             cudaMemsetAsync(ctx->b.count, 0, sizeof(int) * (size_t)ctx->b.ncell, ctx->stream);
             ctx->need_hash = true;

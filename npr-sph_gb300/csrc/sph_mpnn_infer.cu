@@ -250,7 +250,10 @@ __device__ __forceinline__ void load_edge_frags(const uint32_t* __restrict__ fr,
     }
 }
 
-__global__ void __launch_bounds__(kThreads) k_infer_r1(const float4* __restrict__ pos, const float4* __restrict__ vel,
+// 8 CTAs of 4 warps per SM (at most 64 registers): the edge loops wait on neighbour gathers,
+// and 32 warps per SM hide that latency better than 16 (the macro-step takes 2.68 instead of
+// 3.25 ms on the 1M dam break; 6 CTAs per SM, 80 registers, took 3.55 ms).
+__global__ void __launch_bounds__(kThreads, 8) k_infer_r1(const float4* __restrict__ pos, const float4* __restrict__ vel,
                                                       const float2* __restrict__ rhop, const int* __restrict__ nb,
                                                       const int* __restrict__ cnt, FrameConst fc, int n,
                                                       const uint32_t* __restrict__ fr,
@@ -332,7 +335,7 @@ __global__ void __launch_bounds__(kThreads) k_infer_r1(const float4* __restrict_
     }
 }
 
-__global__ void __launch_bounds__(kThreads) k_infer_r2(const float4* __restrict__ pos, const float4* __restrict__ vel,
+__global__ void __launch_bounds__(kThreads, 8) k_infer_r2(const float4* __restrict__ pos, const float4* __restrict__ vel,
                                                       const int* __restrict__ nb, const int* __restrict__ cnt,
                                                       FrameConst fc, int n, const uint32_t* __restrict__ fr,
                                                       const float* __restrict__ prm,

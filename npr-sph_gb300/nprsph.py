@@ -70,7 +70,8 @@ class LearnedReport(C.Structure):
                 ("fallbacks", C.c_uint64), ("last_density_dev", C.c_double), ("last_momentum_dev", C.c_double),
                 ("max_density_dev", C.c_double), ("sum_density_dev", C.c_double),
                 ("discarded_macro_steps", C.c_uint64), ("last_mean_rho_dev", C.c_double),
-                ("max_mean_rho_dev", C.c_double)]
+                ("max_mean_rho_dev", C.c_double), ("last_max_rho_dev", C.c_double),
+                ("max_max_rho_dev", C.c_double)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -136,6 +137,7 @@ _SIGS = {
     "sph_learned_step": (C.c_int32, [_P, _P, C.c_int32, C.c_int32, C.c_float, C.c_float, C.POINTER(LearnedReport)]),
     "sph_refresh_density": (C.c_int32, [_P]),
     "sph_learned_set_judge": (C.c_int32, [_P, C.c_int32]),
+    "sph_learned_set_max_density_tol": (C.c_int32, [_P, C.c_float]),
     "sph_neighbor_lists": (C.c_int32, [_P, _P, _P, _P]),
     "sph_view_default": (C.c_int32, [C.POINTER(View), C.c_int32, C.c_int32, C.c_float]),
     "sph_view_camera": (C.c_int32, [C.POINTER(View), C.c_float, C.c_float, C.POINTER(C.c_float),
@@ -514,6 +516,10 @@ class Sim:
     def set_judge(self, metric: int) -> None:
         """Density deviation of the learned step's judge: JUDGE_MEAN_DENSITY or JUDGE_PARTICLE_DENSITY."""
         _check(lib.sph_learned_set_judge(self._ctx, metric), self._ctx)
+
+    def set_max_density_tol(self, tol: float) -> None:
+        """Bound of the judge on the deviation of the maximum density (sph_learned_set_max_density_tol)."""
+        _check(lib.sph_learned_set_max_density_tol(self._ctx, C.c_float(tol)), self._ctx)
 
     def learned_step(self, net: "Net", n_macro: int, judge_every: int = 8, density_tol: float = 0.01,
                      momentum_tol: float = 0.01) -> LearnedReport:

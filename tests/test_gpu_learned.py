@@ -212,3 +212,25 @@ def test_judge_metric_selects_the_density_deviation(sph, trained):
     mean, part = out[sph.JUDGE_MEAN_DENSITY], out[sph.JUDGE_PARTICLE_DENSITY]
     assert (mean.learned_macro_steps, mean.fallbacks) == (1, 0)
     assert (part.learned_macro_steps, part.fallbacks) == (0, 1)
+
+
+def test_max_density_bound(sph, trained):
+    """sph_learned_set_max_density_tol: the judge also fails an interval whose maximum density
+    deviates from plain SPH's by more than the bound (unbounded by default)."""
+    net, _ = trained
+    sc = sph.dam_break(16, 32, 32, seed=25)
+    with sph.Sim(sc.params, n_max=len(sc.particles)) as sim:
+        sim.upload(sc.particles)
+        sim.step(8)
+        start = sim.download()
+        probe = sim.learned_step(net, 1, 1, 1e30, 1e30)
+        assert probe.learned_macro_steps == 1 and probe.last_max_rho_dev > 0.0
+        out = {}
+        for name, tol in (("tight", 0.5 * probe.last_max_rho_dev), ("loose", 2.0 * probe.last_max_rho_dev + 1e-6)):
+            sim.upload(start)
+            sim.set_max_density_tol(tol)
+            out[name] = sim.learned_step(net, 1, 1, 1e30, 1e30)
+        with pytest.raises(sph.SphError):
+            sim.set_max_density_tol(-1.0)
+    assert (out["tight"].learned_macro_steps, out["tight"].fallbacks) == (0, 1)
+    assert (out["loose"].learned_macro_steps, out["loose"].fallbacks) == (1, 0)
