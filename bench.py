@@ -39,7 +39,7 @@ UNIT = "particle-updates/s"
 #   force+integrate (read pos, vel, rho, p; write pos, vel) 72
 B_ALG = {"sort": 64, "density": 24, "force_integrate": 72}
 B_ALG_STEP = sum(B_ALG.values())
-KERNELS_PER_STEP = 5  # scan, scatter, gather, density, force_integrate
+KERNELS_PER_STEP = 6  # scan_tiles, scan_apply, scatter, gather, density, force_integrate
 L2_FLUSH_BYTES = 256 << 20
 
 

@@ -118,15 +118,30 @@ __global__ void __launch_bounds__(kThreads) k_reduce_partial(const float4* __res
     }
 }
 
-__global__ void k_reduce_final(const double* __restrict__ partials, int chunks, double* __restrict__ out) {
-    const int sc = blockIdx.x, f = threadIdx.x;
-    if (f >= kDiagFields) return;
-    double r = f == 6 ? INFINITY : (f == 7 ? -INFINITY : 0.0);
-    for (int c = 0; c < chunks; ++c) {
-        double x = partials[((size_t)sc * chunks + c) * kDiagFields + f];
-        r = f == 6 ? fmin(r, x) : (f == 7 ? fmax(r, x) : r + x);
+// One CTA per scene: thread t combines chunks t, t + kThreads, ... of every field, then a
+// fixed-order tree over the threads (deterministic, like the partial sums).
+__global__ void __launch_bounds__(kThreads) k_reduce_final(const double* __restrict__ partials, int chunks,
+                                                           double* __restrict__ out) {
+    const int sc = blockIdx.x;
+    __shared__ double sh[kThreads];
+    for (int f = 0; f < kDiagFields; ++f) {
+        double r = f == 6 ? INFINITY : (f == 7 ? -INFINITY : 0.0);
+        for (int c = threadIdx.x; c < chunks; c += kThreads) {
+            const double x = partials[((size_t)sc * chunks + c) * kDiagFields + f];
+            r = f == 6 ? fmin(r, x) : (f == 7 ? fmax(r, x) : r + x);
+        }
+        sh[threadIdx.x] = r;
+        __syncthreads();
+        for (int o = kThreads / 2; o > 0; o >>= 1) {
+            if (threadIdx.x < o) {
+                const double x = sh[threadIdx.x], y = sh[threadIdx.x + o];
+                sh[threadIdx.x] = f == 6 ? fmin(x, y) : (f == 7 ? fmax(x, y) : x + y);
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) out[(size_t)sc * kDiagFields + f] = sh[0];
+        __syncthreads();
     }
-    out[(size_t)sc * kDiagFields + f] = r;
 }
 
 }  // namespace
@@ -156,7 +171,7 @@ void launch_reduce(const Buffers& b, const SceneDev*, int nscene, double* out_de
     const int chunks = reduce_chunks(nscene);
     dim3 grid(chunks, nscene);
     k_reduce_partial<<<grid, kThreads, 0, st>>>(b.pos, b.vel, b.rhop, b.scenes, b.partials);
-    k_reduce_final<<<nscene, 32, 0, st>>>(b.partials, chunks, out_dev);
+    k_reduce_final<<<nscene, kThreads, 0, st>>>(b.partials, chunks, out_dev);
 }
 
 }  // namespace sphgb
