@@ -415,7 +415,9 @@ sph_status sph_image_write_ppm(const char* path, const uint8_t* rgba, int32_t wi
  * The reference keeps its state only in the GL buffer and re-creates it on 'r'
  * (Main.cpp:460-464). A snapshot file holds what resumes a run bit for bit:
  * the records in caller order, the uniforms and particle count of every scene
- * and the step count, with a checksum. A trajectory file is the same header
+ * and the step count, with a checksum. The obstacle (sph_set_obstacle), the launch
+ * shape and the learned judge's settings are not part of it: set them again after a
+ * load. A trajectory file is the same header
  * followed by frames appended during a run. Format (little-endian):
  *   64-byte header: magic "NPRSPHS1" (snapshot) / "NPRSPHT1" (trajectory),
  *     u32 version 1, u32 header bytes 64, u64 particles, u32 scenes, u32 flags,
