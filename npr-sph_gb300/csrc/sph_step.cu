@@ -63,7 +63,7 @@ template <int R>
 struct TileGeom {
     static constexpr int kSide = 2 * R + 1;
     static constexpr int kSegPerRow = kSide * kSide;
-    static constexpr int kMaxRows = R == 1 ? 32 : 16;
+    static constexpr int kMaxRows = 16;  // cell rows per chunk tile (more: the global-memory path)
     static constexpr int kMaxSeg = kMaxRows * kSegPerRow;
 };
 
