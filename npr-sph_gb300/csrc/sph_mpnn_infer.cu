@@ -4,12 +4,14 @@
 // sph_mpnn.cu are its reference.
 //
 // Two kernels, one warp per tile of 16 particles (sorted order):
-//   k_infer_r1  per particle: edge features of its <= 32 neighbours, the
-//               round-1 edge layer as Z^T = We1^T E^T (features on the MMA M
-//               side, 4 tiles of 16; edges on N, 4 tiles of 8), relu and the
-//               edge sum inside the lane plus two shuffles -> M1 in a shared
-//               tile; per 16 particles: H1 = relu([M1 n 1] Wn1'), P = H1 Wp
-//               (H1 is reused from the accumulator registers as the A operand).
+//   k_infer_r1  per particle: edge features of its <= 32 neighbours, built
+//               once per edge into a shared buffer and loaded as B fragments
+//               with ldmatrix, the round-1 edge layer as Z^T = We1^T E^T
+//               (features on the MMA M side, 4 tiles of 16; edges on N, 4
+//               tiles of 8), relu and the edge sum inside the lane -> M1 in a
+//               shared tile; per 16 particles: H1 = relu([M1 n 1] Wn1'),
+//               P = H1 Wp (H1 is reused from the accumulator registers as the
+//               A operand).
 //   k_infer_r2  round 2 likewise, with the gathered P_j as the accumulator's
 //               initial value; per 16 particles: H2 = relu([M2 H1 1] Wn2'),
 //               O = H2 Wo + bo (both heads), then the macro-step update and cell hash.
@@ -102,88 +104,112 @@ __global__ void k_prep_frags(const float* __restrict__ prm, uint32_t* __restrict
     fr[t] = pack_bf16(wel(Wm, kin, nout, b, brow, k, o), wel(Wm, kin, nout, b, brow, k + 1, o));
 }
 
-// B fragment of the edge (i -> j): lane tq holds features (2 tq, 2 tq + 1) in b0 and
-// (8 + 2 tq, 9 + 2 tq) in b1 as bf16 pairs; feature FE (= 14) is the bias column (1) and 15 is
-// zero. Every lane computes all features and selects its pairs (no divergence).
-static_assert(FE == 14, "edge_b is written for 14 edge features plus the bias column");
-__device__ __forceinline__ void edge_b(float4 pi, float4 vi, float4 pj, float4 vj, float ih, float ic, int tq,
-                                       bool valid, uint32_t& b0, uint32_t& b1) {
+struct EdgeFrags {
+    uint32_t a[4][4];  // [mt][reg]
+};
+
+// Feature buffer of one warp: 4 edge slots x 8 particles x kFRow bf16 (48-byte rows, so the
+// 8 rows an ldmatrix reads fall on distinct banks).
+constexpr int kFRow = 24;
+constexpr int kFBuf = 4 * 8 * kFRow;
+static_assert(8 * kLd2 + kFBuf <= kTile * kLd2, "round 2 keeps the feature buffer in X rows 8-15");
+
+__device__ __forceinline__ void ldmatrix_x2(uint32_t& r0, uint32_t& r1, const __nv_bfloat16* p) {
+    const uint32_t a = static_cast<uint32_t>(__cvta_generic_to_shared(p));
+    asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0, %1}, [%2];\n" : "=r"(r0), "=r"(r1) : "r"(a));
+}
+
+// The 16 features of edge (i -> j) as 8 bf16 pairs, in the k order of the edge-layer
+// fragments: d (3), u (3), r/h, q, q^2 d/(r/h) (3), q u (3), the bias column 1, and 0.
+__device__ __forceinline__ void edge_features(float4 pi, float4 vi, float4 pj, float4 vj, float ih, float ic,
+                                              uint4& w0, uint4& w1) {
     const float dx = (pj.x - pi.x) * ih, dy = (pj.y - pi.y) * ih, dz = (pj.z - pi.z) * ih;
     const float ux = (vj.x - vi.x) * ic, uy = (vj.y - vi.y) * ic, uz = (vj.z - vi.z) * ic;
     const float r = sqrtf(dx * dx + dy * dy + dz * dz);
     const float q = 1.0f - r;
     const float sg = r > 0.0f ? q * q / r : 0.0f;
-    const float a0 = tq == 0 ? dx : tq == 1 ? dz : tq == 2 ? uy : r;
-    const float a1 = tq == 0 ? dy : tq == 1 ? ux : tq == 2 ? uz : q;
-    const float c0 = tq == 0 ? sg * dx : tq == 1 ? sg * dz : tq == 2 ? q * uy : 1.0f;
-    const float c1 = tq == 0 ? sg * dy : tq == 1 ? q * ux : tq == 2 ? q * uz : 0.0f;
-    b0 = valid ? pack_bf16(a0, a1) : 0u;
-    b1 = valid ? pack_bf16(c0, c1) : 0u;
+    w0 = make_uint4(pack_bf16(dx, dy), pack_bf16(dz, ux), pack_bf16(uy, uz), pack_bf16(r, q));
+    w1 = make_uint4(pack_bf16(sg * dx, sg * dy), pack_bf16(sg * dz, q * ux), pack_bf16(q * uy, q * uz),
+                    pack_bf16(1.0f, 0.0f));
 }
 
-struct EdgeFrags {
-    uint32_t a[4][4];  // [mt][reg]
-};
-
 // Round-1/2 edge layer of a tile of 16 particles (rows of X), two groups of 8. An MMA n-tile
-// holds the same edge slot e of the group's 8 particles (column c = particle c): the loop over
-// edge slots has no per-particle branch, so the gathers of successive slots overlap. Lane
-// (g, tq) builds the features of particle g's edge e and accumulates relu(Z) for features
-// (16 mt + g, 16 mt + g + 8) of particles 2 tq and 2 tq + 1; padded edges have all-zero
-// features (bias included), so they add exactly zero. The sums / K go to X[:, 0:64].
+// holds the same edge slot e of the group's 8 particles (column c = particle c). The features
+// of each edge are built once: per step of 4 slots, lane L builds those of particle L & 7's
+// slot e0 + L / 8 into the warp's buffer E, and each slot's B fragment is one ldmatrix (matrix
+// 0: features 0-7 of the 8 particles, matrix 1: features 8-15). Lane (g, tq) accumulates
+// relu(Z) for features (16 mt + g, 16 mt + g + 8) of particles 2 tq and 2 tq + 1; padded edges
+// have all-zero features (bias included), so they add exactly zero. The sums / K go to
+// X[:, 0:64].
 template <bool ROUND2>
 __device__ __forceinline__ void edge_tile(const EdgeFrags& A, int base, int n, const float4* __restrict__ pos,
                                           const float4* __restrict__ vel, const int* nb_s, const int* cnt_s,
                                           float ih, float ic, const uint4* __restrict__ Pperm,
-                                          __nv_bfloat16* X, int ld) {
+                                          __nv_bfloat16* X, int ld, __nv_bfloat16* E) {
     const int lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
+    const int fp = lane & 7, fs = lane >> 3;  // the edge this lane builds: particle fp, slot e0 + fs
+    const __nv_bfloat16* lrow = E + (lane & 7) * kFRow + ((lane >> 3) & 1) * 8;  // ldmatrix row address
 #pragma unroll 1
     for (int grp = 0; grp < 2; ++grp) {
-        const int pc = grp * 8 + g;  // this lane's column particle (tile row)
-        const int i = base + pc;
-        const float4 pi = i < n ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-        const float4 vi = i < n ? vel[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-        const int ci = cnt_s[pc];
+        const int pb = grp * 8 + fp, ib = base + pb;
+        const float4 pi = ib < n ? pos[ib] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 vi = ib < n ? vel[ib] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const int cb = cnt_s[pb];
         const int c0 = cnt_s[grp * 8 + 2 * tq], c1 = cnt_s[grp * 8 + 2 * tq + 1];
-        int emax = ci;
+        int emax = cb;
 #pragma unroll
-        for (int o = 16; o >= 4; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+        for (int o = 1; o <= 4; o <<= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
         float s[4][2][2];
 #pragma unroll
         for (int mt = 0; mt < 4; ++mt) s[mt][0][0] = s[mt][0][1] = s[mt][1][0] = s[mt][1][1] = 0.0f;
-#pragma unroll 2
-        for (int e = 0; e < emax; ++e) {
-            const bool valid = e < ci;
-            const int j = valid ? nb_s[pc * K + e] : 0;
-            uint32_t b0, b1;
-            const float4 pj = valid ? pos[j] : pi, vj = valid ? vel[j] : vi;
-            edge_b(pi, vi, pj, vj, ih, ic, tq, valid, b0, b1);
-            float c[4][4];
-            if constexpr (ROUND2) {
-                // accumulators start at P_j of the two column particles 2 tq, 2 tq + 1
-                uint4 p0 = make_uint4(0, 0, 0, 0), p1 = make_uint4(0, 0, 0, 0);
-                if (e < c0) p0 = Pperm[(size_t)nb_s[(grp * 8 + 2 * tq) * K + e] * 8 + g];
-                if (e < c1) p1 = Pperm[(size_t)nb_s[(grp * 8 + 2 * tq + 1) * K + e] * 8 + g];
-                const uint32_t w0[4] = {p0.x, p0.y, p0.z, p0.w}, w1[4] = {p1.x, p1.y, p1.z, p1.w};
-#pragma unroll
-                for (int mt = 0; mt < 4; ++mt) {  // word mt holds features (16 mt + g, 16 mt + g + 8)
-                    c[mt][0] = bf16_lo(w0[mt]);
-                    c[mt][1] = bf16_lo(w1[mt]);
-                    c[mt][2] = bf16_hi(w0[mt]);
-                    c[mt][3] = bf16_hi(w1[mt]);
+#pragma unroll 1
+        for (int e0 = 0; e0 < emax; e0 += 4) {
+            {
+                const int e = e0 + fs;
+                uint4 w0 = make_uint4(0u, 0u, 0u, 0u), w1 = w0;
+                if (e < cb) {
+                    const int j = nb_s[pb * K + e];
+                    edge_features(pi, vi, pos[j], vel[j], ih, ic, w0, w1);
                 }
-            } else {
-#pragma unroll
-                for (int mt = 0; mt < 4; ++mt) c[mt][0] = c[mt][1] = c[mt][2] = c[mt][3] = 0.0f;
+                uint4* dst = reinterpret_cast<uint4*>(E + (fs * 8 + fp) * kFRow);
+                dst[0] = w0;
+                dst[1] = w1;
             }
+            __syncwarp();
+            const int nsl = min(4, emax - e0);
+#pragma unroll 1
+            for (int sl = 0; sl < nsl; ++sl) {
+                const int e = e0 + sl;
+                uint32_t b0, b1;
+                ldmatrix_x2(b0, b1, lrow + sl * 8 * kFRow);
+                float c[4][4];
+                if constexpr (ROUND2) {
+                    // accumulators start at P_j of the two column particles 2 tq, 2 tq + 1
+                    uint4 p0 = make_uint4(0, 0, 0, 0), p1 = make_uint4(0, 0, 0, 0);
+                    if (e < c0) p0 = Pperm[(size_t)nb_s[(grp * 8 + 2 * tq) * K + e] * 8 + g];
+                    if (e < c1) p1 = Pperm[(size_t)nb_s[(grp * 8 + 2 * tq + 1) * K + e] * 8 + g];
+                    const uint32_t q0[4] = {p0.x, p0.y, p0.z, p0.w}, q1[4] = {p1.x, p1.y, p1.z, p1.w};
 #pragma unroll
-            for (int mt = 0; mt < 4; ++mt) {
-                mma(c[mt], A.a[mt], b0, b1);
-                s[mt][0][0] += fmaxf(c[mt][0], 0.0f);
-                s[mt][0][1] += fmaxf(c[mt][1], 0.0f);
-                s[mt][1][0] += fmaxf(c[mt][2], 0.0f);
-                s[mt][1][1] += fmaxf(c[mt][3], 0.0f);
+                    for (int mt = 0; mt < 4; ++mt) {  // word mt holds features (16 mt + g, 16 mt + g + 8)
+                        c[mt][0] = bf16_lo(q0[mt]);
+                        c[mt][1] = bf16_lo(q1[mt]);
+                        c[mt][2] = bf16_hi(q0[mt]);
+                        c[mt][3] = bf16_hi(q1[mt]);
+                    }
+                } else {
+#pragma unroll
+                    for (int mt = 0; mt < 4; ++mt) c[mt][0] = c[mt][1] = c[mt][2] = c[mt][3] = 0.0f;
+                }
+#pragma unroll
+                for (int mt = 0; mt < 4; ++mt) {
+                    mma(c[mt], A.a[mt], b0, b1);
+                    s[mt][0][0] += fmaxf(c[mt][0], 0.0f);
+                    s[mt][0][1] += fmaxf(c[mt][1], 0.0f);
+                    s[mt][1][0] += fmaxf(c[mt][2], 0.0f);
+                    s[mt][1][1] += fmaxf(c[mt][3], 0.0f);
+                }
             }
+            __syncwarp();
         }
         const float sc = 1.0f / K;
 #pragma unroll
@@ -251,14 +277,16 @@ __device__ __forceinline__ void load_edge_frags(const uint32_t* __restrict__ fr,
 }
 
 // 8 CTAs of 4 warps per SM (at most 64 registers): the edge loops wait on neighbour gathers,
-// and 32 warps per SM hide that latency better than 16 (the macro-step takes 2.68 instead of
-// 3.25 ms on the 1M dam break; 6 CTAs per SM, 80 registers, took 3.55 ms).
+// and 32 warps per SM hide that latency better than 16 (with features built in every lane
+// of a quad, the macro-step took 2.68 instead of 3.25 ms on the 1M dam break; 6 CTAs per SM,
+// 80 registers, took 3.55 ms). Building each edge's features once: 2.20 ms.
 __global__ void __launch_bounds__(kThreads, 8) k_infer_r1(const float4* __restrict__ pos, const float4* __restrict__ vel,
                                                       const float2* __restrict__ rhop, const int* __restrict__ nb,
                                                       const int* __restrict__ cnt, FrameConst fc, int n,
                                                       const uint32_t* __restrict__ fr,
                                                       __nv_bfloat16* __restrict__ H1out, uint16_t* __restrict__ Pperm) {
     __shared__ __align__(16) __nv_bfloat16 xs[kWarps][kTile * kLd1];
+    __shared__ __align__(16) __nv_bfloat16 es[kWarps][kFBuf];
     __shared__ int nbs[kWarps][kTile * K];
     __shared__ int cns[kWarps][kTile];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
@@ -270,7 +298,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_infer_r1(const float4* __restri
     for (int tile = blockIdx.x * kWarps + warp; tile < ntiles; tile += gridDim.x * kWarps) {
         const int base = tile * kTile;
         stage_tile_lists(base, n, nb, cnt, nbs[warp], cns[warp]);
-        edge_tile<false>(A, base, n, pos, vel, nbs[warp], cns[warp], ih, ic, nullptr, X, kLd1);
+        edge_tile<false>(A, base, n, pos, vel, nbs[warp], cns[warp], ih, ic, nullptr, X, kLd1, es[warp]);
         // node features, bias column and padding (columns 64 .. 79) of the 16 rows
         for (int q = lane; q < kTile * 16; q += 32) {
             const int p = q >> 4, col = q & 15, i = base + p;
@@ -361,7 +389,9 @@ __global__ void __launch_bounds__(kThreads, 8) k_infer_r2(const float4* __restri
     for (int tile = blockIdx.x * kWarps + warp; tile < ntiles; tile += gridDim.x * kWarps) {
         const int base = tile * kTile;
         stage_tile_lists(base, n, nb, cnt, nbs[warp], cns[warp]);
-        edge_tile<true>(A, base, n, pos, vel, nbs[warp], cns[warp], ih, ic, Pperm, X, kLd2);
+        // the feature buffer lives in X rows 8-15, which only group 1's sums (written after its
+        // last use) overwrite
+        edge_tile<true>(A, base, n, pos, vel, nbs[warp], cns[warp], ih, ic, Pperm, X, kLd2, X + 8 * kLd2);
         // H1 rows (columns 64 .. 127), bias column 128, padding to 143
         for (int p = 0; p < kTile; ++p) {
             const int i = base + p;
