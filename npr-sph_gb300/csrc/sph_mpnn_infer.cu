@@ -363,7 +363,10 @@ __global__ void __launch_bounds__(kThreads, 8) k_infer_r1(const float4* __restri
     }
 }
 
-__global__ void __launch_bounds__(kThreads, 8) k_infer_r2(const float4* __restrict__ pos, const float4* __restrict__ vel,
+// Round 2 runs 6 CTAs per SM (80 registers): fewer spills, and the L1 left beside the CTAs'
+// shared memory holds more of the gathered P_j rows (2.13 ms per macro-step against 2.20 ms
+// at 8 CTAs per SM, 2.25 ms at 4).
+__global__ void __launch_bounds__(kThreads, 6) k_infer_r2(const float4* __restrict__ pos, const float4* __restrict__ vel,
                                                       const int* __restrict__ nb, const int* __restrict__ cnt,
                                                       FrameConst fc, int n, const uint32_t* __restrict__ fr,
                                                       const float* __restrict__ prm,
@@ -461,21 +464,22 @@ void infer_prep(const float* prm, uint32_t* frags, cudaStream_t st) {
     k_prep_frags<<<(kFragTotal + 255) / 256, 256, 0, st>>>(prm, frags);
 }
 
-static int infer_grid(int n) {
+// Grid of a tile-stride inference kernel: at most the CTAs that fit on the GPU at once.
+static int infer_grid(int n, int per_sm) {
     const int tiles = (n + kTile - 1) / kTile;
     const int blocks = (tiles + kWarps - 1) / kWarps;
-    const int cap = device_sm_count() * 8;
+    const int cap = device_sm_count() * per_sm;
     return blocks < cap ? (blocks < 1 ? 1 : blocks) : cap;
 }
 
 void infer_round1(const Frame& f, const uint32_t* frags, __nv_bfloat16* H1, uint16_t* Pperm, cudaStream_t st) {
-    k_infer_r1<<<infer_grid(f.n), kThreads, 0, st>>>(f.pos, f.vel, f.rhop, f.nb, f.cnt, f.fc, f.n, frags, H1, Pperm);
+    k_infer_r1<<<infer_grid(f.n, 8), kThreads, 0, st>>>(f.pos, f.vel, f.rhop, f.nb, f.cnt, f.fc, f.n, frags, H1, Pperm);
 }
 
 void infer_round2(const Frame& f, const uint32_t* frags, const float* prm, const __nv_bfloat16* H1,
                   const uint16_t* Pperm, const SceneDev& S, float4* pos_out, float4* vel_out, float* out, int* key,
                   int* rank, int* count, bool integrate, cudaStream_t st) {
-    k_infer_r2<<<infer_grid(f.n), kThreads, 0, st>>>(f.pos, f.vel, f.nb, f.cnt, f.fc, f.n, frags, prm, H1,
+    k_infer_r2<<<infer_grid(f.n, 6), kThreads, 0, st>>>(f.pos, f.vel, f.nb, f.cnt, f.fc, f.n, frags, prm, H1,
                                                      reinterpret_cast<const uint4*>(Pperm), S, pos_out, vel_out, out,
                                                      key, rank, count, integrate ? 1 : 0);
 }
