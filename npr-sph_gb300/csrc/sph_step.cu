@@ -479,6 +479,7 @@ __global__ void __launch_bounds__(BLOCK) k_density_nb(const float4* __restrict__
         const bool tiled =
             stage_chunk<BATCHED, R, BLOCK>(T, st, c0, n, pos_s, start, s0, scenes, nscene, p, sc, cx, lrow);
         const int t = c0 + threadIdx.x;
+        int c = 0;
         if (t < n) {
             if (!tiled) p = pos_s[t];
             if constexpr (BATCHED) sc = min(max(scene_of(p), 0), nscene - 1);
@@ -486,7 +487,6 @@ __global__ void __launch_bounds__(BLOCK) k_density_nb(const float4* __restrict__
             const float cut = S.cut_d2, h2 = S.h2;
             float sum = 0.0f, comp = 0.0f;
             int* out = nb + (size_t)t * kNbList;
-            int c = 0;
             if (tiled) {
                 // density: the arithmetic of k_density, candidate for candidate; list: the passing
                 // candidates other than the particle itself, pruned to the nearest kNbList
@@ -523,7 +523,7 @@ __global__ void __launch_bounds__(BLOCK) k_density_nb(const float4* __restrict__
                 kahan_add(sum, comp, s2.y);
                 kahan_add(sum, comp, -c2.y);
                 prune_nearest<BLOCK>(lst, c, st, p.x, p.y, p.z);
-                for (int k = 0; k < kNbList; ++k) out[k] = k < c ? st.slot[lst[BLOCK * k]] : -1;
+                c = min(c, kNbList);  // the rows are written below, a warp at a time
             } else {
                 // global-memory path: the list lives in the output row itself
                 float worst = -1.0f;
@@ -562,6 +562,16 @@ __global__ void __launch_bounds__(BLOCK) k_density_nb(const float4* __restrict__
             const float rho = S.poly6c * sum;
             const float pr = S.gas_k * (rho - S.rho0);
             rhop[t] = make_float2(rho, pr < 0.0f ? 0.0f : pr);
+        }
+        if (tiled) {  // uniform: the warp writes its 32 particles' rows, one 128-byte row per store
+            const int lane = threadIdx.x & 31, w0 = threadIdx.x - lane;
+            const unsigned short* lst0 = reinterpret_cast<const unsigned short*>(base + 4 * kCap);
+#pragma unroll 1
+            for (int r = 0; r < 32; ++r) {
+                const int cr = __shfl_sync(0xffffffffu, c, r);
+                const int tr = c0 + w0 + r;
+                if (tr < n) nb[(size_t)tr * kNbList + lane] = lane < cr ? st.slot[lst0[BLOCK * lane + w0 + r]] : -1;
+            }
         }
         if (!tiled && threadIdx.x == 0 && stats) atomicAdd(&stats[0], 1u);
         __syncthreads();
