@@ -74,7 +74,13 @@ struct Buffers {
     int ncell = 0;
     int nscene = 1;
     uint32_t* tile_stats = nullptr;  // [0] chunks staged, [1] chunks on the global-memory path
+    uint32_t* pmask = nullptr; // [kPairMaskWords][n]: the density pass's neighbour predicates for the force pass
 };
+
+// Stencil 1 (cells of edge h): the density pass stores, per particle and per neighbour-row
+// segment, which candidates passed r < h as two 32-bit masks (even and odd candidates), and the
+// force pass reads them instead of testing the candidates again.
+constexpr int kPairMaskWords = 2 * 9;
 
 // Launch shape chosen by the autotuner.
 struct LaunchCfg {

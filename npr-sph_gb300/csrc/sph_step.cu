@@ -23,13 +23,24 @@
 // margin) or the sentinel.
 //
 // Density accumulates every candidate branch-free (its weight is zero outside
-// r < h). Force appends passing candidates to a per-thread list in shared
-// memory (the staged index) and processes the list in a second loop in which
-// all lanes are busy: with ~15% of candidates inside r < h, testing and
-// interacting in one loop would run the ~35-instruction interaction for a
-// minority of lanes almost every iteration. The list holds kNbCapForce
-// entries; a longer neighbourhood is processed in chunks, in candidate order,
-// so results are deterministic either way.
+// r < h). With stencil 1 it also records the predicate r < h of every
+// candidate: per segment, two 32-bit masks (even and odd candidates), shifted
+// in as it goes and stored column-major (kPairMaskWords coalesced words per
+// particle). The force pass then tests nothing: it makes the same chunk plan
+// (the same segments and staged offsets, without staging positions), decodes
+// the masks into a per-thread list in shared memory and reads the neighbours'
+// position, velocity and (rho, p) from global memory. Without a staged tile it
+// needs ~20 KB of shared memory per CTA of 128 instead of ~40, so twice the
+// warps hide the gathers' latency and L1 has room for them. A segment longer
+// than 32 pairs (a pile-up) is tested by the force pass itself.
+//
+// Force processes its list in a second loop in which all lanes are busy: with
+// ~15% of candidates inside r < h, testing and interacting in one loop would
+// run the ~35-instruction interaction for a minority of lanes almost every
+// iteration. The list holds kNbCapForce entries; a longer neighbourhood is
+// processed in chunks, in candidate order, so results are deterministic
+// either way. With stencil 2 force stages x/y/z like density and tests the
+// candidates itself.
 //
 // A chunk with more distinct rows or more staged candidates than the tile
 // holds (heavy pile-ups) takes a global-memory path with the same arithmetic.
@@ -86,9 +97,10 @@ struct Staged {
 };
 
 // Plan and stage one chunk [c0, c0 + BLOCK). Every thread of the CTA calls it.
-// Returns false (for the whole CTA) when the chunk does not fit the tile.
+// Returns false (for the whole CTA) when the chunk does not fit the tile. Without STAGE only
+// the plan is made (the same plan and the same decision as with it), and st is not used.
 // On return each live thread has its position p, scene sc, cell cx and local row lrow.
-template <bool BATCHED, int R, int BLOCK>
+template <bool BATCHED, int R, int BLOCK, bool STAGE = true>
 __device__ bool stage_chunk(TileShared<R, BLOCK>& T, const Staged& st, int c0, int n, const float4* __restrict__ pos_s,
                             const int* __restrict__ start, const SceneDev& s0, const SceneDev* __restrict__ scenes,
                             int nscene, float4& p, int& sc, int& cx, int& lrow) {
@@ -171,22 +183,24 @@ __device__ bool stage_chunk(TileShared<R, BLOCK>& T, const Staged& st, int c0, i
     }
     __syncthreads();
     if (T.seg_off[nseg] > stage_cap<R, BLOCK>()) return false;  // uniform
-    for (int s = warp; s < nseg; s += kWarps) {
-        const int gbeg = T.seg_gbeg[s], len = T.seg_len[s], off = T.seg_off[s];
-        const int plen = (len + 1) & ~1;
-        for (int k = lane; k < plen; k += 32) {
-            float x = kSentinel, y = kSentinel, z = kSentinel;
-            if (k < len) {
-                const float4 o = __ldg(pos_s + gbeg + k);
-                x = o.x; y = o.y; z = o.z;
+    if constexpr (STAGE) {  // without it: the plan only (segment table and staged offsets)
+        for (int s = warp; s < nseg; s += kWarps) {
+            const int gbeg = T.seg_gbeg[s], len = T.seg_len[s], off = T.seg_off[s];
+            const int plen = (len + 1) & ~1;
+            for (int k = lane; k < plen; k += 32) {
+                float x = kSentinel, y = kSentinel, z = kSentinel;
+                if (k < len) {
+                    const float4 o = __ldg(pos_s + gbeg + k);
+                    x = o.x; y = o.y; z = o.z;
+                }
+                st.x[off + k] = x;
+                st.y[off + k] = y;
+                st.z[off + k] = z;
+                if (st.slot) st.slot[off + k] = k < len ? gbeg + k : 0;
             }
-            st.x[off + k] = x;
-            st.y[off + k] = y;
-            st.z[off + k] = z;
-            if (st.slot) st.slot[off + k] = k < len ? gbeg + k : 0;
         }
+        __syncthreads();
     }
-    __syncthreads();
     return true;
 }
 
@@ -235,16 +249,27 @@ __device__ __forceinline__ void kahan_add(float& sum, float& comp, float x) {
 
 template <int R, int BLOCK>
 constexpr size_t density_smem() { return (size_t)3 * stage_cap<R, BLOCK>() * 4; }
+// Stencil 1: the list plus, per thread and segment, the global slot of the segment's first
+// staged candidate (the force pass reads neighbours from global memory). Stencil 2: the staged
+// tile x, y, z, slot plus the list.
 template <int R, int BLOCK>
-constexpr size_t force_smem() { return (size_t)4 * stage_cap<R, BLOCK>() * 4 + (size_t)kNbCapForce * BLOCK * 2; }
+constexpr size_t force_smem() {
+    return R == 1 ? (size_t)kNbCapForce * BLOCK * 2 + (size_t)TileGeom<R>::kSegPerRow * BLOCK * 4
+                  : (size_t)4 * stage_cap<R, BLOCK>() * 4 + (size_t)kNbCapForce * BLOCK * 2;
+}
+template <int R, int BLOCK>
+constexpr size_t nb_smem() { return (size_t)4 * stage_cap<R, BLOCK>() * 4 + (size_t)kNbCapForce * BLOCK * 2; }
 static_assert(stage_cap<2, 256>() < 65536, "staged indices are 16-bit");
 
 template <bool BATCHED, int R, int BLOCK>
 __global__ void __launch_bounds__(BLOCK) k_density(const float4* __restrict__ pos_s, const int* __restrict__ start,
                                                    SceneDev s0, const SceneDev* __restrict__ scenes, int nscene,
-                                                   float2* __restrict__ rhop, int n, uint32_t* __restrict__ stats) {
+                                                   float2* __restrict__ rhop, uint32_t* __restrict__ pmask, int n,
+                                                   uint32_t* __restrict__ stats) {
     using G = TileGeom<R>;
     constexpr int kCap = stage_cap<R, BLOCK>();
+    constexpr bool kMask = R == 1;  // pair masks for the force pass (kPairMaskWords words per particle)
+    static_assert(!kMask || 2 * G::kSegPerRow == kPairMaskWords, "two mask words per segment");
     __shared__ TileShared<R, BLOCK> T;
     extern __shared__ float4 dyn_d[];
     float* base = reinterpret_cast<float*>(dyn_d);
@@ -268,12 +293,13 @@ __global__ void __launch_bounds__(BLOCK) k_density(const float4* __restrict__ po
                 // is below 1e-30 * h^6: invisible in an FP32 sum of terms of order h^6.
                 const float2 npx = make_float2(-p.x, -p.x), npy = make_float2(-p.y, -p.y);
                 const float2 npz = make_float2(-p.z, -p.z);
-                const float2 h2v = make_float2(h2, h2);
+                const float2 h2v = make_float2(h2, h2), ncut = make_float2(-cut, -cut);
                 float2 s2 = make_float2(0.f, 0.f), c2 = make_float2(0.f, 0.f);
-#pragma unroll 1
+#pragma unroll
                 for (int r = 0; r < G::kSegPerRow; ++r) {
                     int a, b;
                     seg_range<R, BLOCK>(T, lrow * G::kSegPerRow + r, cx, S.dim[0], start, a, b);
+                    uint32_t mx = 0, my = 0;
 #pragma unroll 2
                     for (int j = a; j < b; j += 2) {
                         const float2 d2 = pair_d2(st, j, npx, npy, npz);
@@ -286,6 +312,18 @@ __global__ void __launch_bounds__(BLOCK) k_density(const float4* __restrict__ po
                         const float2 lost = __fadd2_rn(tt, make_float2(-s2.x, -s2.y));
                         c2 = __fadd2_rn(lost, make_float2(-y.x, -y.y));
                         s2 = tt;
+                        if constexpr (kMask) {
+                            // d2 - cut is negative exactly when d2 < cut (a difference of two distinct
+                            // floats is never zero; +inf and NaN are positive): its sign bit is the
+                            // force pass's predicate, shifted in as the masks' new lowest bit
+                            const float2 e = __fadd2_rn(d2, ncut);
+                            mx = __funnelshift_l(__float_as_uint(e.x), mx, 1);
+                            my = __funnelshift_l(__float_as_uint(e.y), my, 1);
+                        }
+                    }
+                    if constexpr (kMask) {
+                        pmask[(size_t)(2 * r) * n + t] = mx;
+                        pmask[(size_t)(2 * r + 1) * n + t] = my;
                     }
                 }
                 // combine the two lanes: (s.x - c.x) + (s.y - c.y) with a compensated add
@@ -346,20 +384,27 @@ __global__ void __launch_bounds__(BLOCK) k_force_integrate(const float4* __restr
                                                            SceneDev s0, const SceneDev* __restrict__ scenes, int nscene,
                                                            float4* __restrict__ pos_out, float4* __restrict__ vel_out,
                                                            float4* __restrict__ force_out, int* __restrict__ key_out,
-                                                           int* __restrict__ rank_out, int* __restrict__ count, int n,
+                                                           int* __restrict__ rank_out, int* __restrict__ count,
+                                                           const uint32_t* __restrict__ pmask, int n,
                                                            uint32_t* __restrict__ stats) {
     using G = TileGeom<R>;
     constexpr int kCap = stage_cap<R, BLOCK>();
+    constexpr bool kMask = R == 1;  // the density pass's pair masks replace the candidate tests
     __shared__ TileShared<R, BLOCK> T;
     extern __shared__ float4 dyn_f[];
     float* base = reinterpret_cast<float*>(dyn_f);
-    const Staged st{base, base + kCap, base + 2 * kCap, reinterpret_cast<int*>(base + 3 * kCap)};
-    unsigned short* lst = reinterpret_cast<unsigned short*>(base + 4 * kCap) + threadIdx.x;  // [kNbCapForce][BLOCK]
+    // Stencil 1: [kNbCapForce][BLOCK] list entries (segment * 64 + candidate offset), then
+    // [kSegPerRow][BLOCK] global slots of the segments' first staged candidates. Stencil 2: the
+    // staged tile, then [kNbCapForce][BLOCK] list entries (staged indices).
+    const Staged st = kMask ? Staged{nullptr, nullptr, nullptr, nullptr}
+                            : Staged{base, base + kCap, base + 2 * kCap, reinterpret_cast<int*>(base + 3 * kCap)};
+    unsigned short* lst = reinterpret_cast<unsigned short*>(kMask ? base : base + 4 * kCap) + threadIdx.x;
+    int* seg_slot = reinterpret_cast<int*>(base) + (kNbCapForce * BLOCK) / 2 + threadIdx.x;  // stencil 1 only
     for (int c0 = blockIdx.x * BLOCK; c0 < n; c0 += gridDim.x * BLOCK) {
         float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
         int sc = 0, cx = 0, lrow = 0;
-        const bool tiled =
-            stage_chunk<BATCHED, R, BLOCK>(T, st, c0, n, pos_s, start, s0, scenes, nscene, p, sc, cx, lrow);
+        const bool tiled = stage_chunk<BATCHED, R, BLOCK, !kMask>(T, st, c0, n, pos_s, start, s0, scenes, nscene, p,
+                                                                  sc, cx, lrow);
         const int t = c0 + threadIdx.x;
         if (t < n) {
             if (!tiled) p = pos_s[t];
@@ -374,30 +419,82 @@ __global__ void __launch_bounds__(BLOCK) k_force_integrate(const float4* __restr
                 // its offset and relative velocity are exactly zero, so its pressure term is
                 // skipped (d2 == 0) and its viscosity term adds exact zeros.
                 int cnt = 0;
-                auto flush = [&]() {
-                    for (int k = 0; k < cnt; ++k) {
-                        const int j = lst[BLOCK * k];
-                        const int g = st.slot[j];
-                        acc.add(p.x - st.x[j], p.y - st.y[j], p.z - st.z[j], h, rp.y, v, __ldg(rhop + g),
-                                __ldg(vel_s + g));
+                if constexpr (kMask) {
+                    // Neighbours come from global memory: entry e is candidate (e & 63) of
+                    // segment e >> 6, whose first candidate is global slot seg_slot[segment].
+                    auto interact = [&](int g) {
+                        const float4 q = __ldg(pos_s + g);
+                        acc.add(p.x - q.x, p.y - q.y, p.z - q.z, h, rp.y, v, __ldg(rhop + g), __ldg(vel_s + g));
+                    };
+                    auto flush = [&]() {
+                        for (int k = 0; k < cnt; ++k) {
+                            const int e = lst[BLOCK * k];
+                            interact(seg_slot[BLOCK * (e >> 6)] + (e & 63));
+                        }
+                        cnt = 0;
+                    };
+                    // All masks are loaded up front (one coalesced word per segment and parity).
+                    // Pair k of a segment's staged [a, b) is bit np-1-k of its masks when the
+                    // segment has np <= 32 pairs; a longer segment lost its first bits and is
+                    // tested here, from global memory.
+                    uint32_t m[kPairMaskWords];
+#pragma unroll
+                    for (int w = 0; w < kPairMaskWords; ++w) m[w] = __ldg(pmask + (size_t)w * n + t);
+#pragma unroll
+                    for (int r = 0; r < G::kSegPerRow; ++r) {
+                        const int sg = lrow * G::kSegPerRow + r;
+                        int a, b;
+                        seg_range<R, BLOCK>(T, sg, cx, S.dim[0], start, a, b);
+                        const int np = (b - a + 1) >> 1;
+                        const int g0 = T.seg_gbeg[sg] + (a - T.seg_off[sg]);  // global slot of staged a
+                        if (np > 32) {
+                            for (int g = g0; g < g0 + (b - a); ++g) {
+                                const float4 q = __ldg(pos_s + g);
+                                float dx, dy, dz;
+                                const float d2 = canon_d2(p.x, p.y, p.z, q.x, q.y, q.z, dx, dy, dz);
+                                if (d2 < cut) interact(g);  // :57
+                            }
+                            continue;
+                        }
+                        seg_slot[BLOCK * r] = g0;
+#pragma unroll
+                        for (int par = 0; par < 2; ++par) {
+                            uint32_t mk = m[2 * r + par];
+                            while (mk) {  // highest bit first: candidate order
+                                const int bit = 31 - __clz(mk);
+                                mk ^= 1u << bit;
+                                lst[BLOCK * cnt++] = (unsigned short)(r * 64 + 2 * (np - 1 - bit) + par);
+                                if (cnt == kNbCapForce) flush();
+                            }
+                        }
                     }
-                    cnt = 0;
-                };
-                const float2 npx = make_float2(-p.x, -p.x), npy = make_float2(-p.y, -p.y);
-                const float2 npz = make_float2(-p.z, -p.z);
+                    flush();
+                } else {
+                    auto flush = [&]() {
+                        for (int k = 0; k < cnt; ++k) {
+                            const int j = lst[BLOCK * k];
+                            const int g = st.slot[j];
+                            acc.add(p.x - st.x[j], p.y - st.y[j], p.z - st.z[j], h, rp.y, v, __ldg(rhop + g),
+                                    __ldg(vel_s + g));
+                        }
+                        cnt = 0;
+                    };
+                    const float2 npx = make_float2(-p.x, -p.x), npy = make_float2(-p.y, -p.y);
+                    const float2 npz = make_float2(-p.z, -p.z);
 #pragma unroll 1
-                for (int r = 0; r < G::kSegPerRow; ++r) {
-                    int a, b;
-                    seg_range<R, BLOCK>(T, lrow * G::kSegPerRow + r, cx, S.dim[0], start, a, b);
+                    for (int r = 0; r < G::kSegPerRow; ++r) {
+                        int a, b;
+                        seg_range<R, BLOCK>(T, lrow * G::kSegPerRow + r, cx, S.dim[0], start, a, b);
 #pragma unroll 2
-                    for (int j = a; j < b; j += 2) {
-                        const float2 d2 = pair_d2(st, j, npx, npy, npz);
-                        if (d2.x < cut) lst[BLOCK * cnt++] = (unsigned short)j;  // :57
-                        if (d2.y < cut) lst[BLOCK * cnt++] = (unsigned short)(j + 1);
-                        if (cnt > kNbCapForce - 2) flush();
+                        for (int j = a; j < b; j += 2) {
+                            const float2 d2 = pair_d2(st, j, npx, npy, npz);
+                            if (d2.x < cut) lst[BLOCK * cnt++] = (unsigned short)j;  // :57
+                            if (d2.y < cut) lst[BLOCK * cnt++] = (unsigned short)(j + 1);
+                            if (cnt > kNbCapForce - 2) flush();
+                        }
                     }
+                    flush();
                 }
-                flush();
             } else {
                 const int gx = cell_coord(p.x, S.lo[0], S.inv_edge, S.dim[0]);
                 const int gy = cell_coord(p.y, S.lo[1], S.inv_edge, S.dim[1]);
@@ -592,8 +689,8 @@ template <bool B, int R, int BLOCK>
 void density_impl(const Buffers& b, const SceneDev& s0, cudaStream_t st) {
     auto k = k_density<B, R, BLOCK>;
     constexpr size_t sm = density_smem<R, BLOCK>();
-    k<<<grid_size(k, BLOCK, sm, b.n), BLOCK, sm, st>>>(b.pos_s, b.start, s0, b.scenes, b.nscene, b.rhop, b.n,
-                                                       b.tile_stats);
+    k<<<grid_size(k, BLOCK, sm, b.n), BLOCK, sm, st>>>(b.pos_s, b.start, s0, b.scenes, b.nscene, b.rhop, b.pmask,
+                                                       b.n, b.tile_stats);
 }
 
 template <bool B, int R, int BLOCK>
@@ -602,7 +699,7 @@ void force_impl(const Buffers& b, const SceneDev& s0, float4* force_out, cudaStr
     constexpr size_t sm = force_smem<R, BLOCK>();
     k<<<grid_size(k, BLOCK, sm, b.n), BLOCK, sm, st>>>(b.pos_s, b.vel_s, b.rhop, b.start, s0, b.scenes, b.nscene,
                                                        b.pos, b.vel, force_out, s0.sdf ? nullptr : b.key, b.rank,
-                                                       b.count, b.n, b.tile_stats);
+                                                       b.count, b.pmask, b.n, b.tile_stats);
 }
 
 // The static obstacle's rule (sph_set_obstacle) on the integrated state, then the cell hash of
@@ -633,7 +730,7 @@ __global__ void __launch_bounds__(256) k_obstacle_hash(float4* __restrict__ pos,
 template <bool B, int R>
 void density_nb_impl(const Buffers& b, const SceneDev& s0, int* nb, int* cnt, cudaStream_t st) {
     auto k = k_density_nb<B, R, 128>;
-    constexpr size_t sm = force_smem<R, 128>();
+    constexpr size_t sm = nb_smem<R, 128>();
     k<<<grid_size(k, 128, sm, b.n), 128, sm, st>>>(b.pos_s, b.start, s0, b.scenes, b.nscene, b.rhop, nb, cnt, b.n,
                                                    b.tile_stats);
 }
@@ -669,13 +766,13 @@ void init_step_kernels() {
     set_attrs<true, 2, 128>();
     set_attrs<true, 2, 256>();
     cudaFuncSetAttribute(k_density_nb<false, 1, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)force_smem<1, 128>());
+                         (int)nb_smem<1, 128>());
     cudaFuncSetAttribute(k_density_nb<false, 2, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)force_smem<2, 128>());
+                         (int)nb_smem<2, 128>());
     cudaFuncSetAttribute(k_density_nb<true, 1, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)force_smem<1, 128>());
+                         (int)nb_smem<1, 128>());
     cudaFuncSetAttribute(k_density_nb<true, 2, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)force_smem<2, 128>());
+                         (int)nb_smem<2, 128>());
 }
 
 void launch_density(const Buffers& b, const SceneDev& s0, bool batched, const LaunchCfg& c, cudaStream_t st) {
