@@ -189,9 +189,10 @@ sph_status sph_reduce_scenes(sph_ctx* ctx, sph_diag* out, uint32_t n_scene);
 /* ---- launch shape and autotuner (new) ----------------------------------
  * threads_per_block of the pair passes (128 or 256: the particles of one
  * shared-memory tile) and stencil (1: cell edge >= h, 27 cells; 2: cell edge
- * >= h/2, 125 smaller cells).
+ * >= h/2, 125 smaller cells). A new context starts at (256, 1).
  * sph_autotune times `trial_steps` steps of every candidate shape on the
- * current state (restoring it afterwards) and keeps the fastest. */
+ * current state (restoring it afterwards) and keeps the fastest; the current
+ * shape is kept unless another is more than 3% faster. */
 sph_status sph_set_launch(sph_ctx* ctx, int32_t threads_per_block, int32_t stencil);
 sph_status sph_get_launch(const sph_ctx* ctx, int32_t* threads_per_block, int32_t* stencil);
 sph_status sph_autotune(sph_ctx* ctx, int32_t trial_steps, float* best_ms_per_step);

@@ -679,8 +679,12 @@ sph_status sph_autotune(sph_ctx* ctx, int32_t trial_steps, float* best_ms) {
     const uint64_t steps0 = ctx->steps;
     const bool stepped0 = ctx->stepped, timing0 = ctx->timing;
     ctx->timing = false;
-    const int blocks[] = {128, 256};
-    const int stencils[] = {1, 2};
+    // The current shape is timed first; another replaces it only when it is faster by more than
+    // kSwitchMargin (trial steps of one state are noisy, and the state changes as the run goes on).
+    constexpr float kSwitchMargin = 0.03f;
+    const LaunchCfg cur = ctx->cfg;
+    const int blocks[] = {cur.block, cur.block == 128 ? 256 : 128};
+    const int stencils[] = {cur.stencil, cur.stencil == 1 ? 2 : 1};
     float best = 1e30f;
     LaunchCfg best_cfg = ctx->cfg;
     for (int sten : stencils) {
@@ -707,7 +711,8 @@ sph_status sph_autotune(sph_ctx* ctx, int32_t trial_steps, float* best_ms) {
             float ms = 0;
             cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
             ms /= (float)trial_steps;
-            if (ms < best) { best = ms; best_cfg = ctx->cfg; }
+            const bool is_cur = ctx->cfg.block == cur.block && ctx->cfg.stencil == cur.stencil;
+            if (is_cur ? ms < best : ms < best * (1.0f - kSwitchMargin)) { best = ms; best_cfg = ctx->cfg; }
             restore();
         }
         if (st) break;

@@ -84,13 +84,13 @@ constexpr int kPairMaskWords = 2 * 9;
 
 // Launch shape chosen by the autotuner.
 struct LaunchCfg {
-    int block = 128;     // threads per CTA of the pair kernels (particles per shared-memory tile)
+    int block = 256;     // threads per CTA of the pair kernels (particles per shared-memory tile)
     int stencil = 1;     // cell edge = h/stencil, (2*stencil+1)^3 cells visited
     int grid_cap = 0;    // persistent grid size (CTAs); 0 = one thread per particle
 };
 
 constexpr int kScanThreads = 256;
-constexpr int kScanItems = 32;  // 8192 cells per tile: a 1M-cell grid is 128 tiles
+constexpr int kScanItems = 8;   // 2048 cells per tile: a 1M-cell grid is 512 tiles, 3 or 4 per SM
 constexpr int kScanTile = kScanThreads * kScanItems;
 
 // ---- launchers (sph_grid.cu) ----
@@ -111,7 +111,7 @@ void launch_force_integrate(const Buffers& b, const SceneDev& s0, bool batched, 
                             cudaStream_t st);
 // Density (bit-identical to launch_density) plus, per particle, the kNbList nearest neighbours
 // j != i with r < h as sorted slots into nb[n][kNbList] (-1 padded) and their number in cnt
-// (the learned macro-step's input). The threads of a CTA run kNbList-entry lists of 128.
+// (the learned macro-step's input), with the launch shape of launch_density.
 constexpr int kNbList = 32;
 void launch_density_nb(const Buffers& b, const SceneDev& s0, bool batched, const LaunchCfg& c, int* nb, int* cnt,
                        cudaStream_t st);

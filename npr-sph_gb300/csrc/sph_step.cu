@@ -727,11 +727,11 @@ __global__ void __launch_bounds__(256) k_obstacle_hash(float4* __restrict__ pos,
     }
 }
 
-template <bool B, int R>
+template <bool B, int R, int BLOCK>
 void density_nb_impl(const Buffers& b, const SceneDev& s0, int* nb, int* cnt, cudaStream_t st) {
-    auto k = k_density_nb<B, R, 128>;
-    constexpr size_t sm = nb_smem<R, 128>();
-    k<<<grid_size(k, 128, sm, b.n), 128, sm, st>>>(b.pos_s, b.start, s0, b.scenes, b.nscene, b.rhop, nb, cnt, b.n,
+    auto k = k_density_nb<B, R, BLOCK>;
+    constexpr size_t sm = nb_smem<R, BLOCK>();
+    k<<<grid_size(k, BLOCK, sm, b.n), BLOCK, sm, st>>>(b.pos_s, b.start, s0, b.scenes, b.nscene, b.rhop, nb, cnt, b.n,
                                                    b.tile_stats);
 }
 
@@ -741,6 +741,8 @@ void set_attrs() {
                          (int)density_smem<R, BLOCK>());
     cudaFuncSetAttribute(k_force_integrate<B, R, BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)force_smem<R, BLOCK>());
+    cudaFuncSetAttribute(k_density_nb<B, R, BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)nb_smem<R, BLOCK>());
 }
 
 // Calls f(integral_constant<R>, integral_constant<BLOCK>) for the runtime (block, stencil).
@@ -765,14 +767,6 @@ void init_step_kernels() {
     set_attrs<true, 1, 256>();
     set_attrs<true, 2, 128>();
     set_attrs<true, 2, 256>();
-    cudaFuncSetAttribute(k_density_nb<false, 1, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)nb_smem<1, 128>());
-    cudaFuncSetAttribute(k_density_nb<false, 2, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)nb_smem<2, 128>());
-    cudaFuncSetAttribute(k_density_nb<true, 1, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)nb_smem<1, 128>());
-    cudaFuncSetAttribute(k_density_nb<true, 2, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)nb_smem<2, 128>());
 }
 
 void launch_density(const Buffers& b, const SceneDev& s0, bool batched, const LaunchCfg& c, cudaStream_t st) {
@@ -804,13 +798,11 @@ void launch_force_integrate(const Buffers& b, const SceneDev& s0, bool batched, 
 void launch_density_nb(const Buffers& b, const SceneDev& s0, bool batched, const LaunchCfg& c, int* nb, int* cnt,
                        cudaStream_t st) {
     if (b.n <= 0) return;
-    if (batched) {
-        if (c.stencil == 2) density_nb_impl<true, 2>(b, s0, nb, cnt, st);
-        else density_nb_impl<true, 1>(b, s0, nb, cnt, st);
-    } else {
-        if (c.stencil == 2) density_nb_impl<false, 2>(b, s0, nb, cnt, st);
-        else density_nb_impl<false, 1>(b, s0, nb, cnt, st);
-    }
+    // the launch shape of launch_density, so that the densities agree bit for bit
+    if (batched)
+        dispatch(c.block, c.stencil, [&](auto R, auto BL) { density_nb_impl<true, R.value, BL.value>(b, s0, nb, cnt, st); });
+    else
+        dispatch(c.block, c.stencil, [&](auto R, auto BL) { density_nb_impl<false, R.value, BL.value>(b, s0, nb, cnt, st); });
 }
 
 }  // namespace sphgb
