@@ -549,7 +549,9 @@ def run_ours(args) -> None:
     traffic = profiled_traffic("k_force_integrate")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps,
+        "ms_per_step_by_tenth": [round(float(np.mean(w)), 4) for w in np.array_split(np.array(step_ms), 10) if len(w)],
+        "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "dam break: 1,048,576 particles (64x128x128 block, 0.5h lattice, jitter 0.01h) "
                                "against the x=0 wall of a 5.12x1.28x1.28 box, g=-9.81, dt=1e-4, plain SPH",

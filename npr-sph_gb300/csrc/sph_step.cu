@@ -68,6 +68,8 @@ namespace {
 // With R = 2 (cells of h/2, 25 neighbour rows) a chunk stages ~26 * BLOCK.
 template <int R, int BLOCK> constexpr int stage_cap() { return (R == 1 ? 12 : 30) * BLOCK; }
 constexpr int kNbCapForce = 48;         // force list entries per thread (staged index, u16)
+constexpr int kNbCapNb = 42;            // neighbour-list pass entries per thread (u16): three CTAs of
+                                        // 256 per SM with the staged tile
 constexpr float kSentinel = 1e30f;      // staged padding: its distance to any particle is +inf
 
 template <int R>
@@ -258,8 +260,9 @@ constexpr size_t force_smem() {
                   : (size_t)4 * stage_cap<R, BLOCK>() * 4 + (size_t)kNbCapForce * BLOCK * 2;
 }
 template <int R, int BLOCK>
-constexpr size_t nb_smem() { return (size_t)4 * stage_cap<R, BLOCK>() * 4 + (size_t)kNbCapForce * BLOCK * 2; }
+constexpr size_t nb_smem() { return (size_t)4 * stage_cap<R, BLOCK>() * 4 + (size_t)kNbCapNb * BLOCK * 2; }
 static_assert(stage_cap<2, 256>() < 65536, "staged indices are 16-bit");
+static_assert(kNbCapNb >= kNbList + 2, "the nearest-kNbList pruning runs when two more entries could overflow");
 
 template <bool BATCHED, int R, int BLOCK>
 __global__ void __launch_bounds__(BLOCK) k_density(const float4* __restrict__ pos_s, const int* __restrict__ start,
@@ -569,7 +572,7 @@ __global__ void __launch_bounds__(BLOCK) k_density_nb(const float4* __restrict__
     extern __shared__ float4 dyn_n[];
     float* base = reinterpret_cast<float*>(dyn_n);
     const Staged st{base, base + kCap, base + 2 * kCap, reinterpret_cast<int*>(base + 3 * kCap)};
-    unsigned short* lst = reinterpret_cast<unsigned short*>(base + 4 * kCap) + threadIdx.x;  // [kNbCapForce][BLOCK]
+    unsigned short* lst = reinterpret_cast<unsigned short*>(base + 4 * kCap) + threadIdx.x;  // [kNbCapNb][BLOCK]
     for (int c0 = blockIdx.x * BLOCK; c0 < n; c0 += gridDim.x * BLOCK) {
         float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
         int sc = 0, cx = 0, lrow = 0;
@@ -612,7 +615,7 @@ __global__ void __launch_bounds__(BLOCK) k_density_nb(const float4* __restrict__
                         s2 = tt;
                         if (d2.x < cut && j != self_j) lst[BLOCK * c++] = (unsigned short)j;
                         if (d2.y < cut && j + 1 != self_j) lst[BLOCK * c++] = (unsigned short)(j + 1);
-                        if (c > kNbCapForce - 2) prune_nearest<BLOCK>(lst, c, st, p.x, p.y, p.z);
+                        if (c > kNbCapNb - 2) prune_nearest<BLOCK>(lst, c, st, p.x, p.y, p.z);
                     }
                 }
                 kahan_add(sum, comp, s2.x);
