@@ -45,8 +45,12 @@
 // A chunk with more distinct rows or more staged candidates than the tile
 // holds (heavy pile-ups) takes a global-memory path with the same arithmetic.
 //
-// Numerics: the density sum is compensated (Kahan) in FP32; the force sums are
-// plain FP32 with contraction allowed (only the predicate is pinned bit-exact).
+// Numerics: the density sum is compensated in FP32, by blocks: a plain sum over
+// each neighbour-row segment (at most ~30 terms per lane at the densest), then
+// a Kahan sum of the segment sums and of the two lanes (relative error a few
+// 1e-7 against the FP64 oracle; the global-memory path compensates every term).
+// The force sums are plain FP32 with contraction allowed (only the predicate is
+// pinned bit-exact).
 // For i != j at r == 0 the pressure term is skipped (the shader's
 // normalize(0) is NaN, force_comp.glsl:59); the viscosity term is kept.
 #include <algorithm>
@@ -291,7 +295,7 @@ __global__ void __launch_bounds__(BLOCK) k_density(const float4* __restrict__ po
             float sum = 0.0f, comp = 0.0f;
             if (tiled) {
                 // Branch-free: every candidate adds max(h^2 - d2, 0)^3, two per step in
-                // packed lanes, each lane its own Kahan sum. The weight differs from the
+                // packed lanes, each lane its own blocked compensated sum. The weight differs from the
                 // strict-predicate one (d2 < cut) only for d2 within an ulp of h^2, where it
                 // is below 1e-30 * h^6: invisible in an FP32 sum of terms of order h^6.
                 const float2 npx = make_float2(-p.x, -p.x), npy = make_float2(-p.y, -p.y);
@@ -303,6 +307,7 @@ __global__ void __launch_bounds__(BLOCK) k_density(const float4* __restrict__ po
                     int a, b;
                     seg_range<R, BLOCK>(T, lrow * G::kSegPerRow + r, cx, S.dim[0], start, a, b);
                     uint32_t mx = 0, my = 0;
+                    float2 seg = make_float2(0.f, 0.f);
 #pragma unroll 2
                     for (int j = a; j < b; j += 2) {
                         const float2 d2 = pair_d2(st, j, npx, npy, npz);
@@ -310,11 +315,7 @@ __global__ void __launch_bounds__(BLOCK) k_density(const float4* __restrict__ po
                         w.x = fmaxf(w.x, 0.0f);
                         w.y = fmaxf(w.y, 0.0f);
                         const float2 term = __fmul2_rn(__fmul2_rn(w, w), w);
-                        const float2 y = __fadd2_rn(term, make_float2(-c2.x, -c2.y));  // Kahan, per lane
-                        const float2 tt = __fadd2_rn(s2, y);
-                        const float2 lost = __fadd2_rn(tt, make_float2(-s2.x, -s2.y));
-                        c2 = __fadd2_rn(lost, make_float2(-y.x, -y.y));
-                        s2 = tt;
+                        seg = __fadd2_rn(seg, term);
                         if constexpr (kMask) {
                             // d2 - cut is negative exactly when d2 < cut (a difference of two distinct
                             // floats is never zero; +inf and NaN are positive): its sign bit is the
@@ -323,6 +324,13 @@ __global__ void __launch_bounds__(BLOCK) k_density(const float4* __restrict__ po
                             mx = __funnelshift_l(__float_as_uint(e.x), mx, 1);
                             my = __funnelshift_l(__float_as_uint(e.y), my, 1);
                         }
+                    }
+                    {  // Kahan, per lane, of the segment's sum
+                        const float2 y = __fadd2_rn(seg, make_float2(-c2.x, -c2.y));
+                        const float2 tt = __fadd2_rn(s2, y);
+                        const float2 lost = __fadd2_rn(tt, make_float2(-s2.x, -s2.y));
+                        c2 = __fadd2_rn(lost, make_float2(-y.x, -y.y));
+                        s2 = tt;
                     }
                     if constexpr (kMask) {
                         pmask[(size_t)(2 * r) * n + t] = mx;
@@ -601,6 +609,7 @@ __global__ void __launch_bounds__(BLOCK) k_density_nb(const float4* __restrict__
                 for (int r = 0; r < G::kSegPerRow; ++r) {
                     int a, b;
                     seg_range<R, BLOCK>(T, lrow * G::kSegPerRow + r, cx, S.dim[0], start, a, b);
+                    float2 seg = make_float2(0.f, 0.f);
 #pragma unroll 2
                     for (int j = a; j < b; j += 2) {
                         const float2 d2 = pair_d2(st, j, npx, npy, npz);
@@ -608,14 +617,17 @@ __global__ void __launch_bounds__(BLOCK) k_density_nb(const float4* __restrict__
                         w.x = fmaxf(w.x, 0.0f);
                         w.y = fmaxf(w.y, 0.0f);
                         const float2 term = __fmul2_rn(__fmul2_rn(w, w), w);
-                        const float2 y = __fadd2_rn(term, make_float2(-c2.x, -c2.y));
+                        seg = __fadd2_rn(seg, term);
+                        if (d2.x < cut && j != self_j) lst[BLOCK * c++] = (unsigned short)j;
+                        if (d2.y < cut && j + 1 != self_j) lst[BLOCK * c++] = (unsigned short)(j + 1);
+                        if (c > kNbCapNb - 2) prune_nearest<BLOCK>(lst, c, st, p.x, p.y, p.z);
+                    }
+                    {  // Kahan, per lane, of the segment's sum
+                        const float2 y = __fadd2_rn(seg, make_float2(-c2.x, -c2.y));
                         const float2 tt = __fadd2_rn(s2, y);
                         const float2 lost = __fadd2_rn(tt, make_float2(-s2.x, -s2.y));
                         c2 = __fadd2_rn(lost, make_float2(-y.x, -y.y));
                         s2 = tt;
-                        if (d2.x < cut && j != self_j) lst[BLOCK * c++] = (unsigned short)j;
-                        if (d2.y < cut && j + 1 != self_j) lst[BLOCK * c++] = (unsigned short)(j + 1);
-                        if (c > kNbCapNb - 2) prune_nearest<BLOCK>(lst, c, st, p.x, p.y, p.z);
                     }
                 }
                 kahan_add(sum, comp, s2.x);
