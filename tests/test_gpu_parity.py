@@ -96,6 +96,37 @@ def test_pile_up_takes_the_global_path(sph, orc, gpu, stencil):
     assert fb[0] > 0 and fb[1] > 0
 
 
+@pytest.mark.parametrize("block", [256, 128])
+def test_long_segments_in_a_tile(sph, orc, gpu, block):
+    """A rod of particles one cell thick in y and z, at spacing h/3.5 (~31 per cell): each
+    particle's own 3-cell row segment holds ~90 candidates, more than the 32 candidate pairs of
+    one pair mask, while every chunk fits the shared-memory tile (the neighbour rows are
+    empty). The force pass then tests that segment itself instead of reading the density
+    pass's masks; results as elsewhere."""
+    p = sph.workload_params(lower=(0.0, 0.0, 0.0), upper=(3.6, 0.3, 0.3))
+    s = p.h / 3.5
+    lo = (0.01, 0.1015, 0.1015)  # y and z inside cell 5 (cell edge h (1 + 2^-10))
+    parts = sph.scene_fill(600 * 3 * 3, lo, (lo[0] + 600.5 * s, lo[1] + 3.2 * s, lo[2] + 3.2 * s), s,
+                           0.01 * p.h, 12)
+    edge = p.h * (1.0 + 2.0 ** -10)
+    c = np.floor(parts["pos"][:, :3].astype(np.float64) / edge).astype(np.int64)
+    assert np.all(c[:, 1] == 5) and np.all(c[:, 2] == 5)
+    occ = np.bincount(c[:, 0])
+    seg = occ[c[:, 0]] + occ[np.maximum(c[:, 0] - 1, 0)] * (c[:, 0] > 0) + \
+        np.append(occ, 0)[c[:, 0] + 1]
+    assert (seg > 64).mean() > 0.9  # candidates of the particle's own row segment
+    pp = p.copy()
+    pp.flags |= sph.FLAG_KEEP_FORCE
+    with sph.Sim(pp, n_max=len(parts)) as sim:
+        sim.set_launch(block, 1)
+        sim.upload(parts)
+        sim.step(1)
+        after = sim.download()
+        fb = sim.tile_stats()
+    check_step(orc, pp, parts, after)
+    assert fb == (0, 0), fb  # every chunk took the tile (and the masks)
+
+
 def test_upload_download_roundtrip(sph, gpu):
     sc = sph.reference_scene_10k(seed=2)
     a = sc.particles.copy()
