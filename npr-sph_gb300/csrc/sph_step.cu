@@ -404,9 +404,9 @@ __global__ void __launch_bounds__(BLOCK) k_force_integrate(const float4* __restr
     __shared__ TileShared<R, BLOCK> T;
     extern __shared__ float4 dyn_f[];
     float* base = reinterpret_cast<float*>(dyn_f);
-    // Stencil 1: [kNbCapForce][BLOCK] list entries (segment * 64 + candidate offset), then
-    // [kSegPerRow][BLOCK] global slots of the segments' first staged candidates. Stencil 2: the
-    // staged tile, then [kNbCapForce][BLOCK] list entries (staged indices).
+    // Stencil 1: [kNbCapForce][BLOCK] list entries (segment * 4096 + candidate offset), then
+    // [kSegPerRow][BLOCK] global slots of the segments' first candidates. Stencil 2: the staged
+    // tile, then [kNbCapForce][BLOCK] list entries (staged indices).
     const Staged st = kMask ? Staged{nullptr, nullptr, nullptr, nullptr}
                             : Staged{base, base + kCap, base + 2 * kCap, reinterpret_cast<int*>(base + 3 * kCap)};
     unsigned short* lst = reinterpret_cast<unsigned short*>(kMask ? base : base + 4 * kCap) + threadIdx.x;
@@ -425,25 +425,43 @@ __global__ void __launch_bounds__(BLOCK) k_force_integrate(const float4* __restr
             const float2 rp = rhop[t];
             const float cut = S.cut_d2, h = S.h;
             ForceAcc acc;
-            if (tiled) {
-                // The list keeps the particle itself too (force_comp.glsl:50-53 skips j == i):
-                // its offset and relative velocity are exactly zero, so its pressure term is
-                // skipped (d2 == 0) and its viscosity term adds exact zeros.
-                int cnt = 0;
-                if constexpr (kMask) {
-                    // Neighbours come from global memory: entry e is candidate (e & 63) of
-                    // segment e >> 6, whose first candidate is global slot seg_slot[segment].
-                    auto interact = [&](int g) {
-                        const float4 q = __ldg(pos_s + g);
-                        acc.add(p.x - q.x, p.y - q.y, p.z - q.z, h, rp.y, v, __ldg(rhop + g), __ldg(vel_s + g));
-                    };
-                    auto flush = [&]() {
-                        for (int k = 0; k < cnt; ++k) {
-                            const int e = lst[BLOCK * k];
-                            interact(seg_slot[BLOCK * (e >> 6)] + (e & 63));
+            // The list keeps the particle itself too (force_comp.glsl:50-53 skips j == i): its
+            // offset and relative velocity are exactly zero, so its pressure term is skipped
+            // (d2 == 0) and its viscosity term adds exact zeros.
+            int cnt = 0;
+            // Stencil 1: neighbours come from global memory. List entry e is candidate e & 4095 of
+            // row segment e >> 12, whose first candidate is global slot seg_slot[segment].
+            auto interact = [&](int g) {
+                const float4 q = __ldg(pos_s + g);
+                acc.add(p.x - q.x, p.y - q.y, p.z - q.z, h, rp.y, v, __ldg(rhop + g), __ldg(vel_s + g));
+            };
+            auto flush_slots = [&]() {
+                for (int k = 0; k < cnt; ++k) {
+                    const int e = lst[BLOCK * k];
+                    interact(seg_slot[BLOCK * (e >> 12)] + (e & 4095));
+                }
+                cnt = 0;
+            };
+            // Test candidates [g0, g1) of row segment r from global memory; the passing ones join
+            // the list (a candidate beyond 4095 of its segment, in a pile-up, interacts at once).
+            auto test_row = [&](int r, int g0, int g1) {
+                seg_slot[BLOCK * r] = g0;
+                for (int g = g0; g < g1; ++g) {
+                    const float4 q = __ldg(pos_s + g);
+                    float dx, dy, dz;
+                    const float d2 = canon_d2(p.x, p.y, p.z, q.x, q.y, q.z, dx, dy, dz);
+                    if (d2 < cut) {  // :57
+                        if (g - g0 < 4096) {
+                            lst[BLOCK * cnt++] = (unsigned short)(r * 4096 + (g - g0));
+                            if (cnt == kNbCapForce) flush_slots();
+                        } else {
+                            interact(g);
                         }
-                        cnt = 0;
-                    };
+                    }
+                }
+            };
+            if (tiled) {
+                if constexpr (kMask) {
                     // All masks are loaded up front (one coalesced word per segment and parity).
                     // Pair k of a segment's staged [a, b) is bit np-1-k of its masks when the
                     // segment has np <= 32 pairs; a longer segment lost its first bits and is
@@ -459,12 +477,7 @@ __global__ void __launch_bounds__(BLOCK) k_force_integrate(const float4* __restr
                         const int np = (b - a + 1) >> 1;
                         const int g0 = T.seg_gbeg[sg] + (a - T.seg_off[sg]);  // global slot of staged a
                         if (np > 32) {
-                            for (int g = g0; g < g0 + (b - a); ++g) {
-                                const float4 q = __ldg(pos_s + g);
-                                float dx, dy, dz;
-                                const float d2 = canon_d2(p.x, p.y, p.z, q.x, q.y, q.z, dx, dy, dz);
-                                if (d2 < cut) interact(g);  // :57
-                            }
+                            test_row(r, g0, g0 + (b - a));
                             continue;
                         }
                         seg_slot[BLOCK * r] = g0;
@@ -474,12 +487,12 @@ __global__ void __launch_bounds__(BLOCK) k_force_integrate(const float4* __restr
                             while (mk) {  // highest bit first: candidate order
                                 const int bit = 31 - __clz(mk);
                                 mk ^= 1u << bit;
-                                lst[BLOCK * cnt++] = (unsigned short)(r * 64 + 2 * (np - 1 - bit) + par);
-                                if (cnt == kNbCapForce) flush();
+                                lst[BLOCK * cnt++] = (unsigned short)(r * 4096 + 2 * (np - 1 - bit) + par);
+                                if (cnt == kNbCapForce) flush_slots();
                             }
                         }
                     }
-                    flush();
+                    flush_slots();
                 } else {
                     auto flush = [&]() {
                         for (int k = 0; k < cnt; ++k) {
@@ -510,14 +523,26 @@ __global__ void __launch_bounds__(BLOCK) k_force_integrate(const float4* __restr
                 const int gx = cell_coord(p.x, S.lo[0], S.inv_edge, S.dim[0]);
                 const int gy = cell_coord(p.y, S.lo[1], S.inv_edge, S.dim[1]);
                 const int gz = cell_coord(p.z, S.lo[2], S.inv_edge, S.dim[2]);
-                for_rows_global<R>(S, start, n, gx, gy, gz, [&](int a, int b) {
-                    for (int j = a; j < b; ++j) {
-                        const float4 o = __ldg(pos_s + j);
-                        float dx, dy, dz;
-                        const float d2 = canon_d2(p.x, p.y, p.z, o.x, o.y, o.z, dx, dy, dz);
-                        if (d2 < cut && j != t) acc.add(dx, dy, dz, h, rp.y, v, __ldg(rhop + j), __ldg(vel_s + j));
-                    }
-                });
+                if constexpr (kMask) {  // the same list, rows tested from global memory
+                    const int x0 = max(gx - 1, 0), x1 = min(gx + 1, S.dim[0] - 1);
+                    int r = 0;
+                    for (int z = max(gz - 1, 0); z <= min(gz + 1, S.dim[2] - 1); ++z)
+                        for (int y = max(gy - 1, 0); y <= min(gy + 1, S.dim[1] - 1); ++y, ++r) {
+                            const int row = S.cell_base + S.dim[0] * (y + S.dim[1] * z);
+                            test_row(r, max(__ldg(start + row + x0), 0), min(__ldg(start + row + x1 + 1), n));
+                        }
+                    flush_slots();
+                } else {
+                    for_rows_global<R>(S, start, n, gx, gy, gz, [&](int a, int b) {
+                        for (int j = a; j < b; ++j) {
+                            const float4 o = __ldg(pos_s + j);
+                            float dx, dy, dz;
+                            const float d2 = canon_d2(p.x, p.y, p.z, o.x, o.y, o.z, dx, dy, dz);
+                            if (d2 < cut && j != t)
+                                acc.add(dx, dy, dz, h, rp.y, v, __ldg(rhop + j), __ldg(vel_s + j));
+                        }
+                    });
+                }
             }
             // :63-66 F = f_p + mu*f_v + rho_i*G (constants folded into pres_c, visc_c)
             const float Fx = S.pres_c * acc.fp_xy.x + S.visc_c * acc.fv_xy.x + rp.x * S.g[0];
