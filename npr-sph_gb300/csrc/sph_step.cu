@@ -425,9 +425,9 @@ __global__ void __launch_bounds__(BLOCK) k_force_integrate(const float4* __restr
             const float2 rp = rhop[t];
             const float cut = S.cut_d2, h = S.h;
             ForceAcc acc;
-            // The list keeps the particle itself too (force_comp.glsl:50-53 skips j == i): its
-            // offset and relative velocity are exactly zero, so its pressure term is skipped
-            // (d2 == 0) and its viscosity term adds exact zeros.
+            // Stencil 2 keeps the particle itself in the list (force_comp.glsl:50-53 skips j == i):
+            // its offset and relative velocity are exactly zero, so its pressure term is skipped
+            // (d2 == 0) and its viscosity term adds zeros. Stencil 1 leaves it out.
             int cnt = 0;
             // Stencil 1: neighbours come from global memory. List entry e is candidate e & 4095 of
             // row segment e >> 12, whose first candidate is global slot seg_slot[segment].
@@ -450,7 +450,7 @@ __global__ void __launch_bounds__(BLOCK) k_force_integrate(const float4* __restr
                     const float4 q = __ldg(pos_s + g);
                     float dx, dy, dz;
                     const float d2 = canon_d2(p.x, p.y, p.z, q.x, q.y, q.z, dx, dy, dz);
-                    if (d2 < cut) {  // :57
+                    if (d2 < cut && g != t) {  // :50-57
                         if (g - g0 < 4096) {
                             lst[BLOCK * cnt++] = (unsigned short)(r * 4096 + (g - g0));
                             if (cnt == kNbCapForce) flush_slots();
@@ -481,6 +481,14 @@ __global__ void __launch_bounds__(BLOCK) k_force_integrate(const float4* __restr
                             continue;
                         }
                         seg_slot[BLOCK * r] = g0;
+                        if (r == R * G::kSide + R) {  // the particle's own row: drop its own bit (j == i)
+                            const int o = t - g0;    // in [0, 2 np): the row holds the particle's cell
+                            if (o >= 0 && o < 2 * np) {
+                                const uint32_t bit = 1u << (np - 1 - (o >> 1));
+                                m[2 * r] &= (o & 1) ? ~0u : ~bit;
+                                m[2 * r + 1] &= (o & 1) ? ~bit : ~0u;
+                            }
+                        }
 #pragma unroll
                         for (int par = 0; par < 2; ++par) {
                             uint32_t mk = m[2 * r + par];
