@@ -38,6 +38,10 @@ struct sph_ctx {
     int* scene_first_dev = nullptr;
     bool timing = false;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // host uploads/downloads: record chunks copied on their own stream while the next (or the
+    // previous) chunk is converted on `stream`
+    cudaStream_t xfer = nullptr;
+    cudaEvent_t xev[sphgb::kXferChunks + 1] = {};
     float pass_ms[3] = {0, 0, 0};
     uint32_t* q_ids = nullptr;
     uint32_t* q_cnt = nullptr;

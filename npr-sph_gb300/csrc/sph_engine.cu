@@ -307,6 +307,9 @@ sph_status create_impl(const sph_params* params, const uint32_t* counts, uint32_
         return bail(SPH_ERR_CUDA);
     for (auto& e : ctx->ev)
         if (cudaEventCreate(&e) != cudaSuccess) return bail(SPH_ERR_CUDA);
+    if (cudaStreamCreateWithFlags(&ctx->xfer, cudaStreamNonBlocking) != cudaSuccess) return bail(SPH_ERR_CUDA);
+    for (auto& e : ctx->xev)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return bail(SPH_ERR_CUDA);
     b.n = 0;
     st = rebuild_geometry(ctx);
     if (st) return bail(st);
@@ -314,6 +317,11 @@ sph_status create_impl(const sph_params* params, const uint32_t* counts, uint32_
     return SPH_OK;
     GUARD_END
 }
+
+// Chunks of a host transfer of n records: a few for large transfers, so that the copy of one chunk
+// overlaps the conversion of another.
+static int xfer_chunks(uint32_t n) { return n >= (uint32_t)kXferChunks * 65536u ? kXferChunks : 1; }
+static uint32_t chunk_begin(uint32_t n, int k, int chunks) { return (uint32_t)((uint64_t)n * k / chunks); }
 
 sph_status upload_common(sph_ctx* ctx, const sph_particle* src, uint32_t n, bool host) {
     if (!ctx) return SPH_ERR_INVALID_ARG;
@@ -326,12 +334,7 @@ sph_status upload_common(sph_ctx* ctx, const sph_particle* src, uint32_t n, bool
     }
     GUARD_BEGIN
     CK(cudaSetDevice(ctx->device));
-    const sph_particle* dev = src;
-    if (host) {
-        if (!ctx->b.aos) CK(dalloc(&ctx->b.aos, ctx->n_max));
-        CK(cudaMemcpyAsync(ctx->b.aos, src, sizeof(sph_particle) * n, cudaMemcpyHostToDevice, ctx->stream));
-        dev = ctx->b.aos;
-    }
+    if (host && !ctx->b.aos) CK(dalloc(&ctx->b.aos, ctx->n_max));
     if (!ctx->batched && (int)n != ctx->b.n) {
         ctx->counts[0] = n;
         ctx->b.n = (int)n;
@@ -339,7 +342,23 @@ sph_status upload_common(sph_ctx* ctx, const sph_particle* src, uint32_t n, bool
         if (st) return st;
     }
     ctx->b.n = (int)n;
-    launch_aos_to_soa(ctx->b, dev, ctx->scene_first_dev, ctx->stream);
+    const int chunks = xfer_chunks(n);
+    if (host) {
+        // The records are copied on the transfer stream, chunk by chunk; each chunk is converted
+        // on the context's stream once its copy has landed, while the next one is copied.
+        CK(cudaEventRecord(ctx->xev[kXferChunks], ctx->stream));  // earlier users of the staging buffer
+        CK(cudaStreamWaitEvent(ctx->xfer, ctx->xev[kXferChunks], 0));
+        for (int k = 0; k < chunks; ++k) {
+            const uint32_t i0 = chunk_begin(n, k, chunks), i1 = chunk_begin(n, k + 1, chunks);
+            CK(cudaMemcpyAsync(ctx->b.aos + i0, src + i0, sizeof(sph_particle) * (i1 - i0), cudaMemcpyHostToDevice,
+                               ctx->xfer));
+            CK(cudaEventRecord(ctx->xev[k], ctx->xfer));
+            CK(cudaStreamWaitEvent(ctx->stream, ctx->xev[k], 0));
+            launch_aos_to_soa(ctx->b, ctx->b.aos, ctx->scene_first_dev, (int)i0, (int)i1, ctx->stream);
+        }
+    } else {
+        launch_aos_to_soa(ctx->b, src, ctx->scene_first_dev, 0, (int)n, ctx->stream);
+    }
     CK(cudaMemsetAsync(ctx->b.count, 0, sizeof(int) * (size_t)ctx->b.ncell, ctx->stream));
     CK(cudaGetLastError());
     ctx->have_state = true;
@@ -348,7 +367,8 @@ sph_status upload_common(sph_ctx* ctx, const sph_particle* src, uint32_t n, bool
     ctx->steps = 0;
     ctx->judge_failures = 0;
     ctx->judge_backoff = 0;
-    if (host) CK(cudaStreamSynchronize(ctx->stream));  // caller may reuse its buffer on return
+    // The caller may reuse its buffer on return: wait for the copies (the conversion runs on).
+    if (host) CK(cudaEventSynchronize(ctx->xev[chunks - 1]));
     return SPH_OK;
     GUARD_END
 }
@@ -360,16 +380,28 @@ sph_status download_common(sph_ctx* ctx, sph_particle* dst, uint32_t n, bool hos
     if ((int)n != ctx->b.n) return fail(ctx, SPH_ERR_INVALID_ARG, "n must equal the uploaded particle count");
     GUARD_BEGIN
     CK(cudaSetDevice(ctx->device));
-    sph_particle* dev = dst;
+    const bool keep = (ctx->params[0].flags & SPH_FLAG_KEEP_FORCE) && ctx->stepped;
     if (host) {
         if (!ctx->b.aos) CK(dalloc(&ctx->b.aos, ctx->n_max));
-        dev = ctx->b.aos;
+        // Records are assembled by particle id, chunk by chunk, and each chunk is copied to the
+        // host on the transfer stream while the next one is assembled.
+        launch_slot_of_state_id(ctx->b, ctx->stream);
+        const int chunks = xfer_chunks(n);
+        for (int k = 0; k < chunks; ++k) {
+            const uint32_t i0 = chunk_begin(n, k, chunks), i1 = chunk_begin(n, k + 1, chunks);
+            launch_soa_to_aos_ids(ctx->b, keep, ctx->b.aos, (int)i0, (int)i1, ctx->stream);
+            CK(cudaEventRecord(ctx->xev[k], ctx->stream));
+            CK(cudaStreamWaitEvent(ctx->xfer, ctx->xev[k], 0));
+            CK(cudaMemcpyAsync(dst + i0, ctx->b.aos + i0, sizeof(sph_particle) * (i1 - i0), cudaMemcpyDeviceToHost,
+                               ctx->xfer));
+        }
+        CK(cudaEventRecord(ctx->xev[kXferChunks], ctx->xfer));
+        CK(cudaStreamWaitEvent(ctx->stream, ctx->xev[kXferChunks], 0));  // later users of the staging buffer
+    } else {
+        launch_soa_to_aos(ctx->b, keep, dst, ctx->stream);
     }
-    const bool keep = (ctx->params[0].flags & SPH_FLAG_KEEP_FORCE) && ctx->stepped;
-    launch_soa_to_aos(ctx->b, keep, dev, ctx->stream);
     CK(cudaGetLastError());
-    if (host) CK(cudaMemcpyAsync(dst, ctx->b.aos, sizeof(sph_particle) * n, cudaMemcpyDeviceToHost, ctx->stream));
-    return check_device_error(ctx);  // synchronises
+    return check_device_error(ctx);  // synchronises the context's stream, which waits for the copies
     GUARD_END
 }
 
@@ -436,6 +468,7 @@ sph_status sph_destroy(sph_ctx* ctx) {
     if (!ctx) return SPH_ERR_INVALID_ARG;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->xfer) cudaStreamSynchronize(ctx->xfer);
     free_graph(ctx);
     Buffers& b = ctx->b;
     void* ptrs[] = {b.pos, b.vel, b.pos_s, b.vel_s, b.rhop, b.force_s, b.force_up, b.aux, b.aos, b.key, b.rank,
@@ -445,6 +478,9 @@ sph_status sph_destroy(sph_ctx* ctx) {
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (auto& e : ctx->ev)
+        if (e) cudaEventDestroy(e);
+    if (ctx->xfer) cudaStreamDestroy(ctx->xfer);
+    for (auto& e : ctx->xev)
         if (e) cudaEventDestroy(e);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;

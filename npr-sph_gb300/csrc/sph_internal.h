@@ -123,8 +123,16 @@ constexpr int kDiagFields = 12;
 void launch_reduce(const Buffers& b, const SceneDev* host_scenes, int nscene, double* out_dev,
                    cudaStream_t st);
 size_t reduce_partials_doubles(int nscene);
-void launch_aos_to_soa(const Buffers& b, const sph_particle* aos_dev, const int* scene_first, cudaStream_t st);
+// Records [i0, i1) of aos_dev into the state (record i becomes slot i, particle id i).
+void launch_aos_to_soa(const Buffers& b, const sph_particle* aos_dev, const int* scene_first, int i0, int i1,
+                       cudaStream_t st);
 void launch_soa_to_aos(const Buffers& b, bool force_from_step, sph_particle* aos_dev, cudaStream_t st);
+// The same records by particle id: slot_of_id from the state's ids, then records [i0, i1).
+void launch_slot_of_state_id(const Buffers& b, cudaStream_t st);
+void launch_soa_to_aos_ids(const Buffers& b, bool force_from_step, sph_particle* aos_dev, int i0, int i1,
+                           cudaStream_t st);
+// Chunks of a host upload or download (copies overlap the conversion of the other chunks).
+constexpr int kXferChunks = 4;
 
 int device_sm_count();
 

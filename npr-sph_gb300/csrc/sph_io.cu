@@ -30,12 +30,12 @@ __device__ __forceinline__ int scene_lookup(const int* __restrict__ scene_first,
     return lo;
 }
 
-__global__ void __launch_bounds__(kThreads) k_aos_to_soa(const sph_particle* __restrict__ aos, int n,
+__global__ void __launch_bounds__(kThreads) k_aos_to_soa(const sph_particle* __restrict__ aos, int i0, int i1,
                                                          const int* __restrict__ scene_first, int nscene,
                                                          float4* __restrict__ pos, float4* __restrict__ vel,
                                                          float2* __restrict__ rhop, float4* __restrict__ force_up,
                                                          float4* __restrict__ aux) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (int i = i0 + blockIdx.x * blockDim.x + threadIdx.x; i < i1; i += gridDim.x * blockDim.x) {
         const sph_particle& r = aos[i];
         float4 p = ld4(r.pos), v = ld4(r.vel), f = ld4(r.force), e = ld4(r.extras);
         int sc = nscene > 1 ? scene_lookup(scene_first, nscene, i) : 0;
@@ -62,6 +62,38 @@ __global__ void __launch_bounds__(kThreads) k_soa_to_aos(const float4* __restric
         float4 x = aux[id];
         float4 fu = force_up[id];
         float4 f = force_s ? make_float4(force_s[s].x, force_s[s].y, force_s[s].z, fu.w) : fu;
+        sph_particle& r = aos[id];
+        st4(r.pos, make_float4(p.x, p.y, p.z, x.x));
+        st4(r.vel, make_float4(v.x, v.y, v.z, x.y));
+        st4(r.force, f);
+        st4(r.extras, make_float4(rp.x, rp.y, x.z, x.w));
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_slot_of_state_id(const float4* __restrict__ vel, int n,
+                                                               int* __restrict__ slot_of_id) {
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+        const int id = id_of(vel[s]);
+        if (id >= 0 && id < n) slot_of_id[id] = s;
+    }
+}
+
+// k_soa_to_aos by record: record i from the slot holding particle id i.
+__global__ void __launch_bounds__(kThreads) k_soa_to_aos_ids(const float4* __restrict__ pos, const float4* __restrict__ vel,
+                                                             const float2* __restrict__ rhop,
+                                                             const float4* __restrict__ force_s,
+                                                             const float4* __restrict__ force_up,
+                                                             const float4* __restrict__ aux,
+                                                             const int* __restrict__ slot_of_id, int n, int i0, int i1,
+                                                             sph_particle* __restrict__ aos) {
+    for (int id = i0 + blockIdx.x * blockDim.x + threadIdx.x; id < i1; id += gridDim.x * blockDim.x) {
+        const int s = slot_of_id[id];
+        if (s < 0 || s >= n) continue;
+        const float4 p = pos[s], v = vel[s];
+        const float2 rp = rhop[s];
+        const float4 x = aux[id];
+        const float4 fu = force_up[id];
+        const float4 f = force_s ? make_float4(force_s[s].x, force_s[s].y, force_s[s].z, fu.w) : fu;
         sph_particle& r = aos[id];
         st4(r.pos, make_float4(p.x, p.y, p.z, x.x));
         st4(r.vel, make_float4(v.x, v.y, v.z, x.y));
@@ -146,11 +178,25 @@ __global__ void __launch_bounds__(kThreads) k_reduce_final(const double* __restr
 
 }  // namespace
 
-void launch_aos_to_soa(const Buffers& b, const sph_particle* aos_dev, const int* scene_first, cudaStream_t st) {
+void launch_aos_to_soa(const Buffers& b, const sph_particle* aos_dev, const int* scene_first, int i0, int i1,
+                       cudaStream_t st) {
+    if (i1 <= i0) return;
+    int blocks = (i1 - i0 + kThreads - 1) / kThreads;
+    k_aos_to_soa<<<blocks, kThreads, 0, st>>>(aos_dev, i0, i1, scene_first, b.nscene, b.pos, b.vel, b.rhop,
+                                              b.force_up, b.aux);
+}
+
+void launch_slot_of_state_id(const Buffers& b, cudaStream_t st) {
     if (b.n <= 0) return;
-    int blocks = (b.n + kThreads - 1) / kThreads;
-    k_aos_to_soa<<<blocks, kThreads, 0, st>>>(aos_dev, b.n, scene_first, b.nscene, b.pos, b.vel, b.rhop, b.force_up,
-                                              b.aux);
+    k_slot_of_state_id<<<(b.n + kThreads - 1) / kThreads, kThreads, 0, st>>>(b.vel, b.n, b.slot_of_id);
+}
+
+void launch_soa_to_aos_ids(const Buffers& b, bool force_from_step, sph_particle* aos_dev, int i0, int i1,
+                           cudaStream_t st) {
+    if (i1 <= i0) return;
+    int blocks = (i1 - i0 + kThreads - 1) / kThreads;
+    k_soa_to_aos_ids<<<blocks, kThreads, 0, st>>>(b.pos, b.vel, b.rhop, force_from_step ? b.force_s : nullptr,
+                                                  b.force_up, b.aux, b.slot_of_id, b.n, i0, i1, aos_dev);
 }
 
 void launch_soa_to_aos(const Buffers& b, bool force_from_step, sph_particle* aos_dev, cudaStream_t st) {
