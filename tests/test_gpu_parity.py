@@ -147,6 +147,39 @@ def test_upload_download_roundtrip(sph, gpu):
         np.testing.assert_array_equal(c["force"], a["force"])  # KEEP_FORCE off
 
 
+def test_chunked_host_transfers(sph, gpu):
+    """Host uploads and downloads of more than 4 x 65,536 records move in four uneven chunks on a
+    transfer stream (records assembled by particle id); device-buffer transfers take one pass by
+    slot. Both give the same bytes, before and after steps, with and without kept forces."""
+    import torch
+
+    p = sph.workload_params(lower=(0.0, 0.0, 0.0), upper=(1.6, 1.6, 1.6))
+    n = 4 * 65536 + 3
+    parts = sph.scene_fill(n, (0.02, 0.02, 0.02), (1.58, 1.0, 1.58), 0.5 * p.h, 0.01 * p.h, 21)
+    rng = np.random.default_rng(4)
+    parts["vel"][:, :3] = rng.normal(0.0, 0.2, (n, 3)).astype(np.float32)
+    parts["vel"][:, 3] = rng.normal(size=n).astype(np.float32)
+    parts["force"] = rng.normal(size=(n, 4)).astype(np.float32)
+    parts["extras"][:, 2:] = rng.normal(size=(n, 2)).astype(np.float32)
+    for flags in (0, sph.FLAG_KEEP_FORCE):
+        pp = p.copy()
+        pp.flags |= flags
+        with sph.Sim(pp, n_max=n) as sim:
+            sim.upload(parts)
+            np.testing.assert_array_equal(sim.download().view(np.uint8), parts.view(np.uint8))
+            dev = torch.empty(n * 64, dtype=torch.uint8, device=gpu)
+            for steps in (1, 3):
+                sim.step(steps)
+                host = sim.download()
+                sim.download_device(dev.data_ptr(), n)
+                sim.synchronize()
+                np.testing.assert_array_equal(host.view(np.uint8), dev.cpu().numpy())
+            sim.upload(host)  # a chunked upload of the stepped records, then one more step
+            sim.step(1)
+            again = sim.download()
+            assert np.isfinite(again["pos"][:, :3]).all()
+
+
 def test_device_aos_buffers(sph, gpu):
     import torch
 
