@@ -30,9 +30,11 @@
 // (the same segments and staged offsets, without staging positions), decodes
 // the masks into a per-thread list in shared memory and reads the neighbours'
 // position, velocity and (rho, p) from global memory. Without a staged tile it
-// needs ~20 KB of shared memory per CTA of 128 instead of ~40, so twice the
-// warps hide the gathers' latency and L1 has room for them. A segment longer
-// than 32 pairs (a pile-up) is tested by the force pass itself.
+// needs ~37 KB of shared memory per CTA of 256 (~20 per CTA of 128) instead of
+// ~80, so more warps hide the gathers' latency and L1 has room for them. A
+// segment longer than 32 pairs (a pile-up) is tested by the force pass itself,
+// and so is every segment of a chunk on the global-memory path; the particle's
+// own bit is dropped (force_comp.glsl:50 skips j == i).
 //
 // Force processes its list in a second loop in which all lanes are busy: with
 // ~15% of candidates inside r < h, testing and interacting in one loop would
@@ -63,15 +65,15 @@ namespace sphgb {
 
 namespace {
 
-// BLOCK threads per CTA = target particles per chunk (128 or 256, autotuned).
+// BLOCK threads per CTA = target particles per chunk (256 by default, or 128; autotuned).
 // A chunk stages about (2R+1)^2 * (BLOCK + 2R * cell occupancy * rows in the chunk)
 // candidates: at most 9.6 * BLOCK (mean 9.4) over the chunks of the 1M dam break's 0.5h
 // lattice, its densest state. 12 * BLOCK leaves room for compression and for chunks that
-// straddle rows, and keeps the tiles small enough for 9 density / 5 force CTAs of 128 per SM;
-// a chunk that needs more takes the global-memory path.
+// straddle rows, and keeps the density tile small enough for 5 CTAs of 256 per SM (10 or 11 *
+// BLOCK sends many more chunks to the global-memory path); a chunk that needs more takes it.
 // With R = 2 (cells of h/2, 25 neighbour rows) a chunk stages ~26 * BLOCK.
 template <int R, int BLOCK> constexpr int stage_cap() { return (R == 1 ? 12 : 30) * BLOCK; }
-constexpr int kNbCapForce = 48;         // force list entries per thread (staged index, u16)
+constexpr int kNbCapForce = 48;         // force list entries per thread (u16)
 constexpr int kNbCapNb = 42;            // neighbour-list pass entries per thread (u16): three CTAs of
                                         // 256 per SM with the staged tile
 constexpr float kSentinel = 1e30f;      // staged padding: its distance to any particle is +inf
