@@ -172,6 +172,13 @@ sph_status sph_pass_times(sph_ctx* ctx, float out_ms[3]);
  * New (no reference counterpart): the check that the grid loses no pair. */
 sph_status sph_neighbor_digest(sph_ctx* ctx, const uint32_t* query_ids, uint32_t n_query,
                                int32_t brute_force, uint32_t* count_out, uint64_t* digest_out);
+/* One plain step (as sph_step(ctx, 1), launched without the graph) that also reports, for the
+ * query particles, the neighbour sets its force pass used -- with stencil 1 they are decoded
+ * from the density pass's masks -- as count (self included) and digest, to compare with
+ * sph_neighbor_digest on the positions before the step. Stencil 1 only (SPH_ERR_UNSUPPORTED
+ * otherwise). New (no reference counterpart): the check that the force pass loses no pair. */
+sph_status sph_step_neighbor_digest(sph_ctx* ctx, const uint32_t* query_ids, uint32_t n_query,
+                                    uint32_t* count_out, uint64_t* digest_out);
 
 /* ---- batched scenes (new; no reference counterpart) --------------------
  * n_scene independent boxes, each with its own sph_params and particle count,

@@ -47,6 +47,9 @@ struct sph_ctx {
     uint32_t* q_cnt = nullptr;
     unsigned long long* q_dig = nullptr;
     int q_cap = 0;
+    // sph_step_neighbor_digest: the force pass's neighbour counts and digests per sorted slot
+    uint32_t* fd_cnt = nullptr;
+    unsigned long long* fd_sum = nullptr;
     // static obstacle (sph_set_obstacle): signed distance samples on the device, or null
     float* sdf_dev = nullptr;
     int sdf_dims[3] = {0, 0, 0};

@@ -474,6 +474,7 @@ sph_status sph_destroy(sph_ctx* ctx) {
     void* ptrs[] = {b.pos, b.vel, b.pos_s, b.vel_s, b.rhop, b.force_s, b.force_up, b.aux, b.aos, b.key, b.rank,
                     b.perm, b.count, b.start, b.scan_state, b.slot_of_id, b.err, b.partials,
                     b.scenes, b.tile_stats, b.pmask, ctx->diag_dev, ctx->scene_first_dev, ctx->q_ids, ctx->q_cnt, ctx->q_dig,
+                    ctx->fd_cnt, ctx->fd_sum,
                     ctx->render_buf, ctx->sdf_dev};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -661,6 +662,50 @@ sph_status sph_neighbor_digest(sph_ctx* ctx, const uint32_t* query_ids, uint32_t
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(count_out, ctx->q_cnt, sizeof(uint32_t) * n_query, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaMemcpyAsync(digest_out, ctx->q_dig, sizeof(uint64_t) * n_query, cudaMemcpyDeviceToHost, ctx->stream));
+    return check_device_error(ctx);
+    GUARD_END
+}
+
+sph_status sph_step_neighbor_digest(sph_ctx* ctx, const uint32_t* query_ids, uint32_t n_query, uint32_t* count_out,
+                                    uint64_t* digest_out) {
+    if (!ctx) return SPH_ERR_INVALID_ARG;
+    if (n_query && (!query_ids || !count_out || !digest_out)) return fail(ctx, SPH_ERR_INVALID_ARG, "null pointer");
+    if (!ctx->have_state) return fail(ctx, SPH_ERR_NOT_READY, "no particles uploaded");
+    if (ctx->cfg.stencil != 1)
+        return fail(ctx, SPH_ERR_UNSUPPORTED, "the force pass reads neighbour masks with stencil 1 only");
+    GUARD_BEGIN
+    CK(cudaSetDevice(ctx->device));
+    if ((int)n_query > ctx->q_cap) {
+        cudaFree(ctx->q_ids); cudaFree(ctx->q_cnt); cudaFree(ctx->q_dig);
+        ctx->q_ids = nullptr; ctx->q_cnt = nullptr; ctx->q_dig = nullptr;
+        ctx->q_cap = 0;
+        CK(dalloc(&ctx->q_ids, n_query));
+        CK(dalloc(&ctx->q_cnt, n_query));
+        CK(dalloc(&ctx->q_dig, n_query));
+        ctx->q_cap = (int)n_query;
+    }
+    if (!ctx->fd_cnt) CK(dalloc(&ctx->fd_cnt, ctx->n_max));
+    if (!ctx->fd_sum) CK(dalloc(&ctx->fd_sum, ctx->n_max));
+    if (ctx->need_hash) {
+        launch_hash(ctx->b, ctx->s0, ctx->batched, ctx->stream);
+        ctx->need_hash = false;
+    }
+    enqueue_sort(ctx);
+    launch_density(ctx->b, ctx->s0, ctx->batched, ctx->cfg, ctx->stream);
+    launch_force_integrate(ctx->b, ctx->s0, ctx->batched, ctx->cfg, ctx->stream, ctx->fd_cnt, ctx->fd_sum);
+    launch_slot_of_id(ctx->b, ctx->stream);  // id -> slot of the step's sorted state
+    if (n_query) {
+        CK(cudaMemcpyAsync(ctx->q_ids, query_ids, sizeof(uint32_t) * n_query, cudaMemcpyHostToDevice, ctx->stream));
+        launch_query_gather(ctx->b, ctx->q_ids, (int)n_query, ctx->fd_cnt, ctx->fd_sum, ctx->q_cnt, ctx->q_dig,
+                            ctx->stream);
+    }
+    CK(cudaGetLastError());
+    ctx->steps += 1;
+    ctx->stepped = true;
+    if (n_query) {
+        CK(cudaMemcpyAsync(count_out, ctx->q_cnt, sizeof(uint32_t) * n_query, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(digest_out, ctx->q_dig, sizeof(uint64_t) * n_query, cudaMemcpyDeviceToHost, ctx->stream));
+    }
     return check_device_error(ctx);
     GUARD_END
 }

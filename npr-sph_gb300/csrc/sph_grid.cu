@@ -176,6 +176,19 @@ __global__ void __launch_bounds__(kThreads) k_slot_of_id(const float4* __restric
     }
 }
 
+__global__ void __launch_bounds__(kThreads) k_query_gather(const int* __restrict__ slot_of_id,
+                                                           const uint32_t* __restrict__ qids, int nq, int n,
+                                                           const uint32_t* __restrict__ src_cnt,
+                                                           const unsigned long long* __restrict__ src_sum,
+                                                           uint32_t* __restrict__ cnt, unsigned long long* __restrict__ dig) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nq) return;
+    const int qi = (int)qids[q];
+    const int t = qi >= 0 && qi < n ? slot_of_id[qi] : -1;
+    cnt[q] = t >= 0 && t < n ? src_cnt[t] : 0xffffffffu;
+    dig[q] = t >= 0 && t < n ? src_sum[t] : 0ull;
+}
+
 // Neighbour count + digest over the grid (the same stencil walk as the step).
 template <bool BATCHED>
 __global__ void __launch_bounds__(kThreads) k_digest_grid(const float4* __restrict__ pos_s, const float4* __restrict__ vel_s,
@@ -318,6 +331,13 @@ void launch_scatter(const Buffers& b, cudaStream_t st) {
 void launch_gather(const Buffers& b, cudaStream_t st) {
     if (b.n <= 0) return;
     k_gather<<<grid_for(b.n), kThreads, 0, st>>>(b.perm, b.key, b.start, b.pos, b.vel, b.pos_s, b.vel_s, b.n, b.err);
+}
+
+void launch_query_gather(const Buffers& b, const uint32_t* qids, int nq, const uint32_t* src_cnt,
+                         const unsigned long long* src_sum, uint32_t* cnt, unsigned long long* dig, cudaStream_t st) {
+    if (nq <= 0) return;
+    k_query_gather<<<(nq + kThreads - 1) / kThreads, kThreads, 0, st>>>(b.slot_of_id, qids, nq, b.n, src_cnt, src_sum,
+                                                                         cnt, dig);
 }
 
 void launch_slot_of_id(const Buffers& b, cudaStream_t st) {

@@ -102,13 +102,19 @@ void launch_slot_of_id(const Buffers& b, cudaStream_t st);
 void launch_neighbor_digest(const Buffers& b, const SceneDev& s0, bool batched, int stencil,
                             const uint32_t* qids, int nq, int brute, uint32_t* cnt,
                             unsigned long long* dig, cudaStream_t st);
+// Per query id: cnt[q] = src_cnt[slot_of_id[id]], dig[q] = src_sum[...] (0xffffffff / 0 for a
+// bad id).
+void launch_query_gather(const Buffers& b, const uint32_t* qids, int nq, const uint32_t* src_cnt,
+                         const unsigned long long* src_sum, uint32_t* cnt, unsigned long long* dig, cudaStream_t st);
 // ---- launchers (sph_step.cu) ----
 // Kernel attributes (shared-memory opt-in); called once per process before any capture.
 void init_step_kernels();
 void launch_density(const Buffers& b, const SceneDev& s0, bool batched, const LaunchCfg& c,
                     cudaStream_t st);
+// With dig_cnt/dig_sum (per sorted slot; stencil 1 only), the force pass also reports the
+// neighbour set it used: count (self included) and digest sum mix64(id).
 void launch_force_integrate(const Buffers& b, const SceneDev& s0, bool batched, const LaunchCfg& c,
-                            cudaStream_t st);
+                            cudaStream_t st, uint32_t* dig_cnt = nullptr, unsigned long long* dig_sum = nullptr);
 // Density (bit-identical to launch_density) plus, per particle, the kNbList nearest neighbours
 // j != i with r < h as sorted slots into nb[n][kNbList] (-1 padded) and their number in cnt
 // (the learned macro-step's input), with the launch shape of launch_density.

@@ -391,7 +391,9 @@ struct ForceAcc {
     }
 };
 
-template <bool BATCHED, int R, int BLOCK>
+// DIGEST (stencil 1): also the count (self included) and the digest sum mix64(id) of the
+// neighbours each particle interacted with, per sorted slot, as sph_neighbor_digest reports them.
+template <bool BATCHED, int R, int BLOCK, bool DIGEST = false>
 __global__ void __launch_bounds__(BLOCK) k_force_integrate(const float4* __restrict__ pos_s, const float4* __restrict__ vel_s,
                                                            const float2* __restrict__ rhop, const int* __restrict__ start,
                                                            SceneDev s0, const SceneDev* __restrict__ scenes, int nscene,
@@ -399,10 +401,12 @@ __global__ void __launch_bounds__(BLOCK) k_force_integrate(const float4* __restr
                                                            float4* __restrict__ force_out, int* __restrict__ key_out,
                                                            int* __restrict__ rank_out, int* __restrict__ count,
                                                            const uint32_t* __restrict__ pmask, int n,
-                                                           uint32_t* __restrict__ stats) {
+                                                           uint32_t* __restrict__ stats, uint32_t* __restrict__ dig_cnt,
+                                                           unsigned long long* __restrict__ dig_sum) {
     using G = TileGeom<R>;
     constexpr int kCap = stage_cap<R, BLOCK>();
     constexpr bool kMask = R == 1;  // the density pass's pair masks replace the candidate tests
+    static_assert(!DIGEST || kMask, "the neighbour digest of the force pass is for stencil 1");
     __shared__ TileShared<R, BLOCK> T;
     extern __shared__ float4 dyn_f[];
     float* base = reinterpret_cast<float*>(dyn_f);
@@ -431,11 +435,18 @@ __global__ void __launch_bounds__(BLOCK) k_force_integrate(const float4* __restr
             // its offset and relative velocity are exactly zero, so its pressure term is skipped
             // (d2 == 0) and its viscosity term adds zeros. Stencil 1 leaves it out.
             int cnt = 0;
+            uint32_t dcount = 1;                                                 // DIGEST: self
+            unsigned long long dsum = mix64((unsigned long long)id_of(v));
             // Stencil 1: neighbours come from global memory. List entry e is candidate e & 4095 of
             // row segment e >> 12, whose first candidate is global slot seg_slot[segment].
             auto interact = [&](int g) {
                 const float4 q = __ldg(pos_s + g);
-                acc.add(p.x - q.x, p.y - q.y, p.z - q.z, h, rp.y, v, __ldg(rhop + g), __ldg(vel_s + g));
+                const float4 vj = __ldg(vel_s + g);
+                acc.add(p.x - q.x, p.y - q.y, p.z - q.z, h, rp.y, v, __ldg(rhop + g), vj);
+                if constexpr (DIGEST) {
+                    ++dcount;
+                    dsum += mix64((unsigned long long)id_of(vj));
+                }
             };
             auto flush_slots = [&]() {
                 for (int k = 0; k < cnt; ++k) {
@@ -569,6 +580,10 @@ __global__ void __launch_bounds__(BLOCK) k_force_integrate(const float4* __restr
             }
             pos_out[t] = make_float4(np[0], np[1], np[2], p.w);
             vel_out[t] = make_float4(nv[0], nv[1], nv[2], v.w);
+            if constexpr (DIGEST) {
+                dig_cnt[t] = dcount;
+                dig_sum[t] = dsum;
+            }
             if (force_out) force_out[t] = make_float4(Fx, Fy, Fz, 0.0f);
             // Hash of the new position: the next step's sort starts from here (with an obstacle,
             // k_obstacle_hash hashes after moving the particles out of it).
@@ -744,12 +759,21 @@ void density_impl(const Buffers& b, const SceneDev& s0, cudaStream_t st) {
 }
 
 template <bool B, int R, int BLOCK>
-void force_impl(const Buffers& b, const SceneDev& s0, float4* force_out, cudaStream_t st) {
-    auto k = k_force_integrate<B, R, BLOCK>;
+void force_impl(const Buffers& b, const SceneDev& s0, float4* force_out, uint32_t* dig_cnt,
+                unsigned long long* dig_sum, cudaStream_t st) {
     constexpr size_t sm = force_smem<R, BLOCK>();
-    k<<<grid_size(k, BLOCK, sm, b.n), BLOCK, sm, st>>>(b.pos_s, b.vel_s, b.rhop, b.start, s0, b.scenes, b.nscene,
-                                                       b.pos, b.vel, force_out, s0.sdf ? nullptr : b.key, b.rank,
-                                                       b.count, b.pmask, b.n, b.tile_stats);
+    auto launch = [&](auto k) {
+        k<<<grid_size(k, BLOCK, sm, b.n), BLOCK, sm, st>>>(b.pos_s, b.vel_s, b.rhop, b.start, s0, b.scenes, b.nscene,
+                                                           b.pos, b.vel, force_out, s0.sdf ? nullptr : b.key, b.rank,
+                                                           b.count, b.pmask, b.n, b.tile_stats, dig_cnt, dig_sum);
+    };
+    if constexpr (R == 1) {
+        if (dig_cnt) {
+            launch(k_force_integrate<B, R, BLOCK, true>);
+            return;
+        }
+    }
+    launch(k_force_integrate<B, R, BLOCK>);
 }
 
 // The static obstacle's rule (sph_set_obstacle) on the integrated state, then the cell hash of
@@ -791,6 +815,9 @@ void set_attrs() {
                          (int)density_smem<R, BLOCK>());
     cudaFuncSetAttribute(k_force_integrate<B, R, BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)force_smem<R, BLOCK>());
+    if constexpr (R == 1)
+        cudaFuncSetAttribute(k_force_integrate<B, R, BLOCK, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)force_smem<R, BLOCK>());
     cudaFuncSetAttribute(k_density_nb<B, R, BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)nb_smem<R, BLOCK>());
 }
@@ -828,13 +855,15 @@ void launch_density(const Buffers& b, const SceneDev& s0, bool batched, const La
 }
 
 void launch_force_integrate(const Buffers& b, const SceneDev& s0, bool batched, const LaunchCfg& c,
-                            cudaStream_t st) {
+                            cudaStream_t st, uint32_t* dig_cnt, unsigned long long* dig_sum) {
     if (b.n <= 0) return;
     float4* f = s0.keep_force ? b.force_s : nullptr;
     if (batched)
-        dispatch(c.block, c.stencil, [&](auto R, auto BL) { force_impl<true, R.value, BL.value>(b, s0, f, st); });
+        dispatch(c.block, c.stencil,
+                 [&](auto R, auto BL) { force_impl<true, R.value, BL.value>(b, s0, f, dig_cnt, dig_sum, st); });
     else
-        dispatch(c.block, c.stencil, [&](auto R, auto BL) { force_impl<false, R.value, BL.value>(b, s0, f, st); });
+        dispatch(c.block, c.stencil,
+                 [&](auto R, auto BL) { force_impl<false, R.value, BL.value>(b, s0, f, dig_cnt, dig_sum, st); });
     if (s0.sdf) {
         const int blocks = std::min((b.n + 255) / 256, device_sm_count() * 8);
         if (batched)

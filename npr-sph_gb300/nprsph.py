@@ -117,6 +117,7 @@ _SIGS = {
     "sph_enable_timing": (C.c_int32, [_P, C.c_int32]),
     "sph_pass_times": (C.c_int32, [_P, C.POINTER(C.c_float)]),
     "sph_neighbor_digest": (C.c_int32, [_P, _P, C.c_uint32, C.c_int32, _P, _P]),
+    "sph_step_neighbor_digest": (C.c_int32, [_P, _P, C.c_uint32, _P, _P]),
     "sph_set_launch": (C.c_int32, [_P, C.c_int32, C.c_int32]),
     "sph_get_launch": (C.c_int32, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "sph_autotune": (C.c_int32, [_P, C.c_int32, C.POINTER(C.c_float)]),
@@ -478,6 +479,16 @@ class Sim:
         dig = np.zeros(len(q), dtype=np.uint64)
         _check(lib.sph_neighbor_digest(self._ctx, q.ctypes.data, len(q), 1 if brute_force else 0, cnt.ctypes.data,
                                        dig.ctypes.data), self._ctx)
+        return cnt, dig
+
+    def step_neighbor_digest(self, query_ids):
+        """One plain step that reports the neighbour sets its force pass used for the query
+        particles (count with self, digest), as neighbor_digest reports them before the step."""
+        q = np.ascontiguousarray(query_ids, dtype=np.uint32)
+        cnt = np.zeros(len(q), dtype=np.uint32)
+        dig = np.zeros(len(q), dtype=np.uint64)
+        _check(lib.sph_step_neighbor_digest(self._ctx, q.ctypes.data, len(q), cnt.ctypes.data, dig.ctypes.data),
+               self._ctx)
         return cnt, dig
 
     def set_launch(self, threads_per_block: int, stencil: int) -> None:

@@ -79,6 +79,60 @@ def test_edge_cases(sph, orc, gpu, stencil):
     np.testing.assert_array_equal(db, do)
 
 
+def _rod(sph):
+    """Particles ~31 per cell in one cell row: row segments longer than one pair mask."""
+    p = sph.workload_params(lower=(0.0, 0.0, 0.0), upper=(3.6, 0.3, 0.3))
+    s = p.h / 3.5
+    lo = (0.01, 0.1015, 0.1015)
+    return p, sph.scene_fill(600 * 9, lo, (lo[0] + 600.5 * s, lo[1] + 3.2 * s, lo[2] + 3.2 * s), s, 0.01 * p.h, 12)
+
+
+def _pile_up(sph):
+    """A clump denser than a shared-memory tile holds next to a lattice: the global-memory path."""
+    p = sph.default_params()
+    rng = np.random.default_rng(3)
+    pos = np.concatenate([0.2 + rng.uniform(-p.h, p.h, (4000, 3)),
+                          sph.reference_scene_10k(seed=5).particles["pos"][:6000, :3]])
+    a = sph.empty_particles(len(pos))
+    a["pos"][:, :3] = pos
+    a["pos"][:, 3] = 1
+    return p, a
+
+
+@pytest.mark.parametrize("scene", ["dam_break", "long_segments", "pile_up"])
+@pytest.mark.parametrize("block", [256, 128])
+def test_force_pass_neighbour_sets(sph, gpu, scene, block):
+    """The neighbour sets the force pass interacts with -- decoded from the density pass's pair
+    masks, tested by the force pass itself in over-long segments, or on the global-memory path
+    -- equal brute force on the positions before the step, bit for bit (counts and digests)."""
+    if scene == "dam_break":
+        sc = sph.dam_break(32, 64, 64, seed=8)
+        p, parts, warm = sc.params, sc.particles, 20
+    elif scene == "long_segments":
+        (p, parts), warm = _rod(sph), 0
+    else:
+        (p, parts), warm = _pile_up(sph), 0
+    q = queries(len(parts), 16384, 2)
+    with sph.Sim(p, n_max=len(parts)) as sim:
+        sim.set_launch(block, 1)
+        sim.upload(parts)
+        sim.step(warm)
+        for _ in range(2):
+            cb, db = sim.neighbor_digest(q, brute_force=True)
+            cf, df = sim.step_neighbor_digest(q)
+            np.testing.assert_array_equal(cf, cb)
+            np.testing.assert_array_equal(df, db)
+        fb = sim.tile_stats()
+    assert cb.min() >= 1
+    if scene == "pile_up":
+        assert fb[1] > 0  # chunks on the global-memory path took part
+    with sph.Sim(p, n_max=len(parts)) as sim:
+        sim.set_launch(block, 2)
+        sim.upload(parts)
+        with pytest.raises(sph.SphError):
+            sim.step_neighbor_digest(q)
+
+
 def test_batched_neighbours(sph, orc, gpu):
     plist, counts, parts = sph.batched_scenes(8, seed=31, n_lo=2000, n_hi=8000)
     offs = np.concatenate([[0], np.cumsum(counts, dtype=np.int64)])
