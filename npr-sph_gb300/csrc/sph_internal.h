@@ -86,7 +86,6 @@ constexpr int kPairMaskWords = 2 * 9;
 struct LaunchCfg {
     int block = 256;     // threads per CTA of the pair kernels (particles per shared-memory tile)
     int stencil = 1;     // cell edge = h/stencil, (2*stencil+1)^3 cells visited
-    int grid_cap = 0;    // persistent grid size (CTAs); 0 = one thread per particle
 };
 
 constexpr int kScanThreads = 256;
