@@ -465,21 +465,22 @@ void infer_prep(const float* prm, uint32_t* frags, cudaStream_t st) {
 }
 
 // Grid of a tile-stride inference kernel: at most the CTAs that fit on the GPU at once.
-static int infer_grid(int n, int per_sm) {
+// One warp per tile of particles (the kernels keep their tile loops, so any grid is correct):
+// the block scheduler balances the tiles, which beats a resident grid looping over fixed shares.
+static int infer_grid(int n) {
     const int tiles = (n + kTile - 1) / kTile;
     const int blocks = (tiles + kWarps - 1) / kWarps;
-    const int cap = device_sm_count() * per_sm;
-    return blocks < cap ? (blocks < 1 ? 1 : blocks) : cap;
+    return blocks < 1 ? 1 : blocks;
 }
 
 void infer_round1(const Frame& f, const uint32_t* frags, __nv_bfloat16* H1, uint16_t* Pperm, cudaStream_t st) {
-    k_infer_r1<<<infer_grid(f.n, 8), kThreads, 0, st>>>(f.pos, f.vel, f.rhop, f.nb, f.cnt, f.fc, f.n, frags, H1, Pperm);
+    k_infer_r1<<<infer_grid(f.n), kThreads, 0, st>>>(f.pos, f.vel, f.rhop, f.nb, f.cnt, f.fc, f.n, frags, H1, Pperm);
 }
 
 void infer_round2(const Frame& f, const uint32_t* frags, const float* prm, const __nv_bfloat16* H1,
                   const uint16_t* Pperm, const SceneDev& S, float4* pos_out, float4* vel_out, float* out, int* key,
                   int* rank, int* count, bool integrate, cudaStream_t st) {
-    k_infer_r2<<<infer_grid(f.n, 6), kThreads, 0, st>>>(f.pos, f.vel, f.nb, f.cnt, f.fc, f.n, frags, prm, H1,
+    k_infer_r2<<<infer_grid(f.n), kThreads, 0, st>>>(f.pos, f.vel, f.nb, f.cnt, f.fc, f.n, frags, prm, H1,
                                                      reinterpret_cast<const uint4*>(Pperm), S, pos_out, vel_out, out,
                                                      key, rank, count, integrate ? 1 : 0);
 }
