@@ -11,7 +11,8 @@ outside the events. Prints one JSON line (rank 0).
 
 --impl reference times the CPU implementation of the same step on the host cores: the
 FP64 restatement of the reference shaders (oracle/), grid back-end, all host threads, on
-a 131,072-particle dam break of the same construction (one step of it per bench step).
+the same 1,048,576-particle dam break over the same steps (W warm-up steps, then the first
+min(K, 30) of the K steps the GPU arm times). It loads nothing but oracle/.
 For N > 1 every rank advances its own replica (the path does not shard: "replicas only").
 """
 from __future__ import annotations
@@ -70,12 +71,16 @@ def barrier(world: int) -> None:
         dist.barrier()
 
 
+PROFILE = "profiles/pair_kernels_dam_break_1m.md"
+
+
 def profiled_traffic(kernel: str):
     """DRAM bytes (read + write) per launch of `kernel` from the committed ncu summary of the
-    dam break (a line `traffic_bytes_per_launch <kernel>: <bytes>`), or None."""
+    dam break (a line `traffic_bytes_per_launch <kernel>: <bytes>`), or None. ncu cannot run
+    inside the timed process, so this figure comes from that capture, not from this run."""
     import re
 
-    prof = REPO / "profiles" / "pair_kernels_dam_break_1m.md"
+    prof = REPO / PROFILE
     if not prof.exists():
         return None
     m = re.search(rf"^traffic_bytes_per_launch {re.escape(kernel)}: (\d+)", prof.read_text(), re.M)
@@ -144,58 +149,66 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_oracle_rate(seconds: float, nthreads: int = 0) -> dict:
-    """FP64 oracle steps on a 131,072-particle dam break until `seconds` have passed."""
-    import nprsph as S
-    from oracle import oracle as O
+CPU_STEPS_MAX = 30  # CPU legs: at most this many timed steps (~0.1 s each at 1M on 16 cores)
 
-    sc = S.dam_break(32, 64, 64, seed=2)
-    n = len(sc.particles)
-    pos = np.ascontiguousarray(sc.particles["pos"][:, :3], dtype=np.float64)
-    vel = np.ascontiguousarray(sc.particles["vel"][:, :3], dtype=np.float64)
-    steps, t0 = 0, time.perf_counter()
-    while True:
-        O.run_f64(sc.params, pos, vel, 1, backend="grid", nthreads=nthreads)
-        steps += 1
-        el = time.perf_counter() - t0
-        if el >= seconds and steps >= 3:
-            break
-    cores = nthreads or O.max_threads()
-    return {"value": n * steps / el, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"FP64 oracle (grid back-end, OpenMP) on a {n}-particle dam break "
-                      f"(32x64x64 block, 0.5h lattice, 4:1:1 box), {steps} steps from its initial state in {el:.1f} s"}
+
+def cpu_oracle_legs(warmup: int, steps: int) -> dict:
+    """The FP64 oracle (grid back-end, OpenMP, all host threads) on the host cores, on the GPU
+    arm's own workloads, loading nothing but oracle/:
+      - the 1,048,576-particle dam break (seed 2, as rank 0's GPU replica), W warm-up steps,
+        then min(K, 30) timed steps: the first steps of the GPU arm's timed region;
+      - the 10,000-particle reference-box scene (config 1): its 200 steps from the start."""
+    from oracle import oracle as O
+    from oracle import scenes as OS
+
+    params, parts = OS.dam_break(seed=2)
+    n = len(parts)
+    pos = np.ascontiguousarray(parts["pos"][:, :3], dtype=np.float64)
+    vel = np.ascontiguousarray(parts["vel"][:, :3], dtype=np.float64)
+    O.run_f64(params, pos, vel, warmup, backend="grid")
+    k = max(1, min(steps, CPU_STEPS_MAX))
+    t0 = time.perf_counter()
+    O.run_f64(params, pos, vel, k, backend="grid")
+    el = time.perf_counter() - t0
+    p10, s10 = OS.reference_scene_10k(seed=1)
+    pos10 = np.ascontiguousarray(s10["pos"][:, :3], dtype=np.float64)
+    vel10 = np.ascontiguousarray(s10["vel"][:, :3], dtype=np.float64)
+    t1 = time.perf_counter()
+    O.run_f64(p10, pos10, vel10, 200, backend="grid")
+    el10 = time.perf_counter() - t1
+    cores = O.max_threads()
+    return {"value": n * k / el, "unit": UNIT, "cores": cores, "kind": "port", "model": OS.cpu_model(),
+            "particles": n, "steps": k, "ms_per_step": 1e3 * el / k,
+            "sample": f"FP64 oracle (grid back-end, OpenMP, {cores} threads) on the 1,048,576-particle dam break: "
+                      f"steps {warmup + 1}-{warmup + k}, the first {k} of the GPU arm's timed steps, {el:.1f} s",
+            "reference_scene_10k": {"value": len(s10) * 200 / el10, "unit": UNIT, "particles": len(s10),
+                                    "steps": 200, "ms_per_step": 1e3 * el10 / 200,
+                                    "workload": "config 1: 10,000 particles at 0.5h in the lower-corner quarter "
+                                                "of the reference box, 200 steps from the start"}}
 
 
 def run_reference(args) -> None:
-    """CPU implementation of the step (the FP64 restatement of the reference shaders) on the host cores."""
+    """CPU implementation of the step (the FP64 restatement of the reference shaders) on the
+    host cores, on the GPU arm's workload and steps."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    import nprsph as S
-    from oracle import oracle as O
-
-    O.lib()
-    sc = S.dam_break(32, 64, 64, seed=2)
-    n = len(sc.particles)
-    pos = np.ascontiguousarray(sc.particles["pos"][:, :3], dtype=np.float64)
-    vel = np.ascontiguousarray(sc.particles["vel"][:, :3], dtype=np.float64)
-    O.run_f64(sc.params, pos, vel, args.warmup, backend="grid")
-    t0 = time.perf_counter()
-    O.run_f64(sc.params, pos, vel, args.steps, backend="grid")
-    el = time.perf_counter() - t0
-    v = n * args.steps / el
-    cores = O.max_threads()
+    leg = cpu_oracle_legs(args.warmup, args.steps)
+    v = leg["value"]
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+            "steps": leg["steps"], "warmup": args.warmup, "ms_per_step": leg["ms_per_step"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "dam break, 131,072-particle sample (32x64x64 block of the 1,048,576-particle "
-                                   "64x128x128 construction) per step", "particles": n},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{args.steps} FP64 oracle steps of the {n}-particle dam break after "
-                                       f"{args.warmup} warm-up steps"},
+            "config": {"workload": WORKLOAD, "particles": leg["particles"],
+                       "timed_steps": [args.warmup, args.warmup + leg["steps"]],
+                       "sample": f"the first {leg['steps']} of the {args.steps} steps the GPU arm times"},
+            "cpu_baseline": leg,
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "gpu_launches": 0}
     print(json.dumps(line), flush=True)
+
+
+WORKLOAD = ("dam break: 1,048,576 particles (64x128x128 block, 0.5h lattice, jitter 0.01h) against the x=0 wall "
+            "of a 5.12x1.28x1.28 box, g=-9.81, dt=1e-4, plain SPH")
 
 
 def timed_steps(sim, stream, steps: int, warmup: int) -> float:
@@ -405,9 +418,9 @@ def learned_workload(args, stream, flush) -> dict:
                        "the last macro-step of each interval is judged against 4 plain steps from the same state "
                        "(tolerance 1% density deviation, 5% deviation of the maximum density, 5% momentum difference "
                        "relative to sum m|v| + M|G|4dt); a failed interval is rolled back and run by plain SPH. "
-                       "Density deviation of the judge: "
-                       "|sum rho_learned - sum rho_plain| / sum rho_plain (FP64 reductions; the default), and, "
-                       "in 'judge_particle_density', the mean over particles of |rho_learned - rho_plain| / rho_plain",
+                       "Density deviation of the judge: the mean over particles of |rho_learned - rho_plain| / "
+                       "rho_plain (the default), and, in 'judge_mean_density', the deviation of the mean density "
+                       "|sum rho_learned - sum rho_plain| / sum rho_plain (FP64 reductions)",
            "units": units, "macro_steps": units * judge_every, "dt_equivalents": units * 32}
     runs = {}
     with S.Net(16, stream=stream.cuda_stream) as net, \
@@ -420,8 +433,8 @@ def learned_workload(args, stream, flush) -> dict:
         plain.refresh_density()
         b = plain.download()
         rp = b["extras"][:, 0].astype(np.float64)
-        for name, metric in (("judge_mean_density", S.JUDGE_MEAN_DENSITY),
-                             ("judge_particle_density", S.JUDGE_PARTICLE_DENSITY)):
+        for name, metric in (("judge_particle_density", S.JUDGE_PARTICLE_DENSITY),
+                             ("judge_mean_density", S.JUDGE_MEAN_DENSITY)):
             reps = []
             learned.upload(sc.particles)
             learned.set_judge(metric)
@@ -432,7 +445,7 @@ def learned_workload(args, stream, flush) -> dict:
             learned.refresh_density()
             rl = learned.download()["extras"][:, 0].astype(np.float64)
             runs[name] = summary(reps, t_l, t_p, rl, rp)
-        learned.set_judge(S.JUDGE_MEAN_DENSITY)
+        learned.set_judge(S.JUDGE_PARTICLE_DENSITY)
         learned.set_max_density_tol(float("inf"))
         # What the network gains: one judged macro-step from the same state (the plain run's
         # end state) with the trained network and with a zero network (v' = v, x' = x + 4 dt v,
@@ -445,15 +458,66 @@ def learned_workload(args, stream, flush) -> dict:
                 r = learned.learned_step(nn, 1, 1, 1e30, 1e30)
                 gain[name] = {"mean_rho_dev": r.last_mean_rho_dev, "max_rho_dev": r.last_max_rho_dev,
                               "particle_density_dev": r.last_density_dev, "momentum_dev": r.last_momentum_dev}
-    out.update(runs["judge_mean_density"])
+    out.update(runs["judge_particle_density"])
     out.update({
         "plain_value": n * 32 * units / t_p, "plain_ms_per_dt": 1e3 * t_p / (32 * units),
-        "judge_particle_density": runs["judge_particle_density"],
+        "judge_mean_density": runs["judge_mean_density"],
         "one_macro_step_vs_4_plain_steps": gain,
         "precision": "BF16 weights/activations, FP32 accumulate (mma.sync m16n8k16)",
         "weights": str(WEIGHTS.relative_to(REPO)),
     })
     return out
+
+
+FP32_LANES_PER_SM = 128  # FP32 FMA lanes per SM (4 sub-partitions x 32)
+# FP32 work per unit: a candidate test (3 sub, 3 mul/FMA, the compare: ~9 flop),
+# a density interaction (~10), a force interaction (~40).
+FLOP_CAND, FLOP_DENS, FLOP_FORCE = 9, 10, 40
+
+
+def roofline_block(n, steps, pass_avg, step_s, cand, pairs, hbm, src, peaks, dev) -> dict:
+    """HBM and FP32-pipe rooflines of the dominant pair kernel and of the whole step. Bytes:
+    the algorithmic bytes per particle of each pass over its CUDA-event time. Flops: the
+    on-device counters of this run's trajectory times the per-unit flops, over the same
+    time; peak FP32 = SMs x 128 lanes x 2 flop x the maximum SM clock."""
+    import torch
+
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    mhz = float(peaks.get("sm_max_mhz", 2070.0))
+    fp32_peak = sms * FP32_LANES_PER_SM * 2 * mhz * 1e6 / 1e12  # TFLOP/s
+    flops = {"density": (FLOP_CAND * cand + FLOP_DENS * pairs) / steps,
+             "force_integrate": FLOP_FORCE * (pairs - n * steps) / steps}
+    per = {}
+    for k, ms in (("density", pass_avg[1]), ("force_integrate", pass_avg[2])):
+        gbs = B_ALG[k] * n / (ms * 1e-3) / 1e9
+        tfl = flops[k] / (ms * 1e-3) / 1e12
+        per[k] = {"ms": ms, "hbm_achieved": gbs, "hbm_frac": gbs / hbm, "fp32_achieved": tfl,
+                  "fp32_frac": tfl / fp32_peak, "bytes_per_particle": B_ALG[k], "flop_per_particle": flops[k] / n}
+    kern = max(per, key=lambda k: per[k]["ms"])
+    d = per[kern]
+    bound = "fp32" if d["fp32_frac"] > d["hbm_frac"] else "hbm"
+    step_gbs = B_ALG_STEP * n * steps / step_s / 1e9
+    step_tfl = (flops["density"] + flops["force_integrate"]) * steps / step_s / 1e12
+    traffic = profiled_traffic("k_" + kern)
+    return {
+        "bound": bound, "kernel": kern,
+        "achieved": d["fp32_achieved"] if bound == "fp32" else d["hbm_achieved"],
+        "peak": fp32_peak if bound == "fp32" else hbm,
+        "unit": "TFLOP/s" if bound == "fp32" else "GB/s",
+        "frac": d["fp32_frac"] if bound == "fp32" else d["hbm_frac"],
+        "traffic": traffic,
+        "traffic_source": f"ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_{kern} launch at the "
+                          f"dense start, from the capture summarised in {PROFILE} (not measured in this run)",
+        "hbm_peak": hbm, "hbm_peak_source": f"{src} hbm_gbs",
+        "fp32_peak": fp32_peak, "fp32_peak_source": f"{sms} SMs x {FP32_LANES_PER_SM} lanes x 2 flop x {mhz:.0f} MHz",
+        "passes": per,
+        "work_counters": {"candidate_tests_per_particle": cand / (n * steps),
+                          "pairs_per_particle_incl_self": pairs / (n * steps),
+                          "flop_model": f"{FLOP_CAND} per candidate test, {FLOP_DENS} per density and "
+                                        f"{FLOP_FORCE} per force interaction"},
+        "step_achieved": step_gbs, "step_frac": step_gbs / hbm, "step_bytes_per_particle": B_ALG_STEP,
+        "step_fp32_achieved": step_tfl, "step_fp32_frac": step_tfl / fp32_peak,
+    }
 
 
 def run_ours(args) -> None:
@@ -512,6 +576,19 @@ def run_ours(args) -> None:
     sim.enable_timing(False)
     pass_avg = pass_ms / args.steps
 
+    # Work of the pair passes over the same trajectory, from on-device counters: candidate
+    # tests and r < h pairs of each step's density pass (the force pass interacts with the
+    # pairs other than the particle itself).
+    sim.upload(sc.particles)
+    sim.step(args.warmup)
+    cand = pairs = 0
+    for k in range(args.steps):
+        c, pr = sim.pair_counts()
+        cand += c
+        pairs += pr
+        sim.step(1)
+    sim.synchronize()
+
     # End to end through the C ABI with host buffers: upload + step + download each step.
     host_in = torch.empty(n * 64, dtype=torch.uint8, pin_memory=True).numpy().view(S.PARTICLE_DTYPE)
     host_out = torch.empty(n * 64, dtype=torch.uint8, pin_memory=True).numpy().view(S.PARTICLE_DTYPE)
@@ -542,36 +619,29 @@ def run_ours(args) -> None:
     peaks, src = measured_peaks()
     hbm = float(peaks["hbm_gbs"])
     value = world * n * args.steps / total_s
-    fi_ms = pass_avg[2]
-    achieved = B_ALG["force_integrate"] * n / (fi_ms * 1e-3) / 1e9
-    step_achieved = B_ALG_STEP * n * args.steps / local_s / 1e9
-    cpu = cpu_oracle_rate(args.cpu_seconds) if args.cpu_seconds > 0 else None
-    traffic = profiled_traffic("k_force_integrate")
+    clocks = clk.summary()
+    roofline = roofline_block(n, args.steps, pass_avg, local_s, cand, pairs, hbm, src, peaks, dev)
+    cpu = cpu_oracle_legs(args.warmup, min(args.steps, args.cpu_steps)) if args.cpu_steps > 0 else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps,
         "ms_per_step_by_tenth": [round(float(np.mean(w)), 4) for w in np.array_split(np.array(step_ms), 10) if len(w)],
         "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "dam break: 1,048,576 particles (64x128x128 block, 0.5h lattice, jitter 0.01h) "
-                               "against the x=0 wall of a 5.12x1.28x1.28 box, g=-9.81, dt=1e-4, plain SPH",
+        "config": {"workload": WORKLOAD,
                    "particles": n, "timed_steps": [args.warmup, args.warmup + args.steps],
                    "l2": "flushed between steps (256 MiB write outside the timed events)",
                    "launch": {"threads_per_block": blk, "stencil": sten}, "parallelism": f"replicas x{world}",
                    "global_path_chunks": {"density": fallback[0], "force": fallback[1],
                                           "of": (args.warmup + args.steps) * ((n + blk - 1) // blk)}},
-        "roofline": {"bound": "hbm", "kernel": "force_integrate", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": traffic, "peak_source": f"{src} hbm_gbs",
-                     "bytes_per_particle": B_ALG["force_integrate"],
-                     "step_achieved": step_achieved, "step_frac": step_achieved / hbm,
-                     "step_bytes_per_particle": B_ALG_STEP},
+        "roofline": roofline,
         "passes_ms": {"sort": pass_avg[0], "density": pass_avg[1], "force_integrate": pass_avg[2]},
         "cpu_baseline": cpu,
         "e2e": {"value": world * n * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * 64,
                 "d2h_bytes_per_step": n * 64, "steps": e2e_steps,
                 "path": "sph_upload_aos + sph_step(1) + sph_download_aos, pinned host AoS records"},
         "gpu_launches": KERNELS_PER_STEP * args.steps,
-        "clocks": clk.summary(),
+        "clocks": clocks,
         "final_state": {"mean_rho": diag.mean_rho, "nonfinite": int(diag.nonfinite), "step": int(diag.step)},
         "other_configs": extra,
         "learned": learned,
@@ -589,7 +659,8 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample length (0: skip)")
+    ap.add_argument("--cpu-steps", type=int, default=CPU_STEPS_MAX,
+                    help="cap on the timed steps of the CPU oracle leg (0: skip it)")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="keep the default launch shape instead of timing the candidates first")
     ap.add_argument("--no-learned", dest="learned", action="store_false",

@@ -203,6 +203,13 @@ sph_status sph_reduce_scenes(sph_ctx* ctx, sph_diag* out, uint32_t n_scene);
 sph_status sph_set_launch(sph_ctx* ctx, int32_t threads_per_block, int32_t stencil);
 sph_status sph_get_launch(const sph_ctx* ctx, int32_t* threads_per_block, int32_t* stencil);
 sph_status sph_autotune(sph_ctx* ctx, int32_t trial_steps, float* best_ms_per_step);
+/* Work counters of the next step's pair passes at the current positions
+ * (measurement; the state is not changed): out[0] = candidate tests of the
+ * density pass (the particles of cells cx-R..cx+R of each of its (2R+1)^2
+ * stencil rows, R the stencil), out[1] = pairs with r < h, self included
+ * (rho_pres_comp.glsl:46-54); the force pass interacts with out[1] - n of
+ * them (force_comp.glsl:48-62 skips j == i). Synchronous. */
+sph_status sph_pair_counts(sph_ctx* ctx, uint64_t out[2]);
 /* Chunks of the density (out[0]) and force (out[1]) passes, since creation,
  * that did not fit a shared-memory tile and read their neighbours from global
  * memory instead (heavy pile-ups). Synchronous. */
@@ -224,10 +231,11 @@ sph_status sph_tile_stats(sph_ctx* ctx, uint32_t out[2]);
  * checkpoint and run by plain SPH, and after the k-th failure in a row plain SPH
  * also runs the next 2^(k-1) - 1 intervals (at most 7). The density deviation is
  * (sph_learned_set_judge):
- *   SPH_JUDGE_MEAN_DENSITY (default): the deviation of the mean density,
- *     |sum rho_learned - sum rho_plain| / sum rho_plain;
- *   SPH_JUDGE_PARTICLE_DENSITY: the mean over particles (by id) of
- *     |rho_learned - rho_plain| / rho_plain, a much stricter bound.
+ *   SPH_JUDGE_PARTICLE_DENSITY (default): the mean over particles (by id) of
+ *     |rho_learned - rho_plain| / rho_plain;
+ *   SPH_JUDGE_MEAN_DENSITY: the deviation of the mean density,
+ *     |sum rho_learned - sum rho_plain| / sum rho_plain, a much weaker bound
+ *     (particles can be wrong one by one and still sum right).
  * Both are reported whichever decides. This judge state lives in the context
  * across sph_learned_step calls; an upload clears it (the metric setting stays). */
 typedef struct sph_mpnn sph_mpnn;
@@ -286,7 +294,7 @@ sph_status sph_mpnn_train(sph_mpnn* net, uint32_t steps, float lr, uint64_t seed
 sph_status sph_learned_step(sph_ctx* ctx, sph_mpnn* net, int32_t n_macro, int32_t judge_every,
                             float density_tol, float momentum_tol, sph_learned_report* report);
 /* The density deviation the judge of sph_learned_step compares with density_tol:
- * SPH_JUDGE_MEAN_DENSITY (default) or SPH_JUDGE_PARTICLE_DENSITY. */
+ * SPH_JUDGE_PARTICLE_DENSITY (default) or SPH_JUDGE_MEAN_DENSITY. */
 sph_status sph_learned_set_judge(sph_ctx* ctx, int32_t metric);
 /* A further bound of the judge: the interval also fails when the maximum density deviates by
  * more than tol, |max rho_learned - max rho_plain| / max rho_plain (default: no bound). The
@@ -321,8 +329,12 @@ sph_status sph_neighbor_lists(sph_ctx* ctx, int32_t* nb_ids, int32_t* counts, fl
  * the process exits.
  *   - n <= 4,194,304 records; larger n returns SPH_ERR_CAPACITY.
  *   - Asynchronous on `stream` (cudaStream_t, NULL = legacy default stream).
- *   - The first call on each device looks up the scratch array's device
- *     address; make that first call before any stream capture.
+ *   - Every call looks up the scratch array's device address in the
+ *     context current on the calling thread (the device's primary context,
+ *     or a caller's own driver context), so a reset device or a second
+ *     context never sees a stale address. The first call in a context also
+ *     loads the library's device code there: make that first call before
+ *     any stream capture.
  *   - All calls share the scratch: calls that overlap on the GPU (different
  *     streams without ordering between them) race and give wrong sums. */
 sph_status sph_reduce_aos_noalloc(const sph_particle* dev_particles, uint32_t n, const sph_params* p,

@@ -30,7 +30,7 @@ struct sph_ctx {
     // judge state of the learned macro-step, kept across sph_learned_step calls (cleared by uploads)
     int judge_failures = 0;  // failed judges in a row
     int judge_backoff = 0;   // plain intervals still to run before the next learned attempt
-    int judge_metric = SPH_JUDGE_MEAN_DENSITY;  // density deviation the judge decides on
+    int judge_metric = SPH_JUDGE_PARTICLE_DENSITY;  // density deviation the judge decides on
     double judge_max_rho_tol = INFINITY;        // bound on the deviation of the maximum density
     long long cell_cap = 0;
     int tile_cap = 0;
@@ -50,6 +50,8 @@ struct sph_ctx {
     // sph_step_neighbor_digest: the force pass's neighbour counts and digests per sorted slot
     uint32_t* fd_cnt = nullptr;
     unsigned long long* fd_sum = nullptr;
+    // sph_pair_counts: the density pass's candidate tests and r < h pairs (2 counters)
+    unsigned long long* pc_dev = nullptr;
     // static obstacle (sph_set_obstacle): signed distance samples on the device, or null
     float* sdf_dev = nullptr;
     int sdf_dims[3] = {0, 0, 0};

@@ -474,7 +474,7 @@ sph_status sph_destroy(sph_ctx* ctx) {
     void* ptrs[] = {b.pos, b.vel, b.pos_s, b.vel_s, b.rhop, b.force_s, b.force_up, b.aux, b.aos, b.key, b.rank,
                     b.perm, b.count, b.start, b.scan_state, b.slot_of_id, b.err, b.partials,
                     b.scenes, b.tile_stats, b.pmask, ctx->diag_dev, ctx->scene_first_dev, ctx->q_ids, ctx->q_cnt, ctx->q_dig,
-                    ctx->fd_cnt, ctx->fd_sum,
+                    ctx->fd_cnt, ctx->fd_sum, ctx->pc_dev,
                     ctx->render_buf, ctx->sdf_dev};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -706,6 +706,23 @@ sph_status sph_step_neighbor_digest(sph_ctx* ctx, const uint32_t* query_ids, uin
         CK(cudaMemcpyAsync(count_out, ctx->q_cnt, sizeof(uint32_t) * n_query, cudaMemcpyDeviceToHost, ctx->stream));
         CK(cudaMemcpyAsync(digest_out, ctx->q_dig, sizeof(uint64_t) * n_query, cudaMemcpyDeviceToHost, ctx->stream));
     }
+    return check_device_error(ctx);
+    GUARD_END
+}
+
+sph_status sph_pair_counts(sph_ctx* ctx, uint64_t out[2]) {
+    if (!ctx || !out) return SPH_ERR_INVALID_ARG;
+    if (!ctx->have_state) return fail(ctx, SPH_ERR_NOT_READY, "no particles uploaded");
+    GUARD_BEGIN
+    CK(cudaSetDevice(ctx->device));
+    if (!ctx->pc_dev) CK(dalloc(&ctx->pc_dev, 2));
+    if (ctx->need_hash) launch_hash(ctx->b, ctx->s0, ctx->batched, ctx->stream);
+    enqueue_sort(ctx);  // sorted copy of the current positions; the state itself is untouched
+    ctx->need_hash = true;  // the scan consumed the cell counts
+    CK(cudaMemsetAsync(ctx->pc_dev, 0, 2 * sizeof(unsigned long long), ctx->stream));
+    launch_pair_counts(ctx->b, ctx->s0, ctx->batched, ctx->cfg.stencil, ctx->pc_dev, ctx->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, ctx->pc_dev, 2 * sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx->stream));
     return check_device_error(ctx);
     GUARD_END
 }

@@ -288,6 +288,46 @@ __global__ void __launch_bounds__(kThreads) k_digest_brute(const float4* __restr
     }
 }
 
+// Work counters of the density pass at the current (sorted) positions: out[0] += the
+// candidate tests (the particles of cells cx-R..cx+R of every stencil row, as the pass scans
+// them), out[1] += the pairs with r < h (self included). Measurement only.
+template <bool BATCHED>
+__global__ void __launch_bounds__(kThreads) k_pair_counts(const float4* __restrict__ pos_s, const int* __restrict__ start,
+                                                          SceneDev s0, const SceneDev* __restrict__ scenes, int nscene,
+                                                          int R, int n, unsigned long long* __restrict__ out) {
+    unsigned long long cand = 0, pairs = 0;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const float4 p = pos_s[t];
+        int sc = 0;
+        if constexpr (BATCHED) sc = min(max(scene_of(p), 0), nscene - 1);
+        const SceneDev& S = scene_params<BATCHED>(s0, scenes, sc);
+        const int cx = cell_coord(p.x, S.lo[0], S.inv_edge, S.dim[0]);
+        const int cy = cell_coord(p.y, S.lo[1], S.inv_edge, S.dim[1]);
+        const int cz = cell_coord(p.z, S.lo[2], S.inv_edge, S.dim[2]);
+        for (int z = max(cz - R, 0); z <= min(cz + R, S.dim[2] - 1); ++z)
+            for (int y = max(cy - R, 0); y <= min(cy + R, S.dim[1] - 1); ++y) {
+                const int row = S.cell_base + S.dim[0] * (y + S.dim[1] * z);
+                const int a = max(start[row + max(cx - R, 0)], 0);
+                const int b = min(start[row + min(cx + R, S.dim[0] - 1) + 1], n);
+                cand += (unsigned long long)max(b - a, 0);
+                for (int j = a; j < b; ++j) {
+                    const float4 o = pos_s[j];
+                    float dx, dy, dz;
+                    pairs += canon_d2(p.x, p.y, p.z, o.x, o.y, o.z, dx, dy, dz) < S.cut_d2 ? 1ull : 0ull;
+                }
+            }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        cand += __shfl_xor_sync(0xffffffffu, cand, o);
+        pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(out, cand);
+        atomicAdd(out + 1, pairs);
+    }
+}
+
 }  // namespace
 
 int device_sm_count() {
@@ -364,6 +404,16 @@ void launch_neighbor_digest(const Buffers& b, const SceneDev& s0, bool batched, 
             k_digest_grid<false><<<blocks, kThreads, 0, st>>>(b.pos_s, b.vel_s, b.start, b.slot_of_id, s0, b.scenes, 1,
                                                               stencil, qids, nq, b.n, cnt, dig);
     }
+}
+
+void launch_pair_counts(const Buffers& b, const SceneDev& s0, bool batched, int stencil, unsigned long long* out,
+                        cudaStream_t st) {
+    if (b.n <= 0) return;
+    if (batched)
+        k_pair_counts<true><<<grid_for(b.n), kThreads, 0, st>>>(b.pos_s, b.start, s0, b.scenes, b.nscene, stencil, b.n,
+                                                                out);
+    else
+        k_pair_counts<false><<<grid_for(b.n), kThreads, 0, st>>>(b.pos_s, b.start, s0, b.scenes, 1, stencil, b.n, out);
 }
 
 }  // namespace sphgb

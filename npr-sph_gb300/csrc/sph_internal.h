@@ -103,6 +103,10 @@ void launch_neighbor_digest(const Buffers& b, const SceneDev& s0, bool batched, 
                             unsigned long long* dig, cudaStream_t st);
 // Per query id: cnt[q] = src_cnt[slot_of_id[id]], dig[q] = src_sum[...] (0xffffffff / 0 for a
 // bad id).
+// Candidate tests and r < h pairs (self included) of the density pass at the sorted positions,
+// added to out[0], out[1] (device; measurement only).
+void launch_pair_counts(const Buffers& b, const SceneDev& s0, bool batched, int stencil, unsigned long long* out,
+                        cudaStream_t st);
 void launch_query_gather(const Buffers& b, const uint32_t* qids, int nq, const uint32_t* src_cnt,
                          const unsigned long long* src_sum, uint32_t* cnt, unsigned long long* dig, cudaStream_t st);
 // ---- launchers (sph_step.cu) ----

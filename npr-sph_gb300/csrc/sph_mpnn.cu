@@ -10,9 +10,8 @@
 // and the backward pass mirrors it: dense data/weight gradients, per-edge
 // gradients of round 2 (materialised), the reverse-edge gather that returns
 // dP_j to the sending particle, and the round-1 edge weight gradient. Weight
-// gradients are reduced in fixed-order partials (deterministic); the reverse
-// gather follows atomically built lists, so training is deterministic up to
-// the FP32 summation order of dP.
+// gradients are reduced in fixed-order partials, and the reverse-edge lists are
+// sorted by edge before the gather, so training is deterministic.
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -293,7 +292,25 @@ __global__ void __launch_bounds__(kT) k_rev_fill(const int* __restrict__ nb, con
     edges[off[j] + atomicAdd(&cur[j], 1)] = (int)r;
 }
 
-// dP[j, o] = sum over the edges (i -> j) of dZ2[edge, o].
+// Each particle's reverse edges in ascending edge order (k_rev_fill places them in atomicAdd
+// order): an insertion sort of the short list (~the neighbour count), one thread per particle,
+// so that k_rev_gather sums dP in a fixed order and training is reproducible.
+__global__ void __launch_bounds__(kT) k_rev_sort(const int* __restrict__ off, int n, int* __restrict__ edges) {
+    const int j = blockIdx.x * kT + threadIdx.x;
+    if (j >= n) return;
+    const int a = off[j], b = off[j + 1];
+    for (int q = a + 1; q < b; ++q) {
+        const int x = edges[q];
+        int u = q - 1;
+        while (u >= a && edges[u] > x) {
+            edges[u + 1] = edges[u];
+            --u;
+        }
+        edges[u + 1] = x;
+    }
+}
+
+// dP[j, o] = sum over the edges (i -> j) of dZ2[edge, o], in ascending edge order.
 __global__ void __launch_bounds__(kT) k_rev_gather(const int* __restrict__ off, const int* __restrict__ edges,
                                                   const float* __restrict__ dZ2, int n, float* __restrict__ dP) {
     const long long t = (long long)blockIdx.x * kT + threadIdx.x;
@@ -414,6 +431,7 @@ struct Trainer {
         k_scan_small<<<1, 1024, 0, st>>>(rev_cnt, n, rev_off);
         cudaMemsetAsync(rev_cnt, 0, sizeof(int) * n, st);
         k_rev_fill<<<nblk((long long)n * K), kT, 0, st>>>(f.nb, f.cnt, n, rev_off, rev_cnt, rev_edges);
+        k_rev_sort<<<nblk(n), kT, 0, st>>>(rev_off, n, rev_edges);
         k_rev_gather<<<nblk((long long)n * W), kT, 0, st>>>(rev_off, rev_edges, dZ2, n, dP);
         wgrad(H1, W, W, dP, W, W, n, kWp, -1, st);
         // dY1 = (dX2[:, W:] + dP Wp^T) * (H1 > 0)

@@ -12,8 +12,6 @@
 // scratch is a file-scope __device__ array of fixed size, so the call itself
 // allocates nothing. Every GPU that loads this library holds the array
 // (kNoAllocMaxBlocks * kDiagFields doubles = 96 KiB) until the process exits.
-#include <mutex>
-
 #include "sph_device.cuh"
 
 namespace sphgb {
@@ -23,7 +21,6 @@ constexpr int kNoAllocThreads = 256;
 constexpr int kNoAllocPerBlock = 4096;   // particles reduced by one CTA
 constexpr int kNoAllocMaxBlocks = 1024;  // CTAs, and rows of the scratch array
 constexpr long long kNoAllocMaxParticles = (long long)kNoAllocMaxBlocks * kNoAllocPerBlock;  // 4,194,304
-constexpr int kMaxDevices = 64;
 
 // The scratch: one row of kDiagFields partial sums per CTA. A call writes every
 // row it later reads, so nothing has to be cleared between calls. All calls
@@ -31,10 +28,6 @@ constexpr int kMaxDevices = 64;
 // without ordering between them) race on it.
 static __device__ __align__(256) double g_noalloc_partials[kNoAllocMaxBlocks * kDiagFields];
 
-// Device address of g_noalloc_partials, looked up once per device. In host
-// code the array's name is only a host-side stand-in, not a device address.
-std::mutex g_noalloc_mu;
-double* g_noalloc_ptr[kMaxDevices] = {};
 
 __global__ void __launch_bounds__(kNoAllocThreads) k_noalloc_partial(const sph_particle* __restrict__ aos, int n,
                                                                      double mass, double rho0, double gx, double gy,
@@ -91,17 +84,17 @@ __global__ void k_noalloc_final(const double* __restrict__ partials, int nblocks
     out[f] = r;
 }
 
-// Set-up, once per device, with that device current: the device address of the scratch.
-cudaError_t noalloc_scratch(int dev, double** out) {
-    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
-        double* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress((void**)&p, g_noalloc_partials);
-        if (e != cudaSuccess) return e;
-        g_noalloc_ptr[dev] = p;
-    }
-    *out = g_noalloc_ptr[dev];
+// The device address of the scratch in the context current on the calling thread. In host
+// code the array's name is only a host-side stand-in, not a device address. The address is
+// looked up on every call, not kept: each context that loads the library has its own copy
+// of the array (a caller's own driver context on a device differs from the device's primary
+// context), and after cudaDeviceReset the old address is gone. The first lookup in a
+// context loads the library's module there; later ones are a table lookup.
+cudaError_t noalloc_scratch(double** out) {
+    double* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress((void**)&p, g_noalloc_partials);
+    if (e != cudaSuccess) return e;
+    *out = p;
     return cudaSuccess;
 }
 
@@ -115,10 +108,8 @@ extern "C" sph_status sph_reduce_aos_noalloc(const sph_particle* dev_particles, 
     if (!dev_particles || !p || !dev_sums) return SPH_ERR_INVALID_ARG;
     if ((long long)n > kNoAllocMaxParticles) return SPH_ERR_CAPACITY;
     if (!(p->resting_rho > 0.0f)) return SPH_ERR_INVALID_ARG;
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return SPH_ERR_CUDA;
     double* scratch = nullptr;
-    if (noalloc_scratch(dev, &scratch) != cudaSuccess) return SPH_ERR_CUDA;
+    if (noalloc_scratch(&scratch) != cudaSuccess) return SPH_ERR_CUDA;
     const cudaStream_t st = (cudaStream_t)stream;
     const int nblocks = n == 0 ? 0 : (int)((n + kNoAllocPerBlock - 1) / kNoAllocPerBlock);
     if (nblocks > 0)

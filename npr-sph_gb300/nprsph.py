@@ -160,6 +160,7 @@ _SIGS = {
                                    C.c_float, C.c_uint64]),
     "sph_scene_ball": (C.c_int32, [_P, C.c_uint32, C.POINTER(C.c_float), C.c_float, C.c_float, C.c_uint64]),
     "sph_scene_slosh": (C.c_int32, [_P, C.c_uint32, C.c_float, C.c_float, C.c_float]),
+    "sph_pair_counts": (C.c_int32, [_P, C.POINTER(C.c_uint64)]),
     "sph_set_obstacle": (C.c_int32, [_P, _P, C.POINTER(C.c_int32), C.POINTER(C.c_float), C.c_float]),
     "sph_sdf_from_mesh": (C.c_int32, [_P, C.c_uint32, _P, C.c_uint32, C.POINTER(C.c_int32), C.POINTER(C.c_float),
                                       C.c_float, _P]),
@@ -498,6 +499,13 @@ class Sim:
         a, b = C.c_int32(), C.c_int32()
         _check(lib.sph_get_launch(self._ctx, C.byref(a), C.byref(b)), self._ctx)
         return a.value, b.value
+
+    def pair_counts(self) -> tuple[int, int]:
+        """(candidate tests of the density pass, pairs with r < h incl. self) of the next step at
+        the current positions (sph_pair_counts)."""
+        out = (C.c_uint64 * 2)()
+        _check(lib.sph_pair_counts(self._ctx, out), self._ctx)
+        return int(out[0]), int(out[1])
 
     def tile_stats(self) -> tuple[int, int]:
         """(density, force) chunks that fell back to the global-memory path since creation."""

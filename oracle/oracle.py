@@ -19,18 +19,31 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "liboracle.so"
 REF_LIB = HERE / "_ref" / "libref_shader.so"
-REF_SRC = Path("/root/reference/NPR-SPH")
+# The reference tree (its NPR-SPH/ folder with the .glsl shaders), named by the environment;
+# without it the reference shaders are not built.
+REF_ENV = "NPRSPH_REF_DIR"
 
 _P = C.c_void_p
 _I64 = C.c_int64
 
 
+def ref_source() -> Path | None:
+    """The reference's NPR-SPH/ folder named by $NPRSPH_REF_DIR, if it holds the shaders."""
+    d = os.environ.get(REF_ENV)
+    if not d:
+        return None
+    p = Path(d)
+    return p if (p / "rho_pres_comp.glsl").is_file() else None
+
+
 def build(with_ref: bool = True) -> None:
     """Always a full rebuild (a few seconds): the tree moves between x86-64 and aarch64 hosts,
-    and a library left from the other architecture must never be loaded."""
+    and a library left from the other architecture must never be loaded. The reference
+    shaders are built only when $NPRSPH_REF_DIR names the reference's NPR-SPH/ folder."""
     subprocess.run(["make", "-s", "-B", "-C", str(HERE)], check=True)
-    if with_ref and REF_SRC.is_dir():
-        subprocess.run(["make", "-s", "-B", "-C", str(HERE), "ref", f"REF_DIR={REF_SRC}"], check=True)
+    src = ref_source() if with_ref else None
+    if src is not None:
+        subprocess.run(["make", "-s", "-B", "-C", str(HERE), "ref", f"REF_DIR={src}"], check=True)
 
 
 _lib = None

@@ -3,9 +3,10 @@
 The three GLSL shaders of NPR-SPH (rho_pres_comp.glsl, force_comp.glsl,
 integrate_comp.glsl) are compiled as C++ by `make -C oracle ref` (see
 oracle/ref_shader/) and stepped on the CPU. This script needs the reference
-tree and is run by hand where it is present:
+tree and is run by hand where it is present, with $NPRSPH_REF_DIR naming its
+NPR-SPH/ folder (the one holding the .glsl files):
 
-    python tests/golden/make_golden.py
+    NPRSPH_REF_DIR=<reference>/NPR-SPH python tests/golden/make_golden.py
 
 The fixture holds, per case and step count:
   - sha256 of the full 10,000-record output (bit-exact pin of the FP32 mirror),
@@ -46,7 +47,7 @@ def sha(a: np.ndarray) -> str:
 
 def main() -> None:
     O.build(with_ref=True)
-    assert O.ref_available(), "oracle/_ref/libref_shader.so was not built (is the reference tree present?)"
+    assert O.ref_available(), "oracle/_ref/libref_shader.so was not built (set NPRSPH_REF_DIR)"
     data = {}
     for name, parts in scenes().items():
         data[f"{name}_input_sha"] = np.array(sha(parts))

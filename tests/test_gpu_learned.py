@@ -190,8 +190,8 @@ def test_learned_run_stays_finite(sph, trained):
 def test_judge_metric_selects_the_density_deviation(sph, trained):
     """Both density deviations of a judged macro-step are reported and the selected one
     decides. The deviation of the mean density is far below the mean per-particle deviation,
-    so a tolerance between the two keeps the learned interval under JUDGE_MEAN_DENSITY (the
-    default) and rolls it back under JUDGE_PARTICLE_DENSITY."""
+    so a tolerance between the two keeps the learned interval under JUDGE_MEAN_DENSITY and
+    rolls it back under JUDGE_PARTICLE_DENSITY, which a new context uses by default."""
     net, _ = trained
     sc = sph.dam_break(16, 32, 32, seed=24)
     out = {}
@@ -209,9 +209,13 @@ def test_judge_metric_selects_the_density_deviation(sph, trained):
             out[metric] = sim.learned_step(net, 1, 1, tol, 1e30)
         with pytest.raises(sph.SphError):
             sim.set_judge(7)
+    with sph.Sim(sc.params, n_max=len(sc.particles)) as fresh:  # no set_judge: the default metric
+        fresh.upload(start)
+        default = fresh.learned_step(net, 1, 1, tol, 1e30)
     mean, part = out[sph.JUDGE_MEAN_DENSITY], out[sph.JUDGE_PARTICLE_DENSITY]
     assert (mean.learned_macro_steps, mean.fallbacks) == (1, 0)
     assert (part.learned_macro_steps, part.fallbacks) == (0, 1)
+    assert (default.learned_macro_steps, default.fallbacks) == (0, 1)
 
 
 def test_max_density_bound(sph, trained):
