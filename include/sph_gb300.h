@@ -276,12 +276,25 @@ sph_status sph_mpnn_loss_grad(sph_mpnn* net, uint32_t n, const float* pos4, cons
                               const float* target8, const float fc[6], double* loss, float* out8,
                               float* grad);
 /* Network output (n x 8: O_v, O_x, 0, 0) of a host frame as above: precision 1 runs the
- * BF16 tensor-core inference kernels (the macro-step's path), 0 the FP32 training forward. */
+ * BF16 tensor-core inference kernels (the macro-step's path), 0 the FP32 training forward,
+ * 2 the training forward with the node layers on the BF16 tensor-core GEMMs. */
 sph_status sph_mpnn_forward(sph_mpnn* net, uint32_t n, const float* pos4, const float* vel4,
                             const float* rhop2, const int32_t* nb, const int32_t* cnt, const float fc[6],
                             int32_t precision, float* out8);
+/* Diagnostics of the BF16 tensor-core GEMM that the training passes use (tcgen05 MMA,
+ * FP32 accumulation in tensor memory): D = A B^T for host arrays A (m x k) and B (n x k),
+ * bf16 bit patterns, row-major; D (splits x m x n) FP32, one m x n partial per K slice
+ * (splits = 1: the product). k and n multiples of 16, n <= 256 (16, 32, 64, 80, 128 or
+ * 144). Synchronous; SPH_ERR_DEVICE if a tensor-core wait timed out. */
+sph_status sph_tc_gemm_bf16(const uint16_t* a, const uint16_t* b, int32_t m, int32_t n, int32_t k, int32_t splits,
+                            float* d);
 /* Precision of sph_learned_step: 1 BF16 tensor cores (default), 0 FP32 CUDA cores. */
 sph_status sph_mpnn_set_precision(sph_mpnn* net, int32_t precision);
+/* Precision of the training passes (sph_mpnn_loss_grad, sph_mpnn_train): 1 (default) runs
+ * the node layers -- forward, data gradients and weight gradients -- as BF16 GEMMs on the
+ * tensor cores (tcgen05, FP32 accumulation, FP32 master weights in Adam); 0 runs every layer
+ * in FP32 on the CUDA cores. The per-edge layers run in FP32 either way. */
+sph_status sph_mpnn_set_train_precision(sph_mpnn* net, int32_t precision);
 /* Record n_frames frames of every scene of ctx (created with SPH_FLAG_KEEP_FORCE): the state,
  * its neighbour lists and density, and as targets (O_v, O_x) of the next 4 plain steps from
  * the forces alone (no wall clamp). Advances ctx by 4 * n_frames steps. */

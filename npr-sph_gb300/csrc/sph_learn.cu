@@ -59,7 +59,8 @@ struct sph_mpnn {
     void* harena = nullptr;
     int adam_t = 0;  // Adam steps taken since the parameters were last set
     // BF16 tensor-core inference
-    int precision = 1;               // 1: BF16 tensor cores (default), 0: FP32 CUDA cores
+    int precision = 1;               // inference: 1 BF16 tensor cores (default), 0 FP32 CUDA cores
+    int train_precision = 1;         // training node layers: 1 BF16 tcgen05 GEMMs (default), 0 FP32
     uint32_t* frags = nullptr;       // parameters in MMA fragment order
     bool frags_dirty = true;
     __nv_bfloat16* H1b = nullptr;    // [n][64]
@@ -460,6 +461,7 @@ sph_status sph_mpnn_create(uint32_t n_frame, void* stream, sph_mpnn** out) {
     else if (cudaStreamCreateWithFlags(&net->stream, cudaStreamNonBlocking) == cudaSuccess) net->own_stream = true;
     else { delete net; return SPH_ERR_CUDA; }
     net->tr = M::trainer_new((int)n_frame, true);
+    if (net->tr) M::trainer_set_tc(net->tr, net->train_precision == 1);
     if (!net->tr) { sph_mpnn_destroy(net); return SPH_ERR_OUT_OF_MEMORY; }
     *out = net;
     return SPH_OK;
@@ -538,6 +540,7 @@ sph_status sph_mpnn_loss_grad(sph_mpnn* net, uint32_t n, const float* pos4, cons
     NCK(cudaMemcpyAsync(dnb, nb, (size_t)n * M::K * 4, cudaMemcpyHostToDevice, st));
     M::Frame f{dpos, dvel, drh, dnb, dcnt, dtg, (int)n, {fc[0], fc[1], fc[2], fc[3], fc[4], fc[5]}};
     const double l = M::trainer_loss_grad(net->tr, f, st);
+    if (M::trainer_tc_error(net->tr, st)) { net->err = "tensor-core GEMM wait timed out"; return SPH_ERR_DEVICE; }
     if (loss) *loss = l;
     if (out8)
         NCK(cudaMemcpyAsync(out8, M::trainer_out(net->tr), (size_t)n * 4 * M::kOS, cudaMemcpyDeviceToHost, st));
@@ -553,10 +556,17 @@ sph_status sph_mpnn_set_precision(sph_mpnn* net, int32_t precision) {
     return SPH_OK;
 }
 
+sph_status sph_mpnn_set_train_precision(sph_mpnn* net, int32_t precision) {
+    if (!net || (precision != 0 && precision != 1)) return SPH_ERR_INVALID_ARG;
+    net->train_precision = precision;
+    M::trainer_set_tc(net->tr, precision == 1);
+    return SPH_OK;
+}
+
 sph_status sph_mpnn_forward(sph_mpnn* net, uint32_t n, const float* pos4, const float* vel4, const float* rhop2,
                             const int32_t* nb, const int32_t* cnt, const float fc[6], int32_t precision, float* out8) {
     if (!net || !pos4 || !vel4 || !rhop2 || !nb || !cnt || !fc || !out8 || n == 0) return SPH_ERR_INVALID_ARG;
-    if (precision != 0 && precision != 1) return SPH_ERR_INVALID_ARG;
+    if (precision < 0 || precision > 2) return SPH_ERR_INVALID_ARG;
     if ((int)n > M::trainer_capacity(net->tr)) { net->err = "frame larger than the training workspace"; return SPH_ERR_CAPACITY; }
     for (uint32_t i = 0; i < n; ++i) {
         if (cnt[i] < 0 || cnt[i] > M::K) { net->err = "neighbour count out of [0, 32]"; return SPH_ERR_INVALID_ARG; }
@@ -590,9 +600,13 @@ sph_status sph_mpnn_forward(sph_mpnn* net, uint32_t n, const float* pos4, const 
         M::infer_round2(f, net->frags, M::trainer_params(net->tr), net->H1b, net->Pperm, S, nullptr, nullptr, dout,
                         nullptr, nullptr, nullptr, false, st);
         NCK(cudaMemcpyAsync(out8, dout, (size_t)n * 4 * M::kOS, cudaMemcpyDeviceToHost, st));
-    } else {
+    } else {  // the training forward: 0 FP32, 2 BF16 tensor-core node layers
+        const bool tc_was = M::trainer_tc(net->tr);
+        M::trainer_set_tc(net->tr, precision == 2);
         M::trainer_forward(net->tr, f, st);
+        M::trainer_set_tc(net->tr, tc_was);
         NCK(cudaMemcpyAsync(out8, M::trainer_out(net->tr), (size_t)n * 4 * M::kOS, cudaMemcpyDeviceToHost, st));
+        if (M::trainer_tc_error(net->tr, st)) { net->err = "tensor-core GEMM wait timed out"; return SPH_ERR_DEVICE; }
     }
     NCK(cudaStreamSynchronize(st));
     NCK(cudaGetLastError());
@@ -685,6 +699,7 @@ sph_status sph_mpnn_train(sph_mpnn* net, uint32_t steps, float lr, uint64_t seed
     net->frags_dirty = true;
     NCK(cudaStreamSynchronize(net->stream));
     NCK(cudaGetLastError());
+    if (M::trainer_tc_error(net->tr, net->stream)) { net->err = "tensor-core GEMM wait timed out"; return SPH_ERR_DEVICE; }
     if (net->inf)
         NCK(cudaMemcpyAsync(M::trainer_params(net->inf), M::trainer_params(net->tr), sizeof(float) * M::kParams,
                             cudaMemcpyDeviceToDevice, net->stream));

@@ -18,6 +18,7 @@
 
 #include "sph_mpnn.h"
 #include "sph_internal.h"
+#include "sph_tc.h"
 
 namespace sphgb {
 namespace mpnn {
@@ -334,6 +335,86 @@ __global__ void __launch_bounds__(kT) k_adam(float* __restrict__ p, const float*
     p[t] -= lr * (mt * c1) / (sqrtf(vt * c2) + eps);
 }
 
+// ---- operands of the tensor-core path --------------------------------------------------
+// BF16 copies of an FP32 activation or gradient matrix src [n][lds] (its first ncols columns):
+// dst [n][ldd] row-major with column bias_col = 1 and the other columns >= ncols zero, and/or
+// dstT [ldd][ldt] transposed (the K-major operand of a weight gradient, which contracts over
+// particles), zero for particles n .. kpad - 1. 32 x 32 tiles through shared memory, so both
+// the reads and the transposed writes are coalesced.
+__global__ void __launch_bounds__(256) k_pack_bf16(const float* __restrict__ src, int lds, int ncols, int n, int kpad,
+                                                  int bias_col, __nv_bfloat16* __restrict__ dst, int ldd,
+                                                  __nv_bfloat16* __restrict__ dstT, int ldt) {
+    __shared__ float tile[32][33];
+    const int i0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+#pragma unroll
+    for (int r = ty; r < 32; r += 8) {
+        const int i = i0 + r, c = c0 + tx;
+        float v = 0.0f;
+        if (i < n && c < ldd) v = c < ncols ? src[(size_t)i * lds + c] : (c == bias_col ? 1.0f : 0.0f);
+        tile[r][tx] = v;
+        if (dst && i < n && c < ldd) dst[(size_t)i * ldd + c] = __float2bfloat16_rn(v);
+    }
+    if (!dstT) return;
+    __syncthreads();
+#pragma unroll
+    for (int r = ty; r < 32; r += 8) {
+        const int c = c0 + r, i = i0 + tx;
+        if (c < ldd && i < kpad) dstT[(size_t)c * ldt + i] = __float2bfloat16_rn(tile[tx][r]);
+    }
+}
+
+// Packed BF16 weights of the node layers, rebuilt whenever the parameters change:
+//   forward  B operands [nout_pad][kin_pad] = W^T with the bias in column kin (the activations
+//            carry a constant-1 column there);
+//   backward B operands [kin_pad][nout_pad] = W (the data gradient dX = dY W^T).
+constexpr int kTcK1 = 80, kTcK2 = 144, kTcKo = 80, kTcNo = 16;  // padded K of the node layers, N of the output
+constexpr int kWfN1 = 0, kWfP = kWfN1 + W * kTcK1, kWfN2 = kWfP + W * W, kWfO = kWfN2 + W * kTcK2,
+              kWfTotal = kWfO + kTcNo * kTcKo;
+constexpr int kWbN1 = 0, kWbP = kWbN1 + kTcK1 * W, kWbN2 = kWbP + W * W, kWbO = kWbN2 + 2 * W * W,
+              kWbTotal = kWbO + W * kTcNo;
+
+__device__ __forceinline__ float wfwd(const float* prm, int woff, int boff, int kin, int nout, int o, int k) {
+    if (o >= nout) return 0.0f;
+    if (k < kin) return prm[woff + k * nout + o];
+    return (k == kin && boff >= 0) ? prm[boff + o] : 0.0f;
+}
+
+__global__ void k_pack_weights(const float* __restrict__ prm, __nv_bfloat16* __restrict__ wf,
+                               __nv_bfloat16* __restrict__ wb) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < kWfTotal) {
+        float v;
+        if (t < kWfP) { const int o = t / kTcK1, k = t % kTcK1; v = wfwd(prm, kWn1, kBn1, W + FN, W, o, k); }
+        else if (t < kWfN2) { const int r = t - kWfP, o = r / W, k = r % W; v = wfwd(prm, kWp, -1, W, W, o, k); }
+        else if (t < kWfO) { const int r = t - kWfN2, o = r / kTcK2, k = r % kTcK2; v = wfwd(prm, kWn2, kBn2, 2 * W, W, o, k); }
+        else { const int r = t - kWfO, o = r / kTcKo, k = r % kTcKo; v = wfwd(prm, kWo, kBo, W, FO, o, k); }
+        wf[t] = __float2bfloat16_rn(v);
+    }
+    if (t < kWbTotal) {
+        float v;
+        if (t < kWbP) { const int k = t / W, o = t % W; v = k < W + FN ? prm[kWn1 + k * W + o] : 0.0f; }
+        else if (t < kWbN2) { const int r = t - kWbP; v = prm[kWp + r]; }
+        else if (t < kWbO) { const int r = t - kWbN2; v = prm[kWn2 + r]; }
+        else { const int r = t - kWbO, k = r / kTcNo, o = r % kTcNo; v = o < FO ? prm[kWo + k * FO + o] : 0.0f; }
+        wb[t] = __float2bfloat16_rn(v);
+    }
+}
+
+// Weight gradient from the split-K partials part[split][mpad][npad] of D = X^T dY: rows k < kin
+// go to gw[k][nout], row kin (the constant-1 column) to gb, summed over the splits in order.
+__global__ void __launch_bounds__(kT) k_tc_reduce(const float* __restrict__ part, int splits, int mpad, int npad,
+                                                 int kin, int nout, float* __restrict__ gw, float* __restrict__ gb) {
+    const int t = blockIdx.x * kT + threadIdx.x;
+    const int rows = gb ? kin + 1 : kin;
+    if (t >= rows * nout) return;
+    const int k = t / nout, o = t % nout;
+    float s = 0.0f;
+    for (int q = 0; q < splits; ++q) s += part[((size_t)q * mpad + k) * npad + o];
+    if (k < kin) gw[k * nout + o] = s;
+    else gb[o] = s;
+}
+
 }  // namespace
 
 // Workspace and passes of one training frame (up to n_max particles).
@@ -347,6 +428,19 @@ struct Trainer {
     unsigned long long *mask1 = nullptr, *mask2 = nullptr;
     int *rev_cnt = nullptr, *rev_off = nullptr, *rev_edges = nullptr;
     int splits = 64;
+    // BF16 tensor-core path of the node layers (use_tc): row-major operands with the bias column,
+    // transposed copies for the weight gradients (K = particles, padded to kpad), packed weights,
+    // split-K partials and the GEMM's error word.
+    bool use_tc = false;
+    int kpad_max = 0;
+    __nv_bfloat16 *X1b = nullptr, *H1b = nullptr, *X2b = nullptr, *H2b = nullptr;
+    __nv_bfloat16 *dOb = nullptr, *dY2b = nullptr, *dPb = nullptr, *dY1b = nullptr;
+    __nv_bfloat16 *X1bT = nullptr, *H1bT = nullptr, *X2bT = nullptr, *H2bT = nullptr;
+    __nv_bfloat16 *dOT = nullptr, *dY2T = nullptr, *dPT = nullptr, *dY1T = nullptr;
+    __nv_bfloat16 *Wf = nullptr, *Wb = nullptr;
+    float* tpart = nullptr;
+    uint32_t* tc_err = nullptr;
+    static constexpr int kTcSplits = 64;
 
     template <class T>
     static cudaError_t al(T** p, size_t n) { return cudaMalloc((void**)p, (n ? n : 1) * sizeof(T)); }
@@ -370,12 +464,26 @@ struct Trainer {
             if (r == cudaSuccess) r = cudaMemset(adam_m, 0, sizeof(float) * kParams);
             if (r == cudaSuccess) r = cudaMemset(adam_v, 0, sizeof(float) * kParams);
         }
+        // tensor-core path (forward operands always; transposed copies for training)
+        kpad_max = (nmax + 63) / 64 * 64;
+        const size_t kp = (size_t)kpad_max;
+        A(al(&X1b, n * kTcK1)); A(al(&H1b, n * W)); A(al(&X2b, n * kTcK2)); A(al(&H2b, n * kTcKo));
+        A(al(&Wf, (size_t)kWfTotal)); A(al(&Wb, (size_t)kWbTotal)); A(al(&tc_err, 1));
+        if (r == cudaSuccess) r = cudaMemset(tc_err, 0, sizeof(uint32_t));
+        if (train) {
+            A(al(&dOb, n * kTcNo)); A(al(&dY2b, n * W)); A(al(&dPb, n * W)); A(al(&dY1b, n * W));
+            A(al(&X1bT, kTcK1 * kp)); A(al(&H1bT, W * kp)); A(al(&X2bT, kTcK2 * kp)); A(al(&H2bT, kTcKo * kp));
+            A(al(&dOT, kTcNo * kp)); A(al(&dY2T, W * kp)); A(al(&dPT, W * kp)); A(al(&dY1T, W * kp));
+            A(al(&tpart, (size_t)kTcSplits * kTcK2 * W));
+        }
         return r;
     }
 
     ~Trainer() {
         void* ptrs[] = {prm, grad, adam_m, adam_v, E, X1, H1, P, X2, H2, O, dO, dY2, dX2, dZ2, dP, dY1, dX1,
-                        part, loss_part, mask1, mask2, rev_cnt, rev_off, rev_edges};
+                        part, loss_part, mask1, mask2, rev_cnt, rev_off, rev_edges,
+                        X1b, H1b, X2b, H2b, dOb, dY2b, dPb, dY1b, X1bT, H1bT, X2bT, H2bT, dOT, dY2T, dPT, dY1T,
+                        Wf, Wb, tpart, tc_err};
         for (void* q : ptrs)
             if (q) cudaFree(q);
     }
@@ -404,8 +512,116 @@ struct Trainer {
         k_reduce_split<<<nblk(total), kT, 0, st>>>(part, splits, total, grad + woff, FE * W, grad + boff);
     }
 
+    // ---- tensor-core path ----------------------------------------------------------------
+    static int kpad_of(int n) { return (n + 63) / 64 * 64; }
+
+    // BF16 copies of src [n][lds] (ncols columns; bias_col = 1): row-major dst [n][ldd] and/or
+    // the transposed dstT [ldd][kpad_max] (zero for particles n .. kpad - 1).
+    void pack(const float* src, int lds, int ncols, int n, int bias_col, __nv_bfloat16* dst, int ldd,
+              __nv_bfloat16* dstT, cudaStream_t st) {
+        const int rows = dstT ? kpad_of(n) : n;
+        const dim3 grid((unsigned)((rows + 31) / 32), (unsigned)((ldd + 31) / 32));
+        k_pack_bf16<<<grid, 256, 0, st>>>(src, lds, ncols, n, kpad_of(n), bias_col, dst, ldd, dstT, kpad_max);
+    }
+
+    void tc_gemm(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, int m, int nn, int k,
+                 const tc::Epilogue& e, cudaStream_t st) {
+        tc::gemm_bf16(A, lda, B, ldb, m, nn, k, e, 1, k, tc_err, st);
+    }
+    static tc::Epilogue epi(float* out, int ld, int ncols, int relu = 0) {
+        tc::Epilogue e;
+        e.out = out;
+        e.ld_out = ld;
+        e.ncols = ncols;
+        e.relu = relu;
+        return e;
+    }
+
+    // Weight gradient D = AT BT^T over the particles (AT [mpad][kpad_max], BT [npad][kpad_max],
+    // K = kpad(n)), split over K and reduced in order into grad[woff] (rows < kin) and
+    // grad[boff] (row kin).
+    void tc_wgrad(const __nv_bfloat16* AT, int mpad, const __nv_bfloat16* BT, int npad, int n, int kin, int nout,
+                  int woff, int boff, cudaStream_t st) {
+        const int k = kpad_of(n);
+        int kps = (k + kTcSplits - 1) / kTcSplits;
+        kps = (kps + 63) / 64 * 64;
+        const int sp = (k + kps - 1) / kps;
+        tc::Epilogue e;
+        e.out = tpart;
+        e.ld_out = npad;
+        e.ncols = npad;
+        e.split_stride = (long long)mpad * npad;
+        tc::gemm_bf16(AT, kpad_max, BT, kpad_max, mpad, npad, k, e, sp, kps, tc_err, st);
+        const int rows = boff >= 0 ? kin + 1 : kin;
+        k_tc_reduce<<<nblk((long long)rows * nout), kT, 0, st>>>(tpart, sp, mpad, npad, kin, nout, grad + woff,
+                                                                boff >= 0 ? grad + boff : nullptr);
+    }
+
+    void forward_tc(const Frame& f, bool train, cudaStream_t st) {
+        const int n = f.n;
+        k_pack_weights<<<nblk(kWfTotal), kT, 0, st>>>(prm, Wf, Wb);
+        k_edge1_fwd<<<nblk(n), kT, 0, st>>>(f, prm, E, mask1, X1);
+        pack(X1, W + FN, W + FN, n, W + FN, X1b, kTcK1, train ? X1bT : nullptr, st);
+        tc_gemm(X1b, kTcK1, Wf + kWfN1, kTcK1, n, W, kTcK1, epi(H1, W, W, 1), st);
+        pack(H1, W, W, n, -1, H1b, W, train ? H1bT : nullptr, st);
+        tc_gemm(H1b, W, Wf + kWfP, W, n, W, W, epi(P, W, W), st);
+        k_edge2_fwd<<<nblk(n), kT, 0, st>>>(f, prm, E, P, H1, mask2, X2);
+        pack(X2, 2 * W, 2 * W, n, 2 * W, X2b, kTcK2, train ? X2bT : nullptr, st);
+        tc_gemm(X2b, kTcK2, Wf + kWfN2, kTcK2, n, W, kTcK2, epi(H2, W, W, 1), st);
+        pack(H2, W, W, n, W, H2b, kTcKo, train ? H2bT : nullptr, st);
+        tc_gemm(H2b, kTcKo, Wf + kWfO, kTcKo, n, kTcNo, kTcKo, epi(O, kOS, FO), st);
+    }
+
+    void backward_tc(const Frame& f, cudaStream_t st) {
+        const int n = f.n;
+        k_loss<<<nblk(n), kT, 0, st>>>(O, f.target, n, dO, loss_part);
+        pack(dO, kOS, FO, n, -1, dOb, kTcNo, dOT, st);
+        tc_wgrad(H2bT, kTcKo, dOT, kTcNo, n, W, FO, kWo, kBo, st);
+        {  // dY2 = (dO Wo^T) * (H2 > 0)
+            tc::Epilogue e = epi(dY2, W, W);
+            e.gate = H2;
+            e.ld_gate = W;
+            tc_gemm(dOb, kTcNo, Wb + kWbO, kTcNo, n, W, kTcNo, e, st);
+        }
+        pack(dY2, W, W, n, -1, dY2b, W, dY2T, st);
+        tc_wgrad(X2bT, kTcK2, dY2T, W, n, 2 * W, W, kWn2, kBn2, st);
+        tc_gemm(dY2b, W, Wb + kWbN2, W, n, 2 * W, W, epi(dX2, 2 * W, 2 * W), st);  // dX2 = dY2 Wn2^T
+        k_edge2_bwd<<<nblk((long long)n * K * W), kT, 0, st>>>(dX2, mask2, f.cnt, n, dZ2);
+        edge_wgrad(dZ2, nullptr, 0, nullptr, f.cnt, n, kWe2, kBe2, st);
+        reverse_gather(f, st);
+        pack(dP, W, W, n, -1, dPb, W, dPT, st);
+        tc_wgrad(H1bT, W, dPT, W, n, W, W, kWp, -1, st);
+        {  // dY1 = (dX2[:, W:] + dP Wp^T) * (H1 > 0)
+            tc::Epilogue e = epi(dY1, W, W);
+            e.add = dX2 + W;
+            e.ld_add = 2 * W;
+            e.gate = H1;
+            e.ld_gate = W;
+            tc_gemm(dPb, W, Wb + kWbP, W, n, W, W, e, st);
+        }
+        pack(dY1, W, W, n, -1, dY1b, W, dY1T, st);
+        tc_wgrad(X1bT, kTcK1, dY1T, W, n, W + FN, W, kWn1, kBn1, st);
+        tc_gemm(dY1b, W, Wb + kWbN1, W, n, kTcK1, W, epi(dX1, W + FN, W + FN), st);  // dX1 = dY1 Wn1^T
+        edge_wgrad(nullptr, dX1, W + FN, mask1, f.cnt, n, kWe1, kBe1, st);
+    }
+
+    void reverse_gather(const Frame& f, cudaStream_t st) {
+        const int n = f.n;
+        cudaMemsetAsync(rev_cnt, 0, sizeof(int) * n, st);
+        k_rev_count<<<nblk((long long)n * K), kT, 0, st>>>(f.nb, f.cnt, n, rev_cnt);
+        k_scan_small<<<1, 1024, 0, st>>>(rev_cnt, n, rev_off);
+        cudaMemsetAsync(rev_cnt, 0, sizeof(int) * n, st);
+        k_rev_fill<<<nblk((long long)n * K), kT, 0, st>>>(f.nb, f.cnt, n, rev_off, rev_cnt, rev_edges);
+        k_rev_sort<<<nblk(n), kT, 0, st>>>(rev_off, n, rev_edges);
+        k_rev_gather<<<nblk((long long)n * W), kT, 0, st>>>(rev_off, rev_edges, dZ2, n, dP);
+    }
+
     // Forward: O (n x kOS) from the frame.
     void forward(const Frame& f, cudaStream_t st) {
+        if (use_tc) {
+            forward_tc(f, grad != nullptr, st);
+            return;
+        }
         const int n = f.n;
         k_edge1_fwd<<<nblk(n), kT, 0, st>>>(f, prm, E, mask1, X1);
         dense(X1, W + FN, W + FN, kWn1, kBn1, W, H1, W, n, 1, st);
@@ -417,6 +633,10 @@ struct Trainer {
 
     // Loss partials and the full parameter gradient (forward must have run).
     void backward(const Frame& f, cudaStream_t st) {
+        if (use_tc) {
+            backward_tc(f, st);
+            return;
+        }
         const int n = f.n;
         k_loss<<<nblk(n), kT, 0, st>>>(O, f.target, n, dO, loss_part);
         wgrad(H2, W, W, dO, kOS, FO, n, kWo, kBo, st);
@@ -426,13 +646,7 @@ struct Trainer {
                                                                     0, dX2, 2 * W, n);
         k_edge2_bwd<<<nblk((long long)n * K * W), kT, 0, st>>>(dX2, mask2, f.cnt, n, dZ2);
         edge_wgrad(dZ2, nullptr, 0, nullptr, f.cnt, n, kWe2, kBe2, st);
-        cudaMemsetAsync(rev_cnt, 0, sizeof(int) * n, st);
-        k_rev_count<<<nblk((long long)n * K), kT, 0, st>>>(f.nb, f.cnt, n, rev_cnt);
-        k_scan_small<<<1, 1024, 0, st>>>(rev_cnt, n, rev_off);
-        cudaMemsetAsync(rev_cnt, 0, sizeof(int) * n, st);
-        k_rev_fill<<<nblk((long long)n * K), kT, 0, st>>>(f.nb, f.cnt, n, rev_off, rev_cnt, rev_edges);
-        k_rev_sort<<<nblk(n), kT, 0, st>>>(rev_off, n, rev_edges);
-        k_rev_gather<<<nblk((long long)n * W), kT, 0, st>>>(rev_off, rev_edges, dZ2, n, dP);
+        reverse_gather(f, st);
         wgrad(H1, W, W, dP, W, W, n, kWp, -1, st);
         // dY1 = (dX2[:, W:] + dP Wp^T) * (H1 > 0)
         k_dense_bwd_data<<<nblk((long long)n * W), kT, 0, st>>>(dP, W, W, prm + kWp, W, dX2 + W, 2 * W, H1, W, dY1, W,
@@ -477,6 +691,15 @@ void trainer_reset_adam(Trainer* t) {
     if (t->adam_v) cudaMemset(t->adam_v, 0, sizeof(float) * kParams);
 }
 int trainer_capacity(Trainer* t) { return t->n_max; }
+void trainer_set_tc(Trainer* t, bool on) { t->use_tc = on; }
+bool trainer_tc(Trainer* t) { return t->use_tc; }
+uint32_t trainer_tc_error(Trainer* t, cudaStream_t st) {
+    uint32_t e = 0;
+    cudaMemcpyAsync(&e, t->tc_err, sizeof(e), cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    if (e) cudaMemsetAsync(t->tc_err, 0, sizeof(e), st);
+    return e;
+}
 void trainer_forward(Trainer* t, const Frame& f, cudaStream_t st) { t->forward(f, st); }
 double trainer_loss_grad(Trainer* t, const Frame& f, cudaStream_t st) {
     t->forward(f, st);

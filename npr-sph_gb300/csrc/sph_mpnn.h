@@ -106,6 +106,12 @@ float* trainer_params(Trainer* t);  // device, kParams floats
 float* trainer_grad(Trainer* t);    // device, kParams floats (train only)
 float* trainer_out(Trainer* t);     // device, [n][kOS]: O of the last forward
 void trainer_reset_adam(Trainer* t);
+// Node layers (forward, data and weight gradients) on the BF16 tensor cores (tcgen05, FP32
+// accumulation; FP32 master weights) instead of FP32 CUDA cores.
+void trainer_set_tc(Trainer* t, bool on);
+bool trainer_tc(Trainer* t);
+// Nonzero if a tensor-core wait timed out since the last call (synchronous; clears the word).
+uint32_t trainer_tc_error(Trainer* t, cudaStream_t st);
 void trainer_forward(Trainer* t, const Frame& f, cudaStream_t st);
 double trainer_loss_grad(Trainer* t, const Frame& f, cudaStream_t st);  // synchronous (reads the loss)
 void trainer_adam(Trainer* t, int step, float lr, cudaStream_t st);

@@ -1,0 +1,148 @@
+// sph_tc.cuh -- Blackwell (sm_103a) tensor-core building blocks in inline PTX:
+// tcgen05 MMA of BF16 operands from shared memory with the FP32 accumulator in
+// tensor memory (TMEM), its completion mbarrier, TMEM allocation and TMEM loads.
+//
+// Operand layout in shared memory (canonical K-major layout without swizzle):
+// a tile of R rows x KC bf16 is a grid of 8 x 8 core matrices, each 8 rows of
+// 16 bytes stored as 128 contiguous bytes. Element (r, k) sits at byte
+//     (r / 8) * SBO + (k / 8) * LBO + (r % 8) * 16 + (k % 8) * 2
+// with LBO = 128 (core matrices adjacent along K are adjacent in memory) and
+// SBO = KC * 16 (the next 8-row group follows all of a row group's K core
+// matrices). One MMA consumes K = 16, i.e. two core-matrix columns: the k-th
+// MMA of a staged chunk starts 256 * k bytes into the tile.
+//
+// The accumulator of an M = 128 MMA (cta_group::1) holds row i of D in TMEM
+// lane i, column j in column base + j (FP32); warp w of the CTA reads lanes
+// 32 w .. 32 w + 31 (tcgen05.ld 32x32b).
+//
+// Waits on an mbarrier are bounded by the global timer: a wait that runs out
+// reports failure instead of spinning on, so a kernel can raise an error flag,
+// release its TMEM and return.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sphgb {
+namespace tc {
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Byte offset of the 16-byte chunk (r, k8) -- row r, elements 8 k8 .. 8 k8 + 7 -- of an
+// R x KC tile in the canonical layout.
+__host__ __device__ constexpr uint32_t tile_off(int r, int k8, int kc) {
+    return (uint32_t)((r >> 3) * (kc * 16) + k8 * 128 + (r & 7) * 16);
+}
+
+// Shared-memory matrix descriptor: start address, leading (K) byte offset, stride (M/N) byte
+// offset, all in 16-byte units; bits 46-47 = 1 (the tcgen05 descriptor version); base offset 0,
+// layout type 0 (no swizzle).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)((lbo & 0x3FFFFu) >> 4) << 16;
+    d |= (uint64_t)((sbo & 0x3FFFFu) >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// Instruction descriptor of tcgen05.mma kind::f16: D FP32 (bits 4-5 = 1), A and B BF16
+// (bits 7-9, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at
+// bits 24-28.
+__host__ __device__ constexpr uint32_t idesc_bf16_f32(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+// D[tmem] (+)= A[desc] * B[desc]^T, issued by one thread. accumulate = 0 overwrites D.
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate));
+}
+
+// Arrive on the mbarrier once every MMA this thread issued before has completed.
+__device__ __forceinline__ void mma_commit(uint64_t* mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                     smem_u32(mbar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* mbar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(mbar)), "r"(count) : "memory");
+}
+
+// Make the barrier initialisation visible to the tensor core's (async) proxy.
+__device__ __forceinline__ void mbar_init_fence() {
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* mbar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(mbar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+    return t;
+}
+
+// Wait for the completion of the phase with the given parity, for at most limit_ns
+// nanoseconds. Returns false when the limit ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, uint64_t limit_ns = 2000000000ull) {
+    if (mbar_try_wait(mbar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    while (!mbar_try_wait(mbar, parity))
+        if (global_ns() - t0 > limit_ns) return false;
+    return true;
+}
+
+// Shared-memory writes of the CTA's threads become visible to the tensor core.
+__device__ __forceinline__ void fence_smem_to_async() {
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+}
+__device__ __forceinline__ void fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+
+// TMEM allocation of ncols columns (a power of two >= 32) by one whole warp; the address is
+// written to *slot (shared memory).
+__device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(slot)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+// 16 consecutive FP32 columns of the warp's 32 lanes (one lane per thread).
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
+
+__host__ __device__ constexpr uint32_t tmem_cols_for(int n) {
+    return n <= 32 ? 32u : n <= 64 ? 64u : n <= 128 ? 128u : n <= 256 ? 256u : 512u;
+}
+
+}  // namespace tc
+}  // namespace sphgb

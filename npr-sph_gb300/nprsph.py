@@ -132,6 +132,8 @@ _SIGS = {
     "sph_mpnn_loss_grad": (C.c_int32, [_P, C.c_uint32, _P, _P, _P, _P, _P, _P, _P, C.POINTER(C.c_double), _P, _P]),
     "sph_mpnn_forward": (C.c_int32, [_P, C.c_uint32, _P, _P, _P, _P, _P, _P, C.c_int32, _P]),
     "sph_mpnn_set_precision": (C.c_int32, [_P, C.c_int32]),
+    "sph_mpnn_set_train_precision": (C.c_int32, [_P, C.c_int32]),
+    "sph_tc_gemm_bf16": (C.c_int32, [_P, _P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P]),
     "sph_mpnn_record": (C.c_int32, [_P, _P, C.c_uint32, C.POINTER(C.c_uint32)]),
     "sph_mpnn_clear_frames": (C.c_int32, [_P]),
     "sph_mpnn_train": (C.c_int32, [_P, C.c_uint32, C.c_float, C.c_uint64, _P]),
@@ -214,6 +216,28 @@ def grid_dims(p: Params) -> tuple[float, tuple[int, int, int]]:
     d = (C.c_int32 * 3)()
     _check(lib.sph_grid_dims(C.byref(p), C.byref(e), d), what="sph_grid_dims")
     return float(e.value), (d[0], d[1], d[2])
+
+
+def to_bf16_bits(a: np.ndarray) -> np.ndarray:
+    """float32 -> bf16 bit patterns (uint16), round to nearest even (finite inputs)."""
+    u = np.ascontiguousarray(a, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    return ((u + 0x7FFF + ((u >> 16) & 1)) >> 16).astype(np.uint16)
+
+
+def bf16_bits_to_f32(b: np.ndarray) -> np.ndarray:
+    return (np.asarray(b, dtype=np.uint32) << 16).view(np.float32)
+
+
+def tc_gemm(a_bits: np.ndarray, b_bits: np.ndarray, splits: int = 1) -> np.ndarray:
+    """D = A B^T on the tensor cores (sph_tc_gemm_bf16): A (m x k), B (n x k) bf16 bits;
+    returns (splits, m, n) FP32 partials."""
+    a = np.ascontiguousarray(a_bits, dtype=np.uint16)
+    b = np.ascontiguousarray(b_bits, dtype=np.uint16)
+    m, k = a.shape
+    n = b.shape[0]
+    d = np.zeros((splits, m, n), dtype=np.float32)
+    _check(lib.sph_tc_gemm_bf16(a.ctypes.data, b.ctypes.data, m, n, k, splits, d.ctypes.data), what="sph_tc_gemm_bf16")
+    return d
 
 
 def empty_particles(n: int) -> np.ndarray:
@@ -618,6 +642,10 @@ class Net:
 
     def set_precision(self, precision: int) -> None:
         self._check(lib.sph_mpnn_set_precision(self._h, precision))
+
+    def set_train_precision(self, precision: int) -> None:
+        """1: node layers of the training passes on the BF16 tensor cores (default); 0: FP32."""
+        self._check(lib.sph_mpnn_set_train_precision(self._h, precision))
 
     def record(self, sim: Sim, n_frames: int) -> int:
         tot = C.c_uint32()

@@ -51,6 +51,7 @@ def test_forward_and_gradient_match_fp64_oracle(sph, gpu):
     tg8 = np.zeros((n, 8), np.float32); tg8[:, :MO.FO] = target
     with sph.Net(128) as net:
         net.set_params(flat)
+        net.set_train_precision(0)  # every layer in FP32 on the CUDA cores
         loss, out, grad = net.loss_grad(pos4, vel4, rhop, nb, cnt, tg8, fc)
     e, mask, nf = MO.features(f32(pos), f32(vel), f32(rho), nb, cnt, *[float(np.float32(x)) for x in fc[:2]],
                               float(np.float32(fc[2])), float(np.float32(fc[3])), 3000.0, frame_dt(fc))
@@ -64,6 +65,48 @@ def test_forward_and_gradient_match_fp64_oracle(sph, gpu):
         g, r = grad[off:off + size], ref_grad[off:off + size]
         scale = np.abs(r).max() + 1e-12
         assert np.max(np.abs(g - r)) <= 2e-4 * scale, (name, np.max(np.abs(g - r)) / scale)
+        off += size
+
+
+# BF16 tolerances of the tensor-core training path against the FP64 restatement: the node
+# layers round their operands (activations, gradients, weights) to 8 mantissa bits before the
+# FP32-accumulated GEMMs, so outputs and gradients agree to a few percent of their scale.
+TC_OUT_TOL, TC_GRAD_TOL, TC_LOSS_RTOL, TC_GRAD_CORR = 3e-2, 6e-2, 3e-2, 0.995
+
+
+@pytest.mark.parametrize("seed", [3, 8])
+def test_tensor_core_training_matches_fp64_oracle(sph, gpu, seed):
+    """The training passes with the node layers on the BF16 tcgen05 GEMMs (the default training
+    precision): outputs, loss and every layer's gradient against the FP64 restatement."""
+    from oracle import mpnn_oracle as MO
+
+    pos, vel, rho, nb, cnt, target, fc = random_frame(seed, n=300)
+    n = len(pos)
+    f32 = lambda a: np.asarray(a, np.float32).astype(np.float64)
+    flat = MO.init_params(seed + 4)
+    pos4 = np.zeros((n, 4), np.float32); pos4[:, :3] = pos
+    vel4 = np.zeros((n, 4), np.float32); vel4[:, :3] = vel
+    rhop = np.zeros((n, 2), np.float32); rhop[:, 0] = rho
+    tg8 = np.zeros((n, 8), np.float32); tg8[:, :MO.FO] = target
+    with sph.Net(512) as net:
+        net.set_params(flat)
+        loss, out, grad = net.loss_grad(pos4, vel4, rhop, nb, cnt, tg8, fc)
+        fwd = net.forward(pos4, vel4, rhop, nb, cnt, fc, precision=2)
+    np.testing.assert_array_equal(fwd, out)  # the same forward pass
+    e, mask, nf = MO.features(f32(pos), f32(vel), f32(rho), nb, cnt, *[float(np.float32(x)) for x in fc[:2]],
+                              float(np.float32(fc[2])), float(np.float32(fc[3])), 3000.0, frame_dt(fc))
+    ref_loss, ref_out, ref_grad = MO.loss_and_grad(flat.astype(np.float64), e, mask, nf, nb, f32(target))
+    assert np.abs(out[:, :MO.FO] - ref_out).max() <= TC_OUT_TOL * np.abs(ref_out).max()
+    assert np.all(out[:, MO.FO:] == 0.0)
+    assert loss == pytest.approx(ref_loss, rel=TC_LOSS_RTOL)
+    off = 0
+    for name, shape in MO.LAYOUT:
+        size = int(np.prod(shape))
+        g, r = grad[off:off + size].astype(np.float64), ref_grad[off:off + size]
+        scale = np.abs(r).max() + 1e-12
+        assert np.max(np.abs(g - r)) <= TC_GRAD_TOL * scale, (name, np.max(np.abs(g - r)) / scale)
+        if size > 8:
+            assert np.corrcoef(g, r)[0, 1] > TC_GRAD_CORR, name
         off += size
 
 
