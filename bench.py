@@ -447,6 +447,22 @@ def learned_workload(args, stream, flush) -> dict:
             runs[name] = summary(reps, t_l, t_p, rl, rp)
         learned.set_judge(S.JUDGE_PARTICLE_DENSITY)
         learned.set_max_density_tol(float("inf"))
+        # One unjudged macro-step (sort, neighbour lists, two inference rounds, update) with each
+        # BF16 inference kernel set, from the same state, CUDA events over 8 macro-steps.
+        kernels = {}
+        for name, prec in (("mma_sync", 1), ("tcgen05", 2)):
+            net.set_precision(prec)
+            learned.upload(sc.particles)
+            learned.step(args.warmup)
+            learned.learned_step(net, 2, 0)
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            learned.learned_step(net, 8, 0)
+            b.record(stream)
+            torch.cuda.synchronize()
+            kernels[name] = {"ms_per_macro_step": a.elapsed_time(b) / 8}
+        net.set_precision(1)
         # What the network gains: one judged macro-step from the same state (the plain run's
         # end state) with the trained network and with a zero network (v' = v, x' = x + 4 dt v,
         # then the momentum projection adds gravity).
@@ -463,7 +479,9 @@ def learned_workload(args, stream, flush) -> dict:
         "plain_value": n * 32 * units / t_p, "plain_ms_per_dt": 1e3 * t_p / (32 * units),
         "judge_mean_density": runs["judge_mean_density"],
         "one_macro_step_vs_4_plain_steps": gain,
-        "precision": "BF16 weights/activations, FP32 accumulate (mma.sync m16n8k16)",
+        "inference_kernels": kernels,
+        "precision": "BF16 weights/activations, FP32 accumulate (mma.sync m16n8k16; the tcgen05 kernels are "
+                     "timed in inference_kernels)",
         "weights": str(WEIGHTS.relative_to(REPO)),
     })
     return out

@@ -59,9 +59,11 @@ struct sph_mpnn {
     void* harena = nullptr;
     int adam_t = 0;  // Adam steps taken since the parameters were last set
     // BF16 tensor-core inference
-    int precision = 1;               // inference: 1 BF16 tensor cores (default), 0 FP32 CUDA cores
+    int precision = 1;               // inference: 1 BF16 mma.sync (default), 2 BF16 tcgen05, 0 FP32 CUDA cores
     int train_precision = 1;         // training node layers: 1 BF16 tcgen05 GEMMs (default), 0 FP32
-    uint32_t* frags = nullptr;       // parameters in MMA fragment order
+    uint32_t* frags = nullptr;       // parameters in MMA fragment order (mma.sync kernels)
+    __nv_bfloat16* tcw = nullptr;    // parameters as tcgen05 shared-memory images
+    uint32_t* tc_err = nullptr;      // bit 0: a tensor-core wait of the inference timed out
     bool frags_dirty = true;
     __nv_bfloat16* H1b = nullptr;    // [n][64]
     uint16_t* Pperm = nullptr;       // [n][64], permuted
@@ -330,6 +332,9 @@ cudaError_t ensure_host_arena(sph_mpnn* net, uint32_t n) {
 sph_status ensure_bf16(sph_mpnn* net, int n, cudaStream_t st) {
     if (!net->frags) {
         NCK(cudaMalloc(&net->frags, sizeof(uint32_t) * M::infer_frag_words()));
+        NCK(cudaMalloc(&net->tcw, sizeof(__nv_bfloat16) * M::tc_infer_words()));
+        NCK(cudaMalloc(&net->tc_err, sizeof(uint32_t)));
+        NCK(cudaMemsetAsync(net->tc_err, 0, sizeof(uint32_t), st));
         net->frags_dirty = true;
     }
     if (n > net->bcap) {
@@ -343,6 +348,7 @@ sph_status ensure_bf16(sph_mpnn* net, int n, cudaStream_t st) {
     }
     if (net->frags_dirty) {
         M::infer_prep(M::trainer_params(net->tr), net->frags, st);
+        M::tc_infer_prep(M::trainer_params(net->tr), net->tcw, st);
         net->frags_dirty = false;
     }
     return SPH_OK;
@@ -356,7 +362,12 @@ sph_status learned_macro(sph_ctx* ctx, sph_mpnn* net) {
     M::Frame f{ctx->b.pos_s, ctx->b.vel_s, ctx->b.rhop, net->nb, net->cnt, nullptr, n,
                frame_const(ctx->s0, ctx->params[0].visc)};
     const float* O = nullptr;
-    if (net->precision == 1) {
+    if (net->precision == 2) {
+        M::tc_infer_round1(f, net->tcw, net->H1b, reinterpret_cast<__half*>(net->Pperm), net->tc_err, ctx->stream);
+        M::tc_infer_round2(f, net->tcw, net->H1b, reinterpret_cast<const __half*>(net->Pperm), net->Obuf, net->tc_err,
+                           ctx->stream);
+        O = net->Obuf;
+    } else if (net->precision == 1) {
         M::infer_round1(f, net->frags, net->H1b, net->Pperm, ctx->stream);
         M::infer_round2(f, net->frags, M::trainer_params(net->tr), net->H1b, net->Pperm, ctx->s0, nullptr, nullptr,
                         net->Obuf, nullptr, nullptr, nullptr, false, ctx->stream);
@@ -477,7 +488,7 @@ sph_status sph_mpnn_destroy(sph_mpnn* net) {
     void* ptrs[] = {net->nb, net->cnt, net->snap_pos, net->snap_vel, net->snap_rhop, net->ck_pos, net->ck_vel,
                     net->ck_rhop, net->l_pos, net->l_vel,
                     net->l_rhop, net->acc, net->accx, net->Obuf, net->osum, net->ocorr, net->rho_l, net->rho_p, net->vel_l, net->vel_p, net->cmp, net->harena,
-                    net->frags, net->H1b, net->Pperm};
+                    net->frags, net->H1b, net->Pperm, net->tcw, net->tc_err};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (net->own_stream) cudaStreamDestroy(net->stream);
@@ -551,7 +562,7 @@ sph_status sph_mpnn_loss_grad(sph_mpnn* net, uint32_t n, const float* pos4, cons
 }
 
 sph_status sph_mpnn_set_precision(sph_mpnn* net, int32_t precision) {
-    if (!net || (precision != 0 && precision != 1)) return SPH_ERR_INVALID_ARG;
+    if (!net || precision < 0 || precision > 2) return SPH_ERR_INVALID_ARG;
     net->precision = precision;
     return SPH_OK;
 }
@@ -566,7 +577,7 @@ sph_status sph_mpnn_set_train_precision(sph_mpnn* net, int32_t precision) {
 sph_status sph_mpnn_forward(sph_mpnn* net, uint32_t n, const float* pos4, const float* vel4, const float* rhop2,
                             const int32_t* nb, const int32_t* cnt, const float fc[6], int32_t precision, float* out8) {
     if (!net || !pos4 || !vel4 || !rhop2 || !nb || !cnt || !fc || !out8 || n == 0) return SPH_ERR_INVALID_ARG;
-    if (precision < 0 || precision > 2) return SPH_ERR_INVALID_ARG;
+    if (precision < 0 || precision > 3) return SPH_ERR_INVALID_ARG;
     if ((int)n > M::trainer_capacity(net->tr)) { net->err = "frame larger than the training workspace"; return SPH_ERR_CAPACITY; }
     for (uint32_t i = 0; i < n; ++i) {
         if (cnt[i] < 0 || cnt[i] > M::K) { net->err = "neighbour count out of [0, 32]"; return SPH_ERR_INVALID_ARG; }
@@ -592,7 +603,21 @@ sph_status sph_mpnn_forward(sph_mpnn* net, uint32_t n, const float* pos4, const 
     NCK(cudaMemcpyAsync(dcnt, cnt, (size_t)n * 4, cudaMemcpyHostToDevice, st));
     NCK(cudaMemcpyAsync(dnb, nb, (size_t)n * M::K * 4, cudaMemcpyHostToDevice, st));
     M::Frame f{dpos, dvel, drh, dnb, dcnt, nullptr, (int)n, {fc[0], fc[1], fc[2], fc[3], fc[4], fc[5]}};
-    if (precision == 1) {
+    if (precision == 3) {  // the tcgen05 inference kernels
+        sph_status s2 = ensure_bf16(net, (int)n, st);
+        if (s2) return s2;
+        M::tc_infer_round1(f, net->tcw, net->H1b, reinterpret_cast<__half*>(net->Pperm), net->tc_err, st);
+        M::tc_infer_round2(f, net->tcw, net->H1b, reinterpret_cast<const __half*>(net->Pperm), dout, net->tc_err, st);
+        NCK(cudaMemcpyAsync(out8, dout, (size_t)n * 4 * M::kOS, cudaMemcpyDeviceToHost, st));
+        uint32_t e = 0;
+        NCK(cudaMemcpyAsync(&e, net->tc_err, sizeof(e), cudaMemcpyDeviceToHost, st));
+        NCK(cudaStreamSynchronize(st));
+        if (e) {
+            cudaMemsetAsync(net->tc_err, 0, sizeof(e), st);
+            net->err = "tensor-core inference wait timed out";
+            return SPH_ERR_DEVICE;
+        }
+    } else if (precision == 1) {  // the macro-step's default inference: the mma.sync kernels
         sph_status s2 = ensure_bf16(net, (int)n, st);
         if (s2) return s2;
         SceneDev S{};
@@ -776,7 +801,7 @@ sph_status sph_learned_step(sph_ctx* ctx, sph_mpnn* net, int32_t n_macro, int32_
             return fail(ctx, SPH_ERR_CUDA, "copy of the network parameters");
     }
     sph_status st = ensure_ctx_scratch(net, n);
-    if (!st && net->precision == 1) st = ensure_bf16(net, n, ctx->stream);
+    if (!st && net->precision >= 1) st = ensure_bf16(net, n, ctx->stream);
     if (st) return fail(ctx, st, net->err);
     sph_learned_report r{};
     int& backoff = ctx->judge_backoff;    // plain intervals still to run before the next learned attempt
@@ -840,6 +865,16 @@ sph_status sph_learned_step(sph_ctx* ctx, sph_mpnn* net, int32_t n_macro, int32_
     if (rep) *rep = r;
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(ctx, SPH_ERR_CUDA, std::string("learned step: ") + cudaGetErrorString(e));
+    if (net->tc_err) {
+        uint32_t te = 0;
+        if (cudaMemcpyAsync(&te, net->tc_err, sizeof(te), cudaMemcpyDeviceToHost, ctx->stream) ||
+            cudaStreamSynchronize(ctx->stream))
+            return fail(ctx, SPH_ERR_CUDA, "learned step: error word readback");
+        if (te) {
+            cudaMemsetAsync(net->tc_err, 0, sizeof(te), ctx->stream);
+            return fail(ctx, SPH_ERR_DEVICE, "learned step: a tensor-core wait of the inference timed out");
+        }
+    }
     return engine::check_device_error(ctx);
 }
 

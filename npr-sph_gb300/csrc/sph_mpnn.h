@@ -24,6 +24,7 @@
 
 #include <cstdint>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "sph_internal.h"
@@ -127,6 +128,17 @@ void infer_round1(const Frame& f, const uint32_t* frags, __nv_bfloat16* H1, uint
 void infer_round2(const Frame& f, const uint32_t* frags, const float* prm, const __nv_bfloat16* H1,
                   const uint16_t* Pperm, const SceneDev& S, float4* pos_out, float4* vel_out, float* out, int* key,
                   int* rank, int* count, bool integrate, cudaStream_t st);
+
+// BF16 tcgen05 inference (sph_mpnn_tc.cu): the weights as bf16 images in the tensor cores'
+// shared-memory layout (tc_infer_words() elements, rebuilt by tc_infer_prep when the parameters
+// change); round 1 writes H1 (bf16 [n][64]) and P (f16 [n][64]), round 2 the outputs O
+// ([n][kOS]). *err gets bit 0 if a tensor-core wait timed out.
+int tc_infer_words();
+void tc_infer_prep(const float* prm, __nv_bfloat16* img, cudaStream_t st);
+void tc_infer_round1(const Frame& f, const __nv_bfloat16* img, __nv_bfloat16* H1, __half* P, uint32_t* err,
+                     cudaStream_t st);
+void tc_infer_round2(const Frame& f, const __nv_bfloat16* img, const __nv_bfloat16* H1, const __half* P, float* out,
+                     uint32_t* err, cudaStream_t st);
 
 }  // namespace mpnn
 }  // namespace sphgb

@@ -110,11 +110,12 @@ def test_tensor_core_training_matches_fp64_oracle(sph, gpu, seed):
         off += size
 
 
-@pytest.mark.parametrize("seed", [5, 6])
-def test_bf16_tensor_core_inference_matches_fp32_forward(sph, gpu, seed):
-    """The macro-step's inference kernels (BF16 mma.sync, FP32 accumulate) against the FP32
-    forward on the same frame: BF16 rounds weights and activations to 8 mantissa bits, so the
-    outputs agree to a few percent of their scale."""
+@pytest.mark.parametrize("seed,precision", [(5, 1), (6, 1), (5, 3), (6, 3)])
+def test_bf16_tensor_core_inference_matches_fp32_forward(sph, gpu, seed, precision):
+    """The inference kernels -- precision 1: the macro-step's default mma.sync kernels (BF16,
+    FP32 accumulation); 3: the tcgen05 kernels (BF16 MMAs, FP32 accumulation in TMEM, f16 edge
+    sums) -- against the FP32 forward on the same frame: BF16 rounds weights and activations to
+    8 mantissa bits, so the outputs agree to a few percent of their scale."""
     from oracle import mpnn_oracle as MO
 
     pos, vel, rho, nb, cnt, target, fc = random_frame(seed, n=200)
@@ -125,13 +126,60 @@ def test_bf16_tensor_core_inference_matches_fp32_forward(sph, gpu, seed):
     with sph.Net(256) as net:
         net.set_params(MO.init_params(seed))
         o32 = net.forward(pos4, vel4, rhop, nb, cnt, fc, precision=0)[:, :MO.FO]
-        o16 = net.forward(pos4, vel4, rhop, nb, cnt, fc, precision=1)[:, :MO.FO]
+        o16 = net.forward(pos4, vel4, rhop, nb, cnt, fc, precision=precision)[:, :MO.FO]
     scale = np.abs(o32).max()
     assert scale > 0
     err = np.abs(o16 - o32).max() / scale
     assert err < 0.05, err
     corr = np.corrcoef(o16.ravel(), o32.ravel())[0, 1]
     assert corr > 0.999, corr
+
+
+# BF16 inference against the FP64 network on a frame recorded from the plain step: the
+# outputs agree to INF_TOL of their scale element by element and to INF_RMS in RMS.
+INF_TOL, INF_RMS, INF_CORR = 5e-2, 1.5e-2, 0.999
+WEIGHTS = __import__("pathlib").Path(__file__).resolve().parents[1] / "npr-sph_gb300" / "weights" / "mpnn_w64.npy"
+
+
+@pytest.mark.parametrize("steps,precision", [(8, 1), (60, 1), (8, 3), (60, 3)])
+def test_tensor_core_inference_matches_fp64_oracle_on_dam_break(sph, gpu, steps, precision):
+    """The BF16 inference kernels (precision 1: mma.sync, the macro-step's default; 3: tcgen05)
+    with the committed trained weights, on the neighbour lists, densities and state of a
+    16,384-particle dam break after `steps` plain steps, against oracle/mpnn_oracle.py in FP64
+    on the same inputs."""
+    from oracle import mpnn_oracle as MO
+
+    if not WEIGHTS.exists():
+        pytest.skip("no trained weights")
+    w = np.load(WEIGHTS).astype(np.float32)
+    sc = sph.dam_break(16, 32, 32, seed=41)
+    p = sc.params
+    with sph.Sim(p, n_max=len(sc.particles)) as sim:
+        sim.upload(sc.particles)
+        sim.step(steps)
+        nb, cnt, rho = sim.neighbor_lists()
+        rec = sim.download()
+    n = len(rec)
+    h = p.h
+    c = float(np.sqrt(np.float32(p.gas_const)))
+    rho_self = float(p.mass) * 315.0 / (64.0 * np.pi * h ** 3)
+    fc = np.array([h, c, rho_self, p.resting_rho, np.log10(p.visc) / 4.0, c * p.dt / h], np.float32)
+    pos4 = np.ascontiguousarray(rec["pos"], np.float32)
+    vel4 = np.ascontiguousarray(rec["vel"], np.float32)
+    rhop = np.zeros((n, 2), np.float32)
+    rhop[:, 0] = rho
+    assert cnt.max() > 16 and np.all(nb[np.arange(32)[None, :] >= cnt[:, None]] == -1)
+    with sph.Net(n) as net:
+        net.set_params(w)
+        got = net.forward(pos4, vel4, rhop, nb, cnt, fc, precision=precision)[:, :MO.FO].astype(np.float64)
+    f64 = lambda a: np.asarray(a, np.float32).astype(np.float64)
+    e, mask, nf = MO.features(f64(pos4[:, :3]), f64(vel4[:, :3]), f64(rho), nb, cnt, *[float(x) for x in fc[:4]],
+                              float(p.visc), float(fc[5]) * float(fc[0]) / float(fc[1]))
+    ref, _ = MO.forward(w.astype(np.float64), e, mask, nf, nb)
+    scale = np.abs(ref).max()
+    assert np.abs(got - ref).max() <= INF_TOL * scale, np.abs(got - ref).max() / scale
+    assert np.sqrt(np.mean((got - ref) ** 2)) <= INF_RMS * scale
+    assert np.corrcoef(got.ravel(), ref.ravel())[0, 1] > INF_CORR
 
 
 @pytest.fixture(scope="module")
