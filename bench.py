@@ -291,12 +291,13 @@ def render_workload(stream, frames: int = 20) -> dict:
 WEIGHTS = REPO / "npr-sph_gb300" / "weights" / "mpnn_w64.npy"
 
 
-def slosh_study(args, stream) -> dict:
+def slosh_study(args, stream, total: int = 2000, every: int = 200) -> dict:
     """Learned vs plain on the 16,777,216-particle slosh (256^3 lattice at 0.5h in a 2:1:1 box,
-    v_x = 0.5 sin(pi x / L)): 2,000 dt-equivalents each from the same state (the learned path
-    judged every 8 macro-steps: 1% mean density, 5% maximum density, 5% momentum). Every 200 dt: the
-    FP64 GPU reductions of both runs (momentum, energy, density drift from t = 0) and the
-    learned run's density deviation from the plain run by particle id (mean and max)."""
+    v_x = 0.5 sin(pi x / L)): `total` dt-equivalents each from the same state (the learned path
+    judged every 8 macro-steps: 1% per-particle density deviation, 5% maximum density, 5%
+    momentum). Every `every` dt: the FP64 GPU reductions of both runs (momentum, energy, density
+    drift from t = 0) and the learned run's density deviation from the plain run by particle id
+    (mean and max)."""
     import torch
     import nprsph as S
 
@@ -305,7 +306,6 @@ def slosh_study(args, stream) -> dict:
     params = np.load(WEIGHTS).astype(np.float32)
     sc = S.slosh_block(256, seed=5)
     n = len(sc.particles)
-    every, total = 200, 2000
 
     def diag(sim):
         d = sim.reduce()
@@ -356,11 +356,66 @@ def slosh_study(args, stream) -> dict:
             })
     nl = sum(r.learned_macro_steps for r in reps)
     npl = sum(r.plain_macro_steps for r in reps)
-    return {"workload": "slosh 256^3 = 16,777,216 particles, 2:1:1 box, v_x = 0.5 sin(pi x / L), 2,000 dt-equivalents",
+    return {"workload": f"slosh 256^3 = 16,777,216 particles, 2:1:1 box, v_x = 0.5 sin(pi x / L), {total} dt-equivalents",
             "particles": n, "plain_updates_per_s": n * total / t_plain, "learned_updates_per_s": n * total / t_learned,
             "learned_macro_steps": nl, "plain_macro_steps": npl, "judged": sum(r.judged for r in reps),
             "fallbacks": sum(r.fallbacks for r in reps), "checkpoints": rows,
             "drift_reference": "FP64 GPU reductions (sph_reduce) of each run against its own t = 0"}
+
+
+CROP_STEPS = 20
+
+
+def slosh_crop_fp64(stream) -> dict:
+    """The precision study's CPU leg: a 1,048,576-particle crop of the 16.8M slosh (the corner
+    column x < 64 s, z < 64 s of the 256^3 lattice, in the slosh's box), 20 dt of plain FP32 GPU
+    steps and of learned BF16 macro-steps (unjudged), each against 20 FP64 CPU oracle steps
+    from the same state: mean and max per-particle density error, momentum and kinetic-energy
+    difference."""
+    import nprsph as S
+    from oracle import oracle as O
+
+    if not WEIGHTS.exists():
+        return {"unavailable": f"no trained weights at {WEIGHTS.relative_to(REPO)}"}
+    sc = S.slosh_block(256, seed=5)
+    s = 0.5 * sc.params.h
+    p = sc.particles
+    part = np.ascontiguousarray(p[(p["pos"][:, 0] < 64 * s) & (p["pos"][:, 2] < 64 * s)])
+    n = len(part)
+    params = sc.params
+    pos = np.ascontiguousarray(part["pos"][:, :3], dtype=np.float64)
+    vel = np.ascontiguousarray(part["vel"][:, :3], dtype=np.float64)
+    t0 = time.perf_counter()
+    O.run_f64(params, pos, vel, CROP_STEPS)
+    fin = S.empty_particles(n)
+    fin["pos"][:, :3] = pos
+    fin["pos"][:, 3] = 1.0
+    rho64 = O.step_f64(params, fin)["rho"]
+    cpu_s = time.perf_counter() - t0
+    m = float(np.float32(params.mass))
+
+    def errors(g):
+        rho = g["extras"][:, 0].astype(np.float64)
+        v = g["vel"][:, :3].astype(np.float64)
+        d = np.abs(rho - rho64) / rho64
+        return {"density_err_mean": float(d.mean()), "density_err_max": float(d.max()),
+                "momentum_diff_rel": float(np.linalg.norm(m * v.sum(0) - m * vel.sum(0)) / (m * np.abs(vel).sum())),
+                "kinetic_energy_diff_rel": float(abs((v ** 2).sum() - (vel ** 2).sum()) / (vel ** 2).sum())}
+
+    out = {"particles": n, "dt": CROP_STEPS, "oracle_seconds": cpu_s}
+    with S.Sim(params, n_max=n, stream=stream.cuda_stream) as sim, S.Net(16, stream=stream.cuda_stream) as net:
+        sim.upload(part)
+        sim.step(CROP_STEPS)
+        sim.refresh_density()
+        out["plain_fp32"] = errors(sim.download())
+        for name, w in (("learned_bf16", np.load(WEIGHTS).astype(np.float32)),
+                        ("zero_network", np.zeros(int(S.lib.sph_mpnn_num_params()), np.float32))):
+            net.set_params(w)
+            sim.upload(part)
+            sim.learned_step(net, CROP_STEPS // 4, 0)
+            sim.refresh_density()
+            out[name] = errors(sim.download())
+    return out
 
 
 def learned_workload(args, stream, flush) -> dict:
@@ -456,12 +511,12 @@ def learned_workload(args, stream, flush) -> dict:
             learned.step(args.warmup)
             learned.learned_step(net, 2, 0)
             torch.cuda.synchronize()
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
             learned.learned_step(net, 8, 0)
-            b.record(stream)
+            e1.record(stream)
             torch.cuda.synchronize()
-            kernels[name] = {"ms_per_macro_step": a.elapsed_time(b) / 8}
+            kernels[name] = {"ms_per_macro_step": e0.elapsed_time(e1) / 8}
         net.set_precision(1)
         # What the network gains: one judged macro-step from the same state (the plain run's
         # end state) with the trained network and with a zero network (v' = v, x' = x + 4 dt v,
@@ -632,8 +687,11 @@ def run_ours(args) -> None:
         return
     extra = extra_workloads(args, stream) if args.extra_steps > 0 else {}
     learned = learned_workload(args, stream, flush) if args.learned else {"skipped": "--no-learned"}
-    if args.study:
-        learned["slosh_16m_study"] = slosh_study(args, stream)
+    if args.learned:
+        # config 5: the full study (2,000 dt) with --study, else a short leg of 200 dt
+        learned["slosh_16m_study"] = slosh_study(args, stream, 2000, 200) if args.study else \
+            slosh_study(args, stream, 200, 100)
+        learned["slosh_16m_study"]["crop_1m_vs_fp64_oracle"] = slosh_crop_fp64(stream)
     peaks, src = measured_peaks()
     hbm = float(peaks["hbm_gbs"])
     value = world * n * args.steps / total_s
@@ -684,7 +742,8 @@ def main() -> None:
     ap.add_argument("--no-learned", dest="learned", action="store_false",
                     help="skip the learned macro-step measurement")
     ap.add_argument("--study", action="store_true",
-                    help="also run the 16M-particle slosh study of learned vs plain (2,000 dt-equivalents)")
+                    help="run the 16M-particle slosh study of learned vs plain over 2,000 dt-equivalents "
+                         "(default: 200)")
     ap.add_argument("--extra-steps", type=int, default=100,
                     help="steps of the batched-scenes and 10k reference-scene measurements (0: skip)")
     args = ap.parse_args()

@@ -57,51 +57,63 @@ __device__ __forceinline__ void node_feat(float4 vi, float rho, int cnt, const F
     nf[8] = fc.courant;
 }
 
-// Round 1 edge layer per particle: E (stored), relu masks, X1 = [M1, n].
+// The edge layers run four threads per particle, each owning 16 of the 64 outputs (kGrp
+// groups): 16 accumulators per thread, four times the threads of a thread per particle. Each
+// output is summed over the edges in the same order as with one thread per particle.
+constexpr int kGrp = 4, kGW = W / kGrp;
+
+// Round 1 edge layer: E (stored, by group 0), relu masks (16 bits per group), X1 = [M1, n].
 __global__ void __launch_bounds__(kT) k_edge1_fwd(Frame f, const float* __restrict__ prm, float* __restrict__ E,
                                                  unsigned long long* __restrict__ mask1, float* __restrict__ X1) {
     __shared__ float sW[FE * W], sb[W];
     for (int t = threadIdx.x; t < FE * W; t += kT) sW[t] = prm[kWe1 + t];
     for (int t = threadIdx.x; t < W; t += kT) sb[t] = prm[kBe1 + t];
     __syncthreads();
-    const int i = blockIdx.x * kT + threadIdx.x;
+    const long long gt = (long long)blockIdx.x * kT + threadIdx.x;
+    const int i = (int)(gt / kGrp), g = (int)(gt % kGrp);
     if (i >= f.n) return;
     const float4 pi = f.pos[i], vi = f.vel[i];
     const int cnt = min(max(f.cnt[i], 0), K);
-    float m[W];
+    float m[kGW];
 #pragma unroll
-    for (int o = 0; o < W; ++o) m[o] = 0.0f;
+    for (int o = 0; o < kGW; ++o) m[o] = 0.0f;
+    unsigned short* mk = reinterpret_cast<unsigned short*>(mask1);
     for (int k = 0; k < K; ++k) {
         float e[FE];
-        unsigned long long bits = 0ull;
+        unsigned bits = 0u;
         const int j = k < cnt ? f.nb[i * K + k] : -1;
         if (j >= 0 && j < f.n) {
             edge_feat(pi, vi, f.pos[j], f.vel[j], f.fc, e);
 #pragma unroll
-            for (int o = 0; o < W; ++o) {
+            for (int u = 0; u < kGW; ++u) {
+                const int o = g * kGW + u;
                 float z = sb[o];
 #pragma unroll
                 for (int q = 0; q < FE; ++q) z = fmaf(e[q], sW[q * W + o], z);
-                if (z > 0.0f) { m[o] += z; bits |= 1ull << o; }
+                if (z > 0.0f) { m[u] += z; bits |= 1u << u; }
             }
         } else {
 #pragma unroll
             for (int q = 0; q < FE; ++q) e[q] = 0.0f;
         }
+        if (g == 0) {
 #pragma unroll
-        for (int q = 0; q < FE; ++q) E[((size_t)i * K + k) * FE + q] = e[q];
-        mask1[(size_t)i * K + k] = bits;
+            for (int q = 0; q < FE; ++q) E[((size_t)i * K + k) * FE + q] = e[q];
+        }
+        mk[((size_t)i * K + k) * kGrp + g] = (unsigned short)bits;  // bits 16 g .. 16 g + 15 of the u64
     }
     float* x = X1 + (size_t)i * (W + FN);
 #pragma unroll
-    for (int o = 0; o < W; ++o) x[o] = m[o] * (1.0f / K);
-    float nf[FN];
-    node_feat(vi, f.rhop[i].x, cnt, f.fc, nf);
+    for (int u = 0; u < kGW; ++u) x[g * kGW + u] = m[u] * (1.0f / K);
+    if (g == 0) {
+        float nf[FN];
+        node_feat(vi, f.rhop[i].x, cnt, f.fc, nf);
 #pragma unroll
-    for (int q = 0; q < FN; ++q) x[W + q] = nf[q];
+        for (int q = 0; q < FN; ++q) x[W + q] = nf[q];
+    }
 }
 
-// Round 2 edge layer per particle: relu masks, X2 = [M2, H1].
+// Round 2 edge layer: relu masks, X2 = [M2, H1].
 __global__ void __launch_bounds__(kT) k_edge2_fwd(Frame f, const float* __restrict__ prm, const float* __restrict__ E,
                                                  const float* __restrict__ P, const float* __restrict__ H1,
                                                  unsigned long long* __restrict__ mask2, float* __restrict__ X2) {
@@ -109,34 +121,39 @@ __global__ void __launch_bounds__(kT) k_edge2_fwd(Frame f, const float* __restri
     for (int t = threadIdx.x; t < FE * W; t += kT) sW[t] = prm[kWe2 + t];
     for (int t = threadIdx.x; t < W; t += kT) sb[t] = prm[kBe2 + t];
     __syncthreads();
-    const int i = blockIdx.x * kT + threadIdx.x;
+    const long long gt = (long long)blockIdx.x * kT + threadIdx.x;
+    const int i = (int)(gt / kGrp), g = (int)(gt % kGrp);
     if (i >= f.n) return;
     const int cnt = min(max(f.cnt[i], 0), K);
-    float m[W];
+    float m[kGW];
 #pragma unroll
-    for (int o = 0; o < W; ++o) m[o] = 0.0f;
+    for (int o = 0; o < kGW; ++o) m[o] = 0.0f;
+    unsigned short* mk = reinterpret_cast<unsigned short*>(mask2);
     for (int k = 0; k < K; ++k) {
-        unsigned long long bits = 0ull;
+        unsigned bits = 0u;
         const int j = k < cnt ? f.nb[i * K + k] : -1;
         if (j >= 0 && j < f.n) {
             float e[FE];
 #pragma unroll
             for (int q = 0; q < FE; ++q) e[q] = E[((size_t)i * K + k) * FE + q];
-            const float* pj = P + (size_t)j * W;
+            const float* pj = P + (size_t)j * W + g * kGW;
 #pragma unroll
-            for (int o = 0; o < W; ++o) {
-                float z = sb[o] + pj[o];
+            for (int u = 0; u < kGW; ++u) {
+                const int o = g * kGW + u;
+                float z = sb[o] + pj[u];
 #pragma unroll
                 for (int q = 0; q < FE; ++q) z = fmaf(e[q], sW[q * W + o], z);
-                if (z > 0.0f) { m[o] += z; bits |= 1ull << o; }
+                if (z > 0.0f) { m[u] += z; bits |= 1u << u; }
             }
         }
-        mask2[(size_t)i * K + k] = bits;
+        mk[((size_t)i * K + k) * kGrp + g] = (unsigned short)bits;
     }
     float* x = X2 + (size_t)i * 2 * W;
 #pragma unroll
-    for (int o = 0; o < W; ++o) x[o] = m[o] * (1.0f / K);
-    for (int o = 0; o < W; ++o) x[W + o] = H1[(size_t)i * W + o];
+    for (int u = 0; u < kGW; ++u) {
+        x[g * kGW + u] = m[u] * (1.0f / K);
+        x[W + g * kGW + u] = H1[(size_t)i * W + g * kGW + u];
+    }
 }
 
 // Y[i, o] = act(sum_k X[i, k] W[k, o] + b[o]); one thread per (i, o).
@@ -322,6 +339,24 @@ __global__ void __launch_bounds__(kT) k_rev_gather(const int* __restrict__ off, 
     dP[t] = s;
 }
 
+// dP[j, o] = sum over the edges (i -> j), in ascending edge order, of dZ2[edge, o] formed on the
+// fly: dX2[i, o] / K where relu bit o of the edge is set (the terms of k_rev_gather, without
+// the materialised dZ2).
+__global__ void __launch_bounds__(kT) k_rev_gather_masked(const int* __restrict__ off, const int* __restrict__ edges,
+                                                         const float* __restrict__ dX2,
+                                                         const unsigned long long* __restrict__ mask2, int n,
+                                                         float* __restrict__ dP) {
+    const long long t = (long long)blockIdx.x * kT + threadIdx.x;
+    if (t >= (long long)n * W) return;
+    const int j = (int)(t / W), o = (int)(t % W);
+    float s = 0.0f;
+    for (int q = off[j]; q < off[j + 1]; ++q) {
+        const int e = edges[q];
+        if ((mask2[e] >> o) & 1ull) s += dX2[(size_t)(e / K) * 2 * W + o] * (1.0f / K);
+    }
+    dP[t] = s;
+}
+
 __global__ void __launch_bounds__(kT) k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
                                             float* __restrict__ v, int np, float lr, float b1, float b2, float eps,
                                             float c1, float c2) {
@@ -362,6 +397,59 @@ __global__ void __launch_bounds__(256) k_pack_bf16(const float* __restrict__ src
         const int c = c0 + r, i = i0 + tx;
         if (c < ldd && i < kpad) dstT[(size_t)c * ldt + i] = __float2bfloat16_rn(tile[tx][r]);
     }
+}
+
+// Edge operands of the edge-layer weight gradients, transposed (K = edges, padded to rpad):
+//   ET  [16][rpad]: rows 0..13 the edge features E, row 14 = 1 on real edges (the bias), 15 = 0;
+//   dZT [64][rpad]: dZ[r][o] = dM[i][o] / K where relu bit o of edge r is set, 0 elsewhere
+//                   (dM = columns 0..63 of dX, row stride ld).
+// One thread per edge r, looping over the rows: the 32 lanes of a warp are the 32 edges of one
+// particle, so each transposed write is 32 consecutive bf16 and the reads of dX broadcast.
+__global__ void __launch_bounds__(kT) k_pack_et(const float* __restrict__ E, const int* __restrict__ cnt, int n, int rpad,
+                                               __nv_bfloat16* __restrict__ ET) {
+    const long long r = (long long)blockIdx.x * kT + threadIdx.x;
+    if (r >= rpad) return;
+    float v[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) v[k] = 0.0f;
+    if (r < (long long)n * K) {
+        const int i = (int)(r / K), e = (int)(r % K);
+#pragma unroll
+        for (int k = 0; k < FE; ++k) v[k] = E[r * FE + k];
+        v[FE] = e < cnt[i] ? 1.0f : 0.0f;
+    }
+#pragma unroll
+    for (int k = 0; k < 16; ++k) ET[(size_t)k * rpad + r] = __float2bfloat16_rn(v[k]);
+}
+
+__global__ void __launch_bounds__(kT) k_pack_dzt(const float* __restrict__ dX, int ld,
+                                                const unsigned long long* __restrict__ mask, const int* __restrict__ cnt,
+                                                int n, int rpad, __nv_bfloat16* __restrict__ dZT) {
+    const long long r = (long long)blockIdx.x * kT + threadIdx.x;
+    if (r >= rpad) return;
+    unsigned long long bits = 0ull;
+    int i = 0;
+    if (r < (long long)n * K) {
+        i = (int)(r / K);
+        if ((int)(r % K) < cnt[i]) bits = mask[r];
+    }
+    const float* dm = dX + (size_t)i * ld;
+#pragma unroll 8
+    for (int o = 0; o < W; ++o)
+        dZT[(size_t)o * rpad + r] = __float2bfloat16_rn(((bits >> o) & 1ull) ? dm[o] * (1.0f / K) : 0.0f);
+}
+
+// Edge-layer weight gradient from the split-K partials part[split][64 (o)][16 (k)] of
+// dZ^T E: rows k < FE of the gradient to gw[k][o], row FE (the bias) to gb[o].
+__global__ void __launch_bounds__(kT) k_tc_reduce_edge(const float* __restrict__ part, int splits, float* __restrict__ gw,
+                                                      float* __restrict__ gb) {
+    const int t = blockIdx.x * kT + threadIdx.x;
+    if (t >= (FE + 1) * W) return;
+    const int k = t / W, o = t % W;
+    float s = 0.0f;
+    for (int q = 0; q < splits; ++q) s += part[((size_t)q * W + o) * 16 + k];
+    if (k < FE) gw[k * W + o] = s;
+    else gb[o] = s;
 }
 
 // Packed BF16 weights of the node layers, rebuilt whenever the parameters change:
@@ -441,6 +529,11 @@ struct Trainer {
     float* tpart = nullptr;
     uint32_t* tc_err = nullptr;
     static constexpr int kTcSplits = 64;
+    // edge-layer weight gradients on the tensor cores: transposed edge operands, K = edges
+    long long rpad_max = 0;
+    __nv_bfloat16 *ET = nullptr, *dZT = nullptr;
+    float* epart = nullptr;
+    static constexpr int kEdgeSplits = 512;
 
     template <class T>
     static cudaError_t al(T** p, size_t n) { return cudaMalloc((void**)p, (n ? n : 1) * sizeof(T)); }
@@ -475,6 +568,9 @@ struct Trainer {
             A(al(&X1bT, kTcK1 * kp)); A(al(&H1bT, W * kp)); A(al(&X2bT, kTcK2 * kp)); A(al(&H2bT, kTcKo * kp));
             A(al(&dOT, kTcNo * kp)); A(al(&dY2T, W * kp)); A(al(&dPT, W * kp)); A(al(&dY1T, W * kp));
             A(al(&tpart, (size_t)kTcSplits * kTcK2 * W));
+            rpad_max = ((long long)nmax * K + 63) / 64 * 64;
+            A(al(&ET, (size_t)16 * rpad_max)); A(al(&dZT, (size_t)W * rpad_max));
+            A(al(&epart, (size_t)kEdgeSplits * W * 16));
         }
         return r;
     }
@@ -483,7 +579,7 @@ struct Trainer {
         void* ptrs[] = {prm, grad, adam_m, adam_v, E, X1, H1, P, X2, H2, O, dO, dY2, dX2, dZ2, dP, dY1, dX1,
                         part, loss_part, mask1, mask2, rev_cnt, rev_off, rev_edges,
                         X1b, H1b, X2b, H2b, dOb, dY2b, dPb, dY1b, X1bT, H1bT, X2bT, H2bT, dOT, dY2T, dPT, dY1T,
-                        Wf, Wb, tpart, tc_err};
+                        Wf, Wb, tpart, tc_err, ET, dZT, epart};
         for (void* q : ptrs)
             if (q) cudaFree(q);
     }
@@ -557,15 +653,39 @@ struct Trainer {
                                                                 boff >= 0 ? grad + boff : nullptr);
     }
 
+    // Edge-layer weight gradient on the tensor cores: D^T = dZ^T E over the edges (M = 64
+    // outputs, N = 16 features incl. the bias row, K = edges), split over K, reduced in order.
+    // dX / ld: the data gradient whose first 64 columns are dM of this round; mask: its relu bits.
+    void tc_edge_wgrad(const Frame& f, const float* dX, int ld, const unsigned long long* mask, int woff, int boff,
+                       cudaStream_t st) {
+        const long long r = (long long)f.n * K;
+        const long long rpad = (r + 63) / 64 * 64;
+        k_pack_dzt<<<(unsigned)((rpad + kT - 1) / kT), kT, 0, st>>>(dX, ld, mask, f.cnt, f.n, (int)rpad, dZT);
+        long long kps = (rpad + kEdgeSplits - 1) / kEdgeSplits;
+        kps = (kps + 63) / 64 * 64;
+        const int sp = (int)((rpad + kps - 1) / kps);
+        tc::Epilogue e;
+        e.out = epart;
+        e.ld_out = 16;
+        e.ncols = 16;
+        e.split_stride = (long long)W * 16;
+        tc::gemm_bf16(dZT, (int)rpad, ET, (int)rpad, W, 16, (int)rpad, e, sp, (int)kps, tc_err, st);
+        k_tc_reduce_edge<<<nblk((FE + 1) * W), kT, 0, st>>>(epart, sp, grad + woff, grad + boff);
+    }
+
     void forward_tc(const Frame& f, bool train, cudaStream_t st) {
         const int n = f.n;
         k_pack_weights<<<nblk(kWfTotal), kT, 0, st>>>(prm, Wf, Wb);
-        k_edge1_fwd<<<nblk(n), kT, 0, st>>>(f, prm, E, mask1, X1);
+        k_edge1_fwd<<<nblk((long long)n * kGrp), kT, 0, st>>>(f, prm, E, mask1, X1);
+        if (train) {
+            const long long rpad = ((long long)n * K + 63) / 64 * 64;
+            k_pack_et<<<(unsigned)((rpad + kT - 1) / kT), kT, 0, st>>>(E, f.cnt, n, (int)rpad, ET);
+        }
         pack(X1, W + FN, W + FN, n, W + FN, X1b, kTcK1, train ? X1bT : nullptr, st);
         tc_gemm(X1b, kTcK1, Wf + kWfN1, kTcK1, n, W, kTcK1, epi(H1, W, W, 1), st);
         pack(H1, W, W, n, -1, H1b, W, train ? H1bT : nullptr, st);
         tc_gemm(H1b, W, Wf + kWfP, W, n, W, W, epi(P, W, W), st);
-        k_edge2_fwd<<<nblk(n), kT, 0, st>>>(f, prm, E, P, H1, mask2, X2);
+        k_edge2_fwd<<<nblk((long long)n * kGrp), kT, 0, st>>>(f, prm, E, P, H1, mask2, X2);
         pack(X2, 2 * W, 2 * W, n, 2 * W, X2b, kTcK2, train ? X2bT : nullptr, st);
         tc_gemm(X2b, kTcK2, Wf + kWfN2, kTcK2, n, W, kTcK2, epi(H2, W, W, 1), st);
         pack(H2, W, W, n, W, H2b, kTcKo, train ? H2bT : nullptr, st);
@@ -586,9 +706,8 @@ struct Trainer {
         pack(dY2, W, W, n, -1, dY2b, W, dY2T, st);
         tc_wgrad(X2bT, kTcK2, dY2T, W, n, 2 * W, W, kWn2, kBn2, st);
         tc_gemm(dY2b, W, Wb + kWbN2, W, n, 2 * W, W, epi(dX2, 2 * W, 2 * W), st);  // dX2 = dY2 Wn2^T
-        k_edge2_bwd<<<nblk((long long)n * K * W), kT, 0, st>>>(dX2, mask2, f.cnt, n, dZ2);
-        edge_wgrad(dZ2, nullptr, 0, nullptr, f.cnt, n, kWe2, kBe2, st);
-        reverse_gather(f, st);
+        tc_edge_wgrad(f, dX2, 2 * W, mask2, kWe2, kBe2, st);
+        reverse_gather(f, st, true);
         pack(dP, W, W, n, -1, dPb, W, dPT, st);
         tc_wgrad(H1bT, W, dPT, W, n, W, W, kWp, -1, st);
         {  // dY1 = (dX2[:, W:] + dP Wp^T) * (H1 > 0)
@@ -602,10 +721,11 @@ struct Trainer {
         pack(dY1, W, W, n, -1, dY1b, W, dY1T, st);
         tc_wgrad(X1bT, kTcK1, dY1T, W, n, W + FN, W, kWn1, kBn1, st);
         tc_gemm(dY1b, W, Wb + kWbN1, W, n, kTcK1, W, epi(dX1, W + FN, W + FN), st);  // dX1 = dY1 Wn1^T
-        edge_wgrad(nullptr, dX1, W + FN, mask1, f.cnt, n, kWe1, kBe1, st);
+        tc_edge_wgrad(f, dX1, W + FN, mask1, kWe1, kBe1, st);
     }
 
-    void reverse_gather(const Frame& f, cudaStream_t st) {
+    // dP from the reverse edges: from the materialised dZ2, or (masked) from dX2 and the relu bits.
+    void reverse_gather(const Frame& f, cudaStream_t st, bool masked = false) {
         const int n = f.n;
         cudaMemsetAsync(rev_cnt, 0, sizeof(int) * n, st);
         k_rev_count<<<nblk((long long)n * K), kT, 0, st>>>(f.nb, f.cnt, n, rev_cnt);
@@ -613,7 +733,10 @@ struct Trainer {
         cudaMemsetAsync(rev_cnt, 0, sizeof(int) * n, st);
         k_rev_fill<<<nblk((long long)n * K), kT, 0, st>>>(f.nb, f.cnt, n, rev_off, rev_cnt, rev_edges);
         k_rev_sort<<<nblk(n), kT, 0, st>>>(rev_off, n, rev_edges);
-        k_rev_gather<<<nblk((long long)n * W), kT, 0, st>>>(rev_off, rev_edges, dZ2, n, dP);
+        if (masked)
+            k_rev_gather_masked<<<nblk((long long)n * W), kT, 0, st>>>(rev_off, rev_edges, dX2, mask2, n, dP);
+        else
+            k_rev_gather<<<nblk((long long)n * W), kT, 0, st>>>(rev_off, rev_edges, dZ2, n, dP);
     }
 
     // Forward: O (n x kOS) from the frame.
@@ -623,10 +746,10 @@ struct Trainer {
             return;
         }
         const int n = f.n;
-        k_edge1_fwd<<<nblk(n), kT, 0, st>>>(f, prm, E, mask1, X1);
+        k_edge1_fwd<<<nblk((long long)n * kGrp), kT, 0, st>>>(f, prm, E, mask1, X1);
         dense(X1, W + FN, W + FN, kWn1, kBn1, W, H1, W, n, 1, st);
         dense(H1, W, W, kWp, -1, W, P, W, n, 0, st);
-        k_edge2_fwd<<<nblk(n), kT, 0, st>>>(f, prm, E, P, H1, mask2, X2);
+        k_edge2_fwd<<<nblk((long long)n * kGrp), kT, 0, st>>>(f, prm, E, P, H1, mask2, X2);
         dense(X2, 2 * W, 2 * W, kWn2, kBn2, W, H2, W, n, 1, st);
         dense(H2, W, W, kWo, kBo, FO, O, kOS, n, 0, st);
     }

@@ -15,6 +15,12 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 WEIGHTS = Path(__file__).resolve().parents[1] / "npr-sph_gb300" / "weights" / "mpnn_w64.npy"
+# Bounds on the crop after 20 dt against the FP64 oracle. Plain FP32: 1e-3 (measured ~1e-6).
+# Learned BF16 (5 unjudged macro-steps): mean per-particle density error 10% (measured 6.5%;
+# the network misses the 1% of a judged interval here, which is why the judge exists), and the
+# trained network must beat the macro-step without it on every measure.
+PLAIN_TOL = 1e-3
+LEARNED_DENSITY_TOL = 0.10
 
 
 def crop(sph):
@@ -74,8 +80,9 @@ def test_crop_fp32_and_learned_against_fp64(sph, orc, gpu):
     if os.environ.get("SPH_STUDY_OUT"):
         Path(os.environ["SPH_STUDY_OUT"]).write_text(json.dumps(out, indent=1))
     print(json.dumps(out))
-    assert out["plain_fp32"]["density_err_mean"] < 1e-3
-    assert out["plain_fp32"]["momentum_diff_rel"] < 1e-3
+    assert out["plain_fp32"]["density_err_mean"] < PLAIN_TOL
+    assert out["plain_fp32"]["momentum_diff_rel"] < PLAIN_TOL
     if "learned_bf16" in out:  # the trained network beats the macro-step without it (v' = v, x' = x + 4 dt v)
+        assert out["learned_bf16"]["density_err_mean"] < LEARNED_DENSITY_TOL
         for k in ("density_err_mean", "momentum_diff_rel", "kinetic_energy_diff_rel"):
             assert out["learned_bf16"][k] < out["zero_network"][k], k
