@@ -13,7 +13,9 @@ and viscosity mu and the drop geometry are drawn from the seed:
 Every `gap` steps each run contributes a frame: its state, the <= 32 nearest neighbours and
 density of every particle, and as targets the mean accelerations of the next 4 plain steps
 (the velocity head O_v and the position head O_x, in units of k/h) from the forces. The network is then trained by Adam on the GPU (the library's own forward and
-backward kernels), one frame per step, with a cosine-decayed learning rate.
+backward kernels), one frame per step, with a cosine-decayed learning rate. By default the
+node layers and all weight gradients run as BF16 GEMMs on the tensor cores (FP32 accumulation,
+FP32 master weights); --precision 0 runs every layer in FP32.
 """
 from __future__ import annotations
 
@@ -73,6 +75,8 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=30000, help="Adam steps")
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--seed", type=int, default=4)
+    ap.add_argument("--precision", type=int, default=1, choices=[0, 1],
+                    help="1: node layers and weight gradients as BF16 tensor-core (tcgen05) GEMMs; 0: FP32")
     ap.add_argument("--out", type=Path, default=DEFAULT_OUT)
     args = ap.parse_args()
 
@@ -80,6 +84,7 @@ def main() -> None:
     plist, counts, parts = training_scenes(args.scenes, args.particles, args.seed)
     net = S.Net(args.particles)
     net.set_params(init_params(args.seed))
+    net.set_train_precision(args.precision)
     with S.Sim(plist, counts=counts) as sim:
         sim.upload(parts)
         for f in range(args.frames):
@@ -105,6 +110,7 @@ def main() -> None:
     loss = np.concatenate(losses)
     meta = {"scenes": args.scenes, "particles": args.particles, "frames_per_run": args.frames, "gap": args.gap,
             "frames": int(total), "adam_steps": args.steps, "lr": args.lr, "seed": args.seed,
+            "train_precision": "bf16 tcgen05 GEMMs" if args.precision == 1 else "fp32",
             "loss_first_500": float(loss[:500].mean()), "loss_last_500": float(loss[-500:].mean()),
             "record_s": t_rec, "train_s": t_train}
     args.out.with_suffix(".json").write_text(json.dumps(meta, indent=1))

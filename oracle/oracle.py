@@ -19,6 +19,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "liboracle.so"
 REF_LIB = HERE / "_ref" / "libref_shader.so"
+REF_TOON_LIB = HERE / "_ref" / "libref_toon.so"
 # The reference tree (its NPR-SPH/ folder with the .glsl shaders), named by the environment;
 # without it the reference shaders are not built.
 REF_ENV = "NPRSPH_REF_DIR"
@@ -79,12 +80,65 @@ def lib() -> C.CDLL:
         L.oracle_max_threads.restype = C.c_int
         L.oracle_render.restype = C.c_int
         L.oracle_render.argtypes = [_P, _P, _I64, _P]
+        L.oracle_toon_cel.restype = C.c_int
+        L.oracle_toon_cel.argtypes = [_P, _P, _P, C.c_float, C.c_float, C.c_float, _P]
+        L.oracle_toon_outline.restype = C.c_int
+        L.oracle_toon_outline.argtypes = [_P]
         _lib = L
     return _lib
 
 
 def ref_available() -> bool:
     return REF_LIB.exists()
+
+
+_toon = None
+
+
+def ref_toon_available() -> bool:
+    return REF_TOON_LIB.exists()
+
+
+def ref_toon() -> C.CDLL:
+    """The reference's toon_fs.glsl compiled as C++ (oracle/_ref/libref_toon.so)."""
+    global _toon
+    if _toon is None:
+        T = C.CDLL(str(REF_TOON_LIB))
+        T.ref_toon_cel.restype = C.c_int
+        T.ref_toon_cel.argtypes = [_P, _P, _P, _P, C.c_float]
+        T.ref_toon_outline.restype = C.c_int
+        T.ref_toon_outline.argtypes = [_P, C.c_int, C.c_int]
+        _toon = T
+    return _toon
+
+
+def _f32p(a) -> int:
+    return np.ascontiguousarray(a, dtype=np.float32).ctypes.data
+
+
+def toon_cel(pw, eye, light, px: float, py: float, thr: float) -> tuple[int, float]:
+    """The render restatement's cel-shading choice of one fragment (-1 discard, 0 dark,
+    1 midtone, 2 highlight) and its r.v."""
+    a, b, c = (np.ascontiguousarray(x, dtype=np.float32) for x in (pw, eye, light))
+    rv = C.c_float()
+    k = lib().oracle_toon_cel(a.ctypes.data, b.ctypes.data, c.ctypes.data, px, py, thr, C.byref(rv))
+    return int(k), float(rv.value)
+
+
+def toon_outline(cov) -> int:
+    c = np.ascontiguousarray(cov, dtype=np.int32).reshape(9)
+    return int(lib().oracle_toon_outline(c.ctypes.data))
+
+
+def ref_toon_cel(pw, eye, light, pc, shininess: float) -> int:
+    """celshading() of the reference shader for one fragment (gl_PointCoord pc)."""
+    a, b, c, d = (np.ascontiguousarray(x, dtype=np.float32) for x in (pw, eye, light, pc))
+    return int(ref_toon().ref_toon_cel(a.ctypes.data, b.ctypes.data, c.ctypes.data, d.ctypes.data, shininess))
+
+
+def ref_toon_outline(green, x: int = 5, y: int = 7) -> int:
+    g = np.ascontiguousarray(green, dtype=np.float32).reshape(9)
+    return int(ref_toon().ref_toon_outline(g.ctypes.data, x, y))
 
 
 def ref() -> C.CDLL:

@@ -97,7 +97,50 @@ float sprite(const View& V, int x, float xw, int y, float yw, float& px, float& 
     return px * px + py * py;
 }
 
+// Cel shading of one fragment of particle-space position pw (toon_fs.glsl:90-124, SPH mode):
+// (px, py) = 2 gl_PointCoord - 1, the sphere impostor's normal (px, py, sqrt(1 - |p|^2)),
+// light and view vectors from pw, the reflection of -l about n. Returns -1 (discard: |p|^2 > 1),
+// 0 dark (n.l < 0), 1 midtone, 2 highlight (r.v > 0 and r.v > thr, thr = 0.95^(1/shininess):
+// the shader's pow(r.v, shininess) > 0.95); *rv_out gets r.v.
+int cel_choice(const float* pw, const float* eye, const float* light, float px, float py, float thr, float* rv_out) {
+    const float mag = px * px + py * py;
+    if (mag > 1.0f) return -1;
+    float n3[3] = {px, py, std::sqrt(1.0f - mag)};
+    normalize3(n3);
+    float l[3] = {light[0] - pw[0], light[1] - pw[1], light[2] - pw[2]};
+    normalize3(l);
+    float vv[3] = {eye[0] - pw[0], eye[1] - pw[1], eye[2] - pw[2]};
+    normalize3(vv);
+    const float ml[3] = {-l[0], -l[1], -l[2]};
+    const float d2 = 2.0f * dot3(n3, ml);
+    float r[3] = {ml[0] - d2 * n3[0], ml[1] - d2 * n3[1], ml[2] - d2 * n3[2]};
+    normalize3(r);
+    const float nl = dot3(n3, l), rv = dot3(r, vv);
+    if (rv_out) *rv_out = rv;
+    int c = nl < 0.0f ? 0 : 1;
+    if (rv > 0.0f && rv > thr) c = 2;
+    return c;
+}
+
+// Sobel outline of the pass-0 coverage around a fragment (toon_fs.glsl:126-153): cov[3 i + j]
+// is 1 where pixel (x + i - 1, y + j - 1) is covered. gx = column x-1 minus column x+1, gy =
+// row y-1 minus row y+1 (weights 1, 2, 1); an outline where sqrt(gx^2 + gy^2) > 0.1.
+int outline_choice(const int* cov) {
+    auto c = [&](int i, int j) { return cov[3 * i + j]; };
+    const int gx = (c(0, 0) + 2 * c(0, 1) + c(0, 2)) - (c(2, 0) + 2 * c(2, 1) + c(2, 2));
+    const int gy = (c(0, 0) + 2 * c(1, 0) + c(2, 0)) - (c(0, 2) + 2 * c(1, 2) + c(2, 2));
+    const double g = std::sqrt((double)gx * gx + (double)gy * gy);
+    return g > 0.1 ? 1 : 0;
+}
+
 }  // namespace
+
+extern "C" int oracle_toon_cel(const float pw[3], const float eye[3], const float light[3], float px, float py,
+                               float thr, float* rv) {
+    return cel_choice(pw, eye, light, px, py, thr, rv);
+}
+
+extern "C" int oracle_toon_outline(const int cov[9]) { return outline_choice(cov); }
 
 extern "C" int oracle_render(const sph_view* v, const float* pos4, int64_t n, uint8_t* rgba) {
     if (!v || !rgba || v->width <= 0 || v->height <= 0 || (n > 0 && !pos4)) return -1;
@@ -137,36 +180,22 @@ extern "C" int oracle_render(const sph_view* v, const float* pos4, int64_t n, ui
             const size_t k = (size_t)y * W + x;
             uint32_t c = c_clear;
             if (owner[k] >= 0) {
-                // Sobel of the coverage (toon_fs.glsl:126-153): columns x-1 minus x+1, rows y-1 minus y+1
-                const int gx = (cov(x - 1, y - 1) + 2 * cov(x - 1, y) + cov(x - 1, y + 1)) -
-                               (cov(x + 1, y - 1) + 2 * cov(x + 1, y) + cov(x + 1, y + 1));
-                const int gy = (cov(x - 1, y - 1) + 2 * cov(x, y - 1) + cov(x + 1, y - 1)) -
-                               (cov(x - 1, y + 1) + 2 * cov(x, y + 1) + cov(x + 1, y + 1));
-                const double g = std::sqrt((double)gx * gx + (double)gy * gy);
-                if (g > 0.1) {
+                int nb[9];
+                for (int i = 0; i < 3; ++i)
+                    for (int j = 0; j < 3; ++j) nb[3 * i + j] = cov(x + i - 1, y + j - 1);
+                if (outline_choice(nb)) {
                     c = c_out;
                 } else {
                     const float* p = pos4 + 4 * owner[k];
                     float xw, yw;
                     uint32_t d24;
                     vertex(V, p, xw, yw, d24);
-                    float n3[3];
-                    const float mag = sprite(V, x, xw, y, yw, n3[0], n3[1]);
-                    n3[2] = std::sqrt(1.0f - mag);
-                    normalize3(n3);
+                    float px, py;
+                    sprite(V, x, xw, y, yw, px, py);
                     const float pw[3] = {row4(V.m, p[0], p[1], p[2]), row4(V.m + 4, p[0], p[1], p[2]),
                                          row4(V.m + 8, p[0], p[1], p[2])};
-                    float l[3] = {V.light[0] - pw[0], V.light[1] - pw[1], V.light[2] - pw[2]};
-                    normalize3(l);
-                    float vv[3] = {V.eye[0] - pw[0], V.eye[1] - pw[1], V.eye[2] - pw[2]};
-                    normalize3(vv);
-                    const float ml[3] = {-l[0], -l[1], -l[2]};
-                    const float d2 = 2.0f * dot3(n3, ml);
-                    float r[3] = {ml[0] - d2 * n3[0], ml[1] - d2 * n3[1], ml[2] - d2 * n3[2]};
-                    normalize3(r);
-                    const float nl = dot3(n3, l), rv = dot3(r, vv);
-                    c = nl < 0.0f ? c_dark : c_mid;
-                    if (rv > 0.0f && rv > V.thr) c = c_hi;
+                    const int choice = cel_choice(pw, V.eye, V.light, px, py, V.thr, nullptr);
+                    c = choice == 2 ? c_hi : (choice == 0 ? c_dark : c_mid);
                 }
             }
             std::memcpy(rgba + 4 * k, &c, 4);

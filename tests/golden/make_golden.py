@@ -12,6 +12,9 @@ The fixture holds, per case and step count:
   - sha256 of the full 10,000-record output (bit-exact pin of the FP32 mirror),
   - every 20th record of the output (float32, for readable diffs),
   - sha256 of the input scene (pins the scene generator).
+It also writes tests/golden/reference_toon.npz: the reference's particle fragment shader
+(toon_fs.glsl, celshading() and outline()) on the seeded cases of toon_cases.py.
+
 Cases (the shaders hard-code NUM_PARTICLES = 10000, G = -9806.65, k = 2000, dt = 1e-4):
   literal   make_grid() of Main.cpp:488-505 (10x100x10 at 0.005), the reference's own start
   lattice   10,000 points at 0.5h, jitter +-0.01h, seed 1, in the lower-corner quarter of the box
@@ -31,6 +34,7 @@ import nprsph as S  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 
 OUT = Path(__file__).resolve().parent / "reference_shader.npz"
+OUT_TOON = Path(__file__).resolve().parent / "reference_toon.npz"
 STEPS = {"literal": (1, 3, 20), "lattice": (1, 3, 20)}
 SUB = slice(0, None, 20)
 
@@ -57,6 +61,25 @@ def main() -> None:
             data[f"{name}_s{n}_sub"] = np.ascontiguousarray(out[SUB]).view(np.float32).reshape(-1, 16).copy()
     np.savez_compressed(OUT, **data)
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes)")
+    toon()
+
+
+def toon() -> None:
+    """The reference's toon_fs.glsl (compiled as C++, oracle/_ref/libref_toon.so) on the seeded
+    cases of toon_cases.py: celshading()'s choice per fragment (-1 discard, 0 dark, 1 midtone,
+    2 highlight) and outline()'s decision per 3 x 3 coverage pattern."""
+    sys.path.insert(0, str(Path(__file__).resolve().parent))
+    import toon_cases as TC
+
+    assert O.ref_toon_available(), "oracle/_ref/libref_toon.so was not built (set NPRSPH_REF_DIR)"
+    pw, eye, light, pc, shin = TC.cel_cases()
+    cel = np.array([O.ref_toon_cel(pw[i], eye[i], light[i], pc[i], float(shin[i])) for i in range(len(pw))],
+                   dtype=np.int8)
+    cov = TC.outline_cases()
+    outl = np.array([O.ref_toon_outline(c.astype(np.float32)) for c in cov], dtype=np.int8)
+    inputs = hashlib.sha256(b"".join(np.ascontiguousarray(a).tobytes() for a in (pw, eye, light, pc, shin))).hexdigest()
+    np.savez_compressed(OUT_TOON, cel=cel, outline=outl, inputs_sha=np.array(inputs))
+    print(f"wrote {OUT_TOON} ({OUT_TOON.stat().st_size} bytes)")
 
 
 if __name__ == "__main__":
