@@ -528,7 +528,7 @@ struct Trainer {
     __nv_bfloat16 *Wf = nullptr, *Wb = nullptr;
     float* tpart = nullptr;
     uint32_t* tc_err = nullptr;
-    static constexpr int kTcSplits = 64;
+    static constexpr int kTcSplits = 128;
     // edge-layer weight gradients on the tensor cores: transposed edge operands, K = edges
     long long rpad_max = 0;
     __nv_bfloat16 *ET = nullptr, *dZT = nullptr;

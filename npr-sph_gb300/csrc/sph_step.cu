@@ -293,16 +293,17 @@ __global__ void __launch_bounds__(BLOCK) k_density(const float4* __restrict__ po
             if (!tiled) p = pos_s[t];
             if constexpr (BATCHED) sc = min(max(scene_of(p), 0), nscene - 1);
             const SceneDev& S = scene_params<BATCHED>(s0, scenes, sc);
-            const float cut = S.cut_d2, h2 = S.h2;
+            const float cut = S.cut_d2;
             float sum = 0.0f, comp = 0.0f;
             if (tiled) {
-                // Branch-free: every candidate adds max(h^2 - d2, 0)^3, two per step in
-                // packed lanes, each lane its own blocked compensated sum. The weight differs from the
-                // strict-predicate one (d2 < cut) only for d2 within an ulp of h^2, where it
-                // is below 1e-30 * h^6: invisible in an FP32 sum of terms of order h^6.
+                // Branch-free: every candidate adds max(cut - d2, 0)^3, two per step in packed
+                // lanes, each lane its own blocked compensated sum. cut - d2 is the negated
+                // difference the neighbour masks take their sign from, so the weight is zero
+                // exactly where the predicate d2 < cut fails; it differs from h^2 - d2 by at most
+                // the ulp between cut and h^2 (a relative density change below 1e-7).
                 const float2 npx = make_float2(-p.x, -p.x), npy = make_float2(-p.y, -p.y);
                 const float2 npz = make_float2(-p.z, -p.z);
-                const float2 h2v = make_float2(h2, h2), ncut = make_float2(-cut, -cut);
+                const float2 ncut = make_float2(-cut, -cut);
                 float2 s2 = make_float2(0.f, 0.f), c2 = make_float2(0.f, 0.f);
 #pragma unroll
                 for (int r = 0; r < G::kSegPerRow; ++r) {
@@ -313,16 +314,13 @@ __global__ void __launch_bounds__(BLOCK) k_density(const float4* __restrict__ po
 #pragma unroll 2
                     for (int j = a; j < b; j += 2) {
                         const float2 d2 = pair_d2(st, j, npx, npy, npz);
-                        float2 w = __fadd2_rn(h2v, make_float2(-d2.x, -d2.y));
-                        w.x = fmaxf(w.x, 0.0f);
-                        w.y = fmaxf(w.y, 0.0f);
-                        const float2 term = __fmul2_rn(__fmul2_rn(w, w), w);
-                        seg = __fadd2_rn(seg, term);
+                        // d2 - cut is negative exactly when d2 < cut (a difference of two distinct
+                        // floats is never zero; +inf and NaN are positive): its sign bit is the
+                        // force pass's predicate, shifted in as the masks' new lowest bit
+                        const float2 e = __fadd2_rn(d2, ncut);
+                        const float2 w = make_float2(fmaxf(-e.x, 0.0f), fmaxf(-e.y, 0.0f));
+                        seg = __ffma2_rn(__fmul2_rn(w, w), w, seg);
                         if constexpr (kMask) {
-                            // d2 - cut is negative exactly when d2 < cut (a difference of two distinct
-                            // floats is never zero; +inf and NaN are positive): its sign bit is the
-                            // force pass's predicate, shifted in as the masks' new lowest bit
-                            const float2 e = __fadd2_rn(d2, ncut);
                             mx = __funnelshift_l(__float_as_uint(e.x), mx, 1);
                             my = __funnelshift_l(__float_as_uint(e.y), my, 1);
                         }
@@ -354,7 +352,7 @@ __global__ void __launch_bounds__(BLOCK) k_density(const float4* __restrict__ po
                         float dx, dy, dz;
                         const float d2 = canon_d2(p.x, p.y, p.z, o.x, o.y, o.z, dx, dy, dz);
                         if (d2 < cut) {
-                            const float w = h2 - d2;
+                            const float w = cut - d2;
                             kahan_add(sum, comp, w * w * w);
                         }
                     }
@@ -642,7 +640,7 @@ __global__ void __launch_bounds__(BLOCK) k_density_nb(const float4* __restrict__
             if (!tiled) p = pos_s[t];
             if constexpr (BATCHED) sc = min(max(scene_of(p), 0), nscene - 1);
             const SceneDev& S = scene_params<BATCHED>(s0, scenes, sc);
-            const float cut = S.cut_d2, h2 = S.h2;
+            const float cut = S.cut_d2;
             float sum = 0.0f, comp = 0.0f;
             int* out = nb + (size_t)t * kNbList;
             if (tiled) {
@@ -650,7 +648,7 @@ __global__ void __launch_bounds__(BLOCK) k_density_nb(const float4* __restrict__
                 // candidates other than the particle itself, pruned to the nearest kNbList
                 const float2 npx = make_float2(-p.x, -p.x), npy = make_float2(-p.y, -p.y);
                 const float2 npz = make_float2(-p.z, -p.z);
-                const float2 h2v = make_float2(h2, h2);
+                const float2 ncut = make_float2(-cut, -cut);
                 float2 s2 = make_float2(0.f, 0.f), c2 = make_float2(0.f, 0.f);
                 // the particle's own staged index: its row's centre segment (dy = dz = 0) holds it
                 const int cseg = lrow * G::kSegPerRow + R * G::kSide + R;
@@ -663,11 +661,9 @@ __global__ void __launch_bounds__(BLOCK) k_density_nb(const float4* __restrict__
 #pragma unroll 2
                     for (int j = a; j < b; j += 2) {
                         const float2 d2 = pair_d2(st, j, npx, npy, npz);
-                        float2 w = __fadd2_rn(h2v, make_float2(-d2.x, -d2.y));
-                        w.x = fmaxf(w.x, 0.0f);
-                        w.y = fmaxf(w.y, 0.0f);
-                        const float2 term = __fmul2_rn(__fmul2_rn(w, w), w);
-                        seg = __fadd2_rn(seg, term);
+                        const float2 e = __fadd2_rn(d2, ncut);
+                        const float2 w = make_float2(fmaxf(-e.x, 0.0f), fmaxf(-e.y, 0.0f));
+                        seg = __ffma2_rn(__fmul2_rn(w, w), w, seg);
                         if (d2.x < cut && j != self_j) lst[BLOCK * c++] = (unsigned short)j;
                         if (d2.y < cut && j + 1 != self_j) lst[BLOCK * c++] = (unsigned short)(j + 1);
                         if (c > kNbCapNb - 2) prune_nearest<BLOCK>(lst, c, st, p.x, p.y, p.z);
@@ -699,7 +695,7 @@ __global__ void __launch_bounds__(BLOCK) k_density_nb(const float4* __restrict__
                         float dx, dy, dz;
                         const float d2 = canon_d2(p.x, p.y, p.z, o.x, o.y, o.z, dx, dy, dz);
                         if (!(d2 < cut)) continue;
-                        const float wgt = h2 - d2;
+                        const float wgt = cut - d2;
                         kahan_add(sum, comp, wgt * wgt * wgt);
                         if (j == t) continue;
                         if (c < kNbList) {

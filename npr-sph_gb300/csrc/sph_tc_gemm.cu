@@ -32,15 +32,27 @@ constexpr int kChunkK8 = kKC / 8;       // 16-byte chunks per row of a staged ch
 constexpr uint32_t kLBO = 128;
 constexpr uint32_t kSBO = kKC * 16;
 
-__device__ __forceinline__ void stage_rows(uint8_t* tile, const __nv_bfloat16* __restrict__ G, int ld, int rows,
-                                           int row0, int nrow_valid, int k0, int kend) {
-    const int total = rows * kChunkK8;
-    for (int c = threadIdx.x; c < total; c += kThreads) {
+// Copy rows row0 .. row0 + ROWS - 1, columns k0 .. k0 + kKC - 1 of G into the tile (zeros past
+// nrow_valid and kend). Each thread issues all of its 16-byte loads before any store, so the
+// loads of a chunk are in flight together.
+template <int ROWS>
+__device__ __forceinline__ void stage_rows(uint8_t* tile, const __nv_bfloat16* __restrict__ G, int ld, int row0,
+                                           int nrow_valid, int k0, int kend) {
+    constexpr int kTotal = ROWS * kChunkK8;
+    constexpr int kPer = (kTotal + kThreads - 1) / kThreads;
+    uint4 v[kPer];
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) {
+        const int c = threadIdx.x + i * kThreads;
         const int r = c / kChunkK8, k8 = c % kChunkK8;
         const int gr = row0 + r, gk = k0 + 8 * k8;
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (gr < nrow_valid && gk < kend) v = *reinterpret_cast<const uint4*>(G + (size_t)gr * ld + gk);
-        *reinterpret_cast<uint4*>(tile + tile_off(r, k8, kKC)) = v;
+        v[i] = make_uint4(0u, 0u, 0u, 0u);
+        if (c < kTotal && gr < nrow_valid && gk < kend) v[i] = __ldg(reinterpret_cast<const uint4*>(G + (size_t)gr * ld + gk));
+    }
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) {
+        const int c = threadIdx.x + i * kThreads;
+        if (c < kTotal) *reinterpret_cast<uint4*>(tile + tile_off(c / kChunkK8, c % kChunkK8, kKC)) = v[i];
     }
 }
 
@@ -52,8 +64,8 @@ __global__ void __launch_bounds__(kThreads) k_gemm_bf16(const __nv_bfloat16* __r
     constexpr uint32_t kCols = tmem_cols_for(N);
     constexpr int kTileBytesA = kTileM * kKC * 2, kTileBytesB = N * kKC * 2;
     extern __shared__ __align__(1024) uint8_t smem[];
-    uint8_t* bufA[2] = {smem, smem + kTileBytesA + kTileBytesB};
-    uint8_t* bufB[2] = {smem + kTileBytesA, smem + 2 * kTileBytesA + kTileBytesB};
+    // buffer b: its A tile at smem + b * kBufBytes, its B tile right after
+    constexpr int kBufBytes = kTileBytesA + kTileBytesB;
     __shared__ __align__(8) uint64_t mbar[2];
     __shared__ uint32_t tmem_slot;
     __shared__ int timed_out;
@@ -81,13 +93,14 @@ __global__ void __launch_bounds__(kThreads) k_gemm_bf16(const __nv_bfloat16* __r
         if (c >= 2 && !mbar_wait(&mbar[b], ((c - 2) >> 1) & 1)) ok = false;
         if (__syncthreads_or(!ok)) { ok = false; break; }
         const int k0 = kb + c * kKC;
-        stage_rows(bufA[b], A, lda, kTileM, m0, M, k0, ke);
-        stage_rows(bufB[b], B, ldb, N, 0, N, k0, ke);
+        uint8_t* const tA = smem + b * kBufBytes;
+        stage_rows<kTileM>(tA, A, lda, m0, M, k0, ke);
+        stage_rows<N>(tA + kTileBytesA, B, ldb, 0, N, k0, ke);
         fence_smem_to_async();
         __syncthreads();
         if (threadIdx.x == 0) {
             fence_after_sync();
-            const uint32_t a0 = smem_u32(bufA[b]), b0 = smem_u32(bufB[b]);
+            const uint32_t a0 = smem_u32(smem + b * kBufBytes), b0 = a0 + (uint32_t)kTileBytesA;
             const int steps = min(kKC, ke - k0) / 16;
             for (int s = 0; s < steps; ++s)
                 mma_bf16(tmem, smem_desc(a0 + 256u * s, kLBO, kSBO), smem_desc(b0 + 256u * s, kLBO, kSBO), idesc,

@@ -1,7 +1,7 @@
 """Train the learned macro-step network on trajectories the GPU SPH step generates.
 
     python npr-sph_gb300/train_mpnn.py [--scenes 200] [--particles 65536] [--frames 24]
-                                       [--gap 32] [--steps 30000] [--out npr-sph_gb300/weights/mpnn_w64.npy]
+                                       [--gap 8] [--steps 60000] [--out npr-sph_gb300/weights/mpnn_w64.npy]
 
 Training data: `scenes` seeded runs of `particles` particles each, advanced together in one
 batched context with the literal mass and smoothing length and g = -9.81. Per run the stiffness k
@@ -71,8 +71,8 @@ def main() -> None:
     ap.add_argument("--scenes", type=int, default=200)
     ap.add_argument("--particles", type=int, default=65536)
     ap.add_argument("--frames", type=int, default=24, help="frames per run")
-    ap.add_argument("--gap", type=int, default=32, help="plain steps between frames")
-    ap.add_argument("--steps", type=int, default=30000, help="Adam steps")
+    ap.add_argument("--gap", type=int, default=8, help="plain steps between frames")
+    ap.add_argument("--steps", type=int, default=60000, help="Adam steps")
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--seed", type=int, default=4)
     ap.add_argument("--precision", type=int, default=1, choices=[0, 1],
