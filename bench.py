@@ -505,7 +505,8 @@ def learned_workload(args, stream, flush) -> dict:
         # One unjudged macro-step (sort, neighbour lists, two inference rounds, update) with each
         # BF16 inference kernel set, from the same state, CUDA events over 8 macro-steps.
         kernels = {}
-        for name, prec in (("mma_sync", 1), ("tcgen05", 2)):
+        for name, prec in (("tcgen05_round1_lanes+mma_sync_round2 (default)", 3), ("mma_sync", 1),
+                           ("tcgen05_edges_on_lanes", 2)):
             net.set_precision(prec)
             learned.upload(sc.particles)
             learned.step(args.warmup)
@@ -517,7 +518,7 @@ def learned_workload(args, stream, flush) -> dict:
             e1.record(stream)
             torch.cuda.synchronize()
             kernels[name] = {"ms_per_macro_step": e0.elapsed_time(e1) / 8}
-        net.set_precision(1)
+        net.set_precision(3)
         # What the network gains: one judged macro-step from the same state (the plain run's
         # end state) with the trained network and with a zero network (v' = v, x' = x + 4 dt v,
         # then the momentum projection adds gravity).
@@ -535,8 +536,8 @@ def learned_workload(args, stream, flush) -> dict:
         "judge_mean_density": runs["judge_mean_density"],
         "one_macro_step_vs_4_plain_steps": gain,
         "inference_kernels": kernels,
-        "precision": "BF16 weights/activations, FP32 accumulate (mma.sync m16n8k16; the tcgen05 kernels are "
-                     "timed in inference_kernels)",
+        "precision": "BF16 weights/activations, FP32 accumulate: round 1 tcgen05 MMAs (TMEM accumulators), "
+                     "round 2 mma.sync m16n8k16; every kernel set is timed in inference_kernels",
         "weights": str(WEIGHTS.relative_to(REPO)),
     })
     return out

@@ -276,9 +276,10 @@ sph_status sph_mpnn_loss_grad(sph_mpnn* net, uint32_t n, const float* pos4, cons
                               const float* target8, const float fc[6], double* loss, float* out8,
                               float* grad);
 /* Network output (n x 8: O_v, O_x, 0, 0) of a host frame as above: precision 1 runs the
- * macro-step's default inference kernels (BF16 mma.sync, FP32 accumulation), 3 the BF16
- * tcgen05 inference kernels (FP32 accumulation in tensor memory), 0 the FP32 training
- * forward, 2 the training forward with the node layers on the BF16 tensor-core GEMMs. */
+ * mma.sync inference kernels (BF16, FP32 accumulation), 4 the macro-step's default inference
+ * (round 1 tcgen05 with the features on the tensor-memory lanes, round 2 mma.sync), 3 the
+ * tcgen05 kernels of sph_mpnn_set_precision(net, 2), 0 the FP32 training forward, 2 the
+ * training forward with the node layers on the BF16 tensor-core GEMMs. */
 sph_status sph_mpnn_forward(sph_mpnn* net, uint32_t n, const float* pos4, const float* vel4,
                             const float* rhop2, const int32_t* nb, const int32_t* cnt, const float fc[6],
                             int32_t precision, float* out8);
@@ -289,9 +290,10 @@ sph_status sph_mpnn_forward(sph_mpnn* net, uint32_t n, const float* pos4, const 
  * 144). Synchronous; SPH_ERR_DEVICE if a tensor-core wait timed out. */
 sph_status sph_tc_gemm_bf16(const uint16_t* a, const uint16_t* b, int32_t m, int32_t n, int32_t k, int32_t splits,
                             float* d);
-/* Inference of sph_learned_step: 1 BF16 mma.sync tensor-core kernels (default), 2 BF16
- * tcgen05 kernels (FP32 accumulators in tensor memory; slower on the 1M dam break: 2.97
- * against 2.03 ms per macro-step), 0 FP32 CUDA cores. */
+/* Inference kernels of sph_learned_step, all BF16 on the tensor cores with FP32 accumulation
+ * unless 0: 3 (default) round 1 as tcgen05 MMAs with the features on the tensor-memory lanes
+ * and round 2 as mma.sync; 1 both rounds mma.sync; 2 both rounds tcgen05 with the edges on the
+ * tensor-memory lanes (slower: the edge sum crosses lanes); 0 FP32 CUDA cores. */
 sph_status sph_mpnn_set_precision(sph_mpnn* net, int32_t precision);
 /* Precision of the training passes (sph_mpnn_loss_grad, sph_mpnn_train): 1 (default) runs
  * the node layers -- forward, data gradients and weight gradients -- as BF16 GEMMs on the

@@ -59,7 +59,8 @@ struct sph_mpnn {
     void* harena = nullptr;
     int adam_t = 0;  // Adam steps taken since the parameters were last set
     // BF16 tensor-core inference
-    int precision = 1;               // inference: 1 BF16 mma.sync (default), 2 BF16 tcgen05, 0 FP32 CUDA cores
+    int precision = 3;               // inference: 3 BF16 tcgen05 round 1 (features on the TMEM lanes) +
+                                     // mma.sync round 2 (default), 1 BF16 mma.sync, 2 BF16 tcgen05, 0 FP32
     int train_precision = 1;         // training node layers: 1 BF16 tcgen05 GEMMs (default), 0 FP32
     uint32_t* frags = nullptr;       // parameters in MMA fragment order (mma.sync kernels)
     __nv_bfloat16* tcw = nullptr;    // parameters as tcgen05 shared-memory images
@@ -367,6 +368,11 @@ sph_status learned_macro(sph_ctx* ctx, sph_mpnn* net) {
         M::tc_infer_round2(f, net->tcw, net->H1b, reinterpret_cast<const __half*>(net->Pperm), net->Obuf, net->tc_err,
                            ctx->stream);
         O = net->Obuf;
+    } else if (net->precision == 3) {
+        M::tc_infer_round1_lanes(f, net->tcw, net->H1b, net->Pperm, net->tc_err, ctx->stream);
+        M::infer_round2(f, net->frags, M::trainer_params(net->tr), net->H1b, net->Pperm, ctx->s0, nullptr, nullptr,
+                        net->Obuf, nullptr, nullptr, nullptr, false, ctx->stream);
+        O = net->Obuf;
     } else if (net->precision == 1) {
         M::infer_round1(f, net->frags, net->H1b, net->Pperm, ctx->stream);
         M::infer_round2(f, net->frags, M::trainer_params(net->tr), net->H1b, net->Pperm, ctx->s0, nullptr, nullptr,
@@ -562,7 +568,7 @@ sph_status sph_mpnn_loss_grad(sph_mpnn* net, uint32_t n, const float* pos4, cons
 }
 
 sph_status sph_mpnn_set_precision(sph_mpnn* net, int32_t precision) {
-    if (!net || precision < 0 || precision > 2) return SPH_ERR_INVALID_ARG;
+    if (!net || precision < 0 || precision > 3) return SPH_ERR_INVALID_ARG;
     net->precision = precision;
     return SPH_OK;
 }
@@ -577,7 +583,7 @@ sph_status sph_mpnn_set_train_precision(sph_mpnn* net, int32_t precision) {
 sph_status sph_mpnn_forward(sph_mpnn* net, uint32_t n, const float* pos4, const float* vel4, const float* rhop2,
                             const int32_t* nb, const int32_t* cnt, const float fc[6], int32_t precision, float* out8) {
     if (!net || !pos4 || !vel4 || !rhop2 || !nb || !cnt || !fc || !out8 || n == 0) return SPH_ERR_INVALID_ARG;
-    if (precision < 0 || precision > 3) return SPH_ERR_INVALID_ARG;
+    if (precision < 0 || precision > 4) return SPH_ERR_INVALID_ARG;
     if ((int)n > M::trainer_capacity(net->tr)) { net->err = "frame larger than the training workspace"; return SPH_ERR_CAPACITY; }
     for (uint32_t i = 0; i < n; ++i) {
         if (cnt[i] < 0 || cnt[i] > M::K) { net->err = "neighbour count out of [0, 32]"; return SPH_ERR_INVALID_ARG; }
@@ -617,14 +623,25 @@ sph_status sph_mpnn_forward(sph_mpnn* net, uint32_t n, const float* pos4, const 
             net->err = "tensor-core inference wait timed out";
             return SPH_ERR_DEVICE;
         }
-    } else if (precision == 1) {  // the macro-step's default inference: the mma.sync kernels
+    } else if (precision == 1 || precision == 4) {  // mma.sync (4: its round 1 on tcgen05, features on lanes)
         sph_status s2 = ensure_bf16(net, (int)n, st);
         if (s2) return s2;
         SceneDev S{};
-        M::infer_round1(f, net->frags, net->H1b, net->Pperm, st);
+        if (precision == 4) M::tc_infer_round1_lanes(f, net->tcw, net->H1b, net->Pperm, net->tc_err, st);
+        else M::infer_round1(f, net->frags, net->H1b, net->Pperm, st);
         M::infer_round2(f, net->frags, M::trainer_params(net->tr), net->H1b, net->Pperm, S, nullptr, nullptr, dout,
                         nullptr, nullptr, nullptr, false, st);
         NCK(cudaMemcpyAsync(out8, dout, (size_t)n * 4 * M::kOS, cudaMemcpyDeviceToHost, st));
+        if (precision == 4) {
+            uint32_t e = 0;
+            NCK(cudaMemcpyAsync(&e, net->tc_err, sizeof(e), cudaMemcpyDeviceToHost, st));
+            NCK(cudaStreamSynchronize(st));
+            if (e) {
+                cudaMemsetAsync(net->tc_err, 0, sizeof(e), st);
+                net->err = "tensor-core inference wait timed out";
+                return SPH_ERR_DEVICE;
+            }
+        }
     } else {  // the training forward: 0 FP32, 2 BF16 tensor-core node layers
         const bool tc_was = M::trainer_tc(net->tr);
         M::trainer_set_tc(net->tr, precision == 2);

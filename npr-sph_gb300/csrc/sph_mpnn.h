@@ -139,6 +139,10 @@ void tc_infer_round1(const Frame& f, const __nv_bfloat16* img, __nv_bfloat16* H1
                      cudaStream_t st);
 void tc_infer_round2(const Frame& f, const __nv_bfloat16* img, const __nv_bfloat16* H1, const __half* P, float* out,
                      uint32_t* err, cudaStream_t st);
+// Round 1 with the features on the TMEM lanes (the edge sum inside each thread); writes H1 and P
+// in the permuted BF16 layout of the mma.sync round 2 (infer_round2).
+void tc_infer_round1_lanes(const Frame& f, const __nv_bfloat16* img, __nv_bfloat16* H1, uint16_t* Pperm, uint32_t* err,
+                           cudaStream_t st);
 
 }  // namespace mpnn
 }  // namespace sphgb

@@ -63,7 +63,9 @@ constexpr int kImgWp = kImgWn1 + W * kKX1;
 constexpr int kImgWe2 = kImgWp + W * kKH1;
 constexpr int kImgWn2 = kImgWe2 + W * kKE;
 constexpr int kImgWo = kImgWn2 + W * kKX2;
-constexpr int kImgTotal = kImgWo + kNO * kKH2;
+constexpr int kImgAE1 = kImgWo + kNO * kKH2;  // round 1 with the features on the TMEM lanes:
+constexpr int kKA = 32;                          // [128][32], rows 0..63 [We1' | 0], rows 64..127 [0 | We1']
+constexpr int kImgTotal = kImgAE1 + 128 * kKA;
 
 __host__ __device__ constexpr uint32_t sbo(int kc) { return (uint32_t)kc * 16u; }
 
@@ -82,6 +84,12 @@ __device__ __forceinline__ float wv(const float* prm, int woff, int boff, int ki
 __global__ void k_tc_infer_prep(const float* __restrict__ prm, __nv_bfloat16* __restrict__ img) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= kImgTotal) return;
+    if (t >= kImgAE1) {  // the block-diagonal edge weights of round 1 (two sub-tiles stacked along K)
+        const int r = t - kImgAE1, m = r / kKA, k = r % kKA, half = m >> 6;
+        const float v = (k >> 4) == half ? wv(prm, kWe1, kBe1, FE, W, FE, m & 63, k & 15) : 0.0f;
+        img[kImgAE1 + img_at(m, k, kKA)] = __float2bfloat16_rn(v);
+        return;
+    }
     int base, kc, woff, boff, kin, nout, brow;
     if (t < kImgWn1) { base = kImgWe1; kc = kKE; woff = kWe1; boff = kBe1; kin = FE; nout = W; brow = FE; }
     else if (t < kImgWp) { base = kImgWn1; kc = kKX1; woff = kWn1; boff = kBn1; kin = W + FN; nout = W; brow = W + FN; }
@@ -450,6 +458,241 @@ __global__ void __launch_bounds__(kThr) k_tc_round(const float4* __restrict__ po
     if (warp == 0) tc::tmem_dealloc(tmem, kCols);
 }
 
+// ---- round 1 with the features on the TMEM lanes -------------------------------------------
+// The edge MMA of k_tc_round puts the edges on the TMEM lanes, so the sum over a particle's 32
+// edges crosses the lanes of a warp. Here the 64 features are the lanes and the edges the
+// columns: D [128 x 128] = A [128 x 32] * B [128 x 32]^T where B's row n holds edge n of two
+// 4-particle sub-tiles X and Y side by side ([e_X(n) | e_Y(n)], 16 features each) and A is
+// block-diagonal ([We1' | 0] for rows 0..63, [0 | We1'] for rows 64..127), so rows 0..63 of D
+// are sub-tile X's pre-activations and rows 64..127 sub-tile Y's. Thread t drains TMEM lane t
+// (feature t % 64 of sub-tile t / 64): for each of the 4 particles, 32 consecutive columns =
+// its 32 edges, ReLU-packed to f16x2 and summed by a tree inside the thread. One MMA covers 8
+// particles; a 128-particle tile is 16 MMAs, then the node layers as in k_tc_round. P is
+// written in the permuted BF16 layout that the mma.sync round 2 (sph_mpnn_infer.cu) reads.
+constexpr int kLanesMma = kTP / 8;  // edge MMAs per tile (even: the barrier's phases restart)
+static_assert(kLanesMma % 2 == 0, "barrier phases must restart with every tile");
+struct SmemLanes {
+    static constexpr int kOffAE = 0;                          // [128][32] block-diagonal We1'
+    static constexpr int kOffWn = kOffAE + 128 * kKA * 2;     // Wn1' [64][80] then Wp [64][64]
+    static constexpr int kOffB = kOffWn + (kImgWe2 - kImgWn1) * 2;  // edge tile [128][32]
+    static constexpr int kOffX = kOffB + 128 * kKA * 2;       // node tile [128][80]
+    static constexpr int kBytes = kOffX + kTP * kKX1 * 2;
+};
+
+__global__ void __launch_bounds__(kThr) k_tc_r1_lanes(const float4* __restrict__ pos, const float4* __restrict__ vel,
+                                                      const float2* __restrict__ rhop, const int* __restrict__ nb,
+                                                      const int* __restrict__ cnt, FrameConst fc, int n,
+                                                      const __nv_bfloat16* __restrict__ img,
+                                                      __nv_bfloat16* __restrict__ H1, uint4* __restrict__ Pperm,
+                                                      uint32_t* __restrict__ err) {
+    using L = SmemLanes;
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ uint32_t tmem_slot;
+    __shared__ int bad;
+    uint8_t* const sB = smem + L::kOffB;
+    uint8_t* const sX = smem + L::kOffX;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    {
+        const uint4* a = reinterpret_cast<const uint4*>(img + kImgAE1);
+        uint4* da = reinterpret_cast<uint4*>(smem + L::kOffAE);
+        for (int i = tid; i < 128 * kKA * 2 / 16; i += kThr) da[i] = __ldg(a + i);
+        const uint4* w = reinterpret_cast<const uint4*>(img + kImgWn1);
+        uint4* dw = reinterpret_cast<uint4*>(smem + L::kOffWn);
+        for (int i = tid; i < (kImgWe2 - kImgWn1) * 2 / 16; i += kThr) dw[i] = __ldg(w + i);
+    }
+    if (tid == 0) {
+        tc::mbar_init(&mbar[0], 1);
+        tc::mbar_init(&mbar[1], 1);
+        tc::mbar_init_fence();
+        bad = 0;
+    }
+    if (warp == 0) tc::tmem_alloc(&tmem_slot, kCols);
+    tc::fence_smem_to_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tmem_slot;
+    const uint32_t s_ae = smem_u32(smem + L::kOffAE), s_wn = smem_u32(smem + L::kOffWn);
+    const uint32_t s_wp = s_wn + (uint32_t)((kImgWp - kImgWn1) * 2);
+    const uint32_t sb = smem_u32(sB), sx = smem_u32(sX);
+    const uint32_t id_e = tc::idesc_bf16_f32(128, 128), id_n = tc::idesc_bf16_f32(128, W);
+    const float ih = 1.0f / fc.h, ic = 1.0f / fc.c;
+    const int ntiles = (n + kTP - 1) / kTP;
+    const int q = tid >> 5, e = tid & 31;   // the edge column this thread builds: particle q, slot e
+    const int f = tid & 63, half = tid >> 6;  // the TMEM lane it drains: feature f of sub-tile half
+
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int tile0 = tile * kTP;
+        {  // node features, bias column and padding (columns 64 .. 79) of particle tid
+            const int p = tile0 + tid;
+            float v[16];
+#pragma unroll
+            for (int c = 0; c < 16; ++c) v[c] = 0.0f;
+            if (p < n) {
+                const float4 vi = vel[p];
+                const float rho = rhop[p].x;
+                v[0] = vi.x * ic; v[1] = vi.y * ic; v[2] = vi.z * ic;
+                v[3] = rho / fc.rho_self - 1.0f;
+                v[4] = (rho - fc.rho0) / fc.rho_self;
+                v[5] = fc.log_mu;
+                v[6] = (float)min(max(cnt[p], 0), K) / K;
+                v[7] = 1.0f;
+                v[8] = fc.courant;
+                v[9] = 1.0f;
+            }
+#pragma unroll
+            for (int c = 0; c < 2; ++c)
+                *reinterpret_cast<uint4*>(sX + tile_off(tid, 8 + c, kKX1)) =
+                    make_uint4(pk_bf16(v[8 * c], v[8 * c + 1]), pk_bf16(v[8 * c + 2], v[8 * c + 3]),
+                               pk_bf16(v[8 * c + 4], v[8 * c + 5]), pk_bf16(v[8 * c + 6], v[8 * c + 7]));
+        }
+        // edge phase: MMA i takes sub-tile X = particles 8 i .. 8 i + 3, Y = 8 i + 4 .. 8 i + 7
+        int jx = edge_j(tile0 + q, e, n, nb, cnt), jy = edge_j(tile0 + 4 + q, e, n, nb, cnt);
+        EdgeIn ix = edge_load(tile0 + q, jx, pos, vel), iy = edge_load(tile0 + 4 + q, jy, pos, vel);
+        jx = edge_j(tile0 + 8 + q, e, n, nb, cnt);
+        jy = edge_j(tile0 + 12 + q, e, n, nb, cnt);
+        bool quit = false;
+        for (int i = 0; i < kLanesMma; ++i) {
+            {
+                uint4 w[4] = {make_uint4(0u, 0u, 0u, 0u), make_uint4(0u, 0u, 0u, 0u), make_uint4(0u, 0u, 0u, 0u),
+                              make_uint4(0u, 0u, 0u, 0u)};
+                if (ix.j >= 0) edge_feat16(ix.pi, ix.vi, ix.pj, ix.vj, ih, ic, w[0], w[1]);
+                if (iy.j >= 0) edge_feat16(iy.pi, iy.vi, iy.pj, iy.vj, ih, ic, w[2], w[3]);
+#pragma unroll
+                for (int c = 0; c < 4; ++c) *reinterpret_cast<uint4*>(sB + tile_off(tid, c, kKA)) = w[c];
+            }
+            tc::fence_smem_to_async();
+            tc::fence_before_sync();
+            if (__syncthreads_or(bad)) { quit = true; break; }
+            if (tid == 0) {
+                tc::fence_after_sync();
+                for (int k = 0; k < kKA / 16; ++k)
+                    tc::mma_bf16(tmem, smem_desc(s_ae + 256u * k, 128u, sbo(kKA)), smem_desc(sb + 256u * k, 128u, sbo(kKA)),
+                                 id_e, k > 0 ? 1u : 0u);
+                tc::mma_commit(&mbar[0]);
+            }
+            if (i + 1 < kLanesMma) {  // gathers of MMA i + 1, neighbour indices of MMA i + 2, in flight
+                const int b1 = tile0 + 8 * (i + 1);
+                ix = edge_load(b1 + q, jx, pos, vel);
+                iy = edge_load(b1 + 4 + q, jy, pos, vel);
+                jx = i + 2 < kLanesMma ? edge_j(b1 + 8 + q, e, n, nb, cnt) : -1;
+                jy = i + 2 < kLanesMma ? edge_j(b1 + 12 + q, e, n, nb, cnt) : -1;
+            }
+            if (!tc::mbar_wait(&mbar[0], i & 1)) bad = 1;
+            if (__syncthreads_or(bad)) { quit = true; break; }
+            tc::fence_after_sync();
+#pragma unroll 1
+            for (int pq = 0; pq < 4; ++pq) {
+                uint32_t r[32];
+                tc::tmem_ld32(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(32 * pq), r);
+                tc::tmem_wait_ld();
+                uint32_t h[16];
+#pragma unroll
+                for (int k = 0; k < 16; ++k) h[k] = relu_f16x2(__uint_as_float(r[2 * k]), __uint_as_float(r[2 * k + 1]));
+#pragma unroll
+                for (int w = 8; w >= 1; w >>= 1)
+#pragma unroll
+                    for (int k = 0; k < w; ++k) h[k] = hadd2(h[k], h[k + w]);
+                const float2 s2 = __half22float2(*reinterpret_cast<__half2*>(&h[0]));
+                const int row = 8 * i + 4 * half + pq;
+                *reinterpret_cast<__nv_bfloat16*>(sX + tile_off(row, f >> 3, kKX1) + (f & 7) * 2) =
+                    __float2bfloat16_rn((s2.x + s2.y) * (1.0f / K));
+            }
+            tc::fence_before_sync();  // the next MMA overwrites the accumulator
+        }
+        if (quit) break;
+        // node layers: H1 = relu([M1 n 1] Wn1'), then P = H1 Wp
+        tc::fence_smem_to_async();
+        tc::fence_before_sync();
+        if (__syncthreads_or(bad)) break;
+        if (tid == 0) {
+            tc::fence_after_sync();
+            for (int k = 0; k < kKX1 / 16; ++k)
+                tc::mma_bf16(tmem, smem_desc(sx + 256u * k, 128u, sbo(kKX1)), smem_desc(s_wn + 256u * k, 128u, sbo(kKX1)),
+                             id_n, k > 0 ? 1u : 0u);
+            tc::mma_commit(&mbar[1]);
+        }
+        if (!tc::mbar_wait(&mbar[1], 0)) bad = 1;
+        if (__syncthreads_or(bad)) break;
+        tc::fence_after_sync();
+        const int p = tile0 + tid;
+        {
+            float hv[64];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                float v[16];
+                tc::tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(16 * c), v);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) hv[16 * c + j] = fmaxf(v[j], 0.0f);
+            }
+            tc::tmem_wait_ld();
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                const uint4 w = make_uint4(pk_bf16(hv[8 * c], hv[8 * c + 1]), pk_bf16(hv[8 * c + 2], hv[8 * c + 3]),
+                                           pk_bf16(hv[8 * c + 4], hv[8 * c + 5]), pk_bf16(hv[8 * c + 6], hv[8 * c + 7]));
+                *reinterpret_cast<uint4*>(sX + tile_off(tid, c, kKH1)) = w;
+                if (p < n) reinterpret_cast<uint4*>(H1 + (size_t)p * W)[c] = w;
+            }
+        }
+        tc::fence_smem_to_async();
+        tc::fence_before_sync();
+        if (__syncthreads_or(bad)) break;
+        if (tid == 0) {
+            tc::fence_after_sync();
+            for (int k = 0; k < kKH1 / 16; ++k)
+                tc::mma_bf16(tmem + (uint32_t)W, smem_desc(sx + 256u * k, 128u, sbo(kKH1)),
+                             smem_desc(s_wp + 256u * k, 128u, sbo(kKH1)), id_n, k > 0 ? 1u : 0u);
+            tc::mma_commit(&mbar[1]);
+        }
+        if (!tc::mbar_wait(&mbar[1], 1)) bad = 1;
+        if (__syncthreads_or(bad)) break;
+        tc::fence_after_sync();
+        {
+            float pv[64];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                float v[16];
+                tc::tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(W + 16 * c), v);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) pv[16 * c + j] = v[j];
+            }
+            tc::tmem_wait_ld();
+            if (p < n) {  // word mt of lane group g: features (16 mt + g, 16 mt + g + 8)
+#pragma unroll
+                for (int g = 0; g < 8; ++g)
+                    Pperm[(size_t)p * 8 + g] =
+                        make_uint4(pk_bf16(pv[g], pv[g + 8]), pk_bf16(pv[16 + g], pv[24 + g]),
+                                   pk_bf16(pv[32 + g], pv[40 + g]), pk_bf16(pv[48 + g], pv[56 + g]));
+            }
+        }
+        tc::fence_before_sync();
+        __syncthreads();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (bad && tid == 0 && err) atomicOr(err, 1u);
+    if (warp == 0) tc::tmem_dealloc(tmem, kCols);
+}
+
+int lanes_grid(int n) {
+    static int per_sm = 0;
+    if (!per_sm) {
+        cudaFuncSetAttribute(k_tc_r1_lanes, cudaFuncAttributeMaxDynamicSharedMemorySize, SmemLanes::kBytes);
+        int dev = 0, smem_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+        cudaFuncAttributes fa{};
+        cudaFuncGetAttributes(&fa, k_tc_r1_lanes);
+        per_sm = smem_sm / (SmemLanes::kBytes + (int)fa.sharedSizeBytes + 1024);
+        if (per_sm < 1) per_sm = 1;
+        if (per_sm > 4) per_sm = 4;
+    }
+    const int ntiles = (n + kTP - 1) / kTP;
+    const int cap = device_sm_count() * per_sm;
+    return ntiles < cap ? ntiles : cap;
+}
+
 // Resident CTAs per SM: shared memory (dynamic + static + the 1 KB the hardware reserves per
 // CTA) and TMEM (4 x 128 columns) decide; the persistent grid holds that many per SM.
 template <bool ROUND2>
@@ -487,6 +730,14 @@ void tc_infer_round1(const Frame& f, const __nv_bfloat16* img, __nv_bfloat16* H1
     const int g = tc_grid<false>(f.n);
     k_tc_round<false><<<g, kThr, Smem<false>::kBytes, st>>>(f.pos, f.vel, f.rhop, f.nb, f.cnt, f.fc, f.n, img, H1, P,
                                                             nullptr, err);
+}
+
+void tc_infer_round1_lanes(const Frame& f, const __nv_bfloat16* img, __nv_bfloat16* H1, uint16_t* Pperm, uint32_t* err,
+                           cudaStream_t st) {
+    if (f.n <= 0) return;
+    const int g = lanes_grid(f.n);
+    k_tc_r1_lanes<<<g, kThr, SmemLanes::kBytes, st>>>(f.pos, f.vel, f.rhop, f.nb, f.cnt, f.fc, f.n, img, H1,
+                                                     reinterpret_cast<uint4*>(Pperm), err);
 }
 
 void tc_infer_round2(const Frame& f, const __nv_bfloat16* img, const __nv_bfloat16* H1, const __half* P, float* out,

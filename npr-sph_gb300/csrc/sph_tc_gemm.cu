@@ -127,18 +127,54 @@ __global__ void __launch_bounds__(kThreads) k_gemm_bf16(const __nv_bfloat16* __r
                 for (int j = 0; j < 16; ++j) v[j] = 0.0f;
             }
             if (row >= M) continue;
+            const bool full = c0 + 16 <= epi.ncols;
+            if (!split_k) {
+                // 16-byte loads and stores where the chunk is whole and the rows are 16-byte aligned
+                if (epi.add) {
+                    const float* a = epi.add + (size_t)row * epi.ld_add + c0;
+                    if (full && ((reinterpret_cast<uintptr_t>(a) & 15) == 0)) {
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                const int col = c0 + j;
-                if (col >= epi.ncols) break;
-                float x = v[j];
-                if (!split_k) {
-                    if (epi.add) x += epi.add[(size_t)row * epi.ld_add + col];
-                    if (epi.relu) x = fmaxf(x, 0.0f);
-                    if (epi.gate && !(epi.gate[(size_t)row * epi.ld_gate + col] > 0.0f)) x = 0.0f;
-                    if (epi.outb) epi.outb[(size_t)row * epi.ld_outb + col] = __float2bfloat16_rn(x);
+                        for (int j = 0; j < 16; j += 4) {
+                            const float4 t = *reinterpret_cast<const float4*>(a + j);
+                            v[j] += t.x; v[j + 1] += t.y; v[j + 2] += t.z; v[j + 3] += t.w;
+                        }
+                    } else {
+                        for (int j = 0; j < 16 && c0 + j < epi.ncols; ++j) v[j] += a[j];
+                    }
                 }
-                if (out) out[(size_t)row * epi.ld_out + col] = x;
+                if (epi.relu) {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) v[j] = fmaxf(v[j], 0.0f);
+                }
+                if (epi.gate) {
+                    const float* gt = epi.gate + (size_t)row * epi.ld_gate + c0;
+                    if (full && ((reinterpret_cast<uintptr_t>(gt) & 15) == 0)) {
+#pragma unroll
+                        for (int j = 0; j < 16; j += 4) {
+                            const float4 t = *reinterpret_cast<const float4*>(gt + j);
+                            if (!(t.x > 0.0f)) v[j] = 0.0f;
+                            if (!(t.y > 0.0f)) v[j + 1] = 0.0f;
+                            if (!(t.z > 0.0f)) v[j + 2] = 0.0f;
+                            if (!(t.w > 0.0f)) v[j + 3] = 0.0f;
+                        }
+                    } else {
+                        for (int j = 0; j < 16 && c0 + j < epi.ncols; ++j)
+                            if (!(gt[j] > 0.0f)) v[j] = 0.0f;
+                    }
+                }
+                if (epi.outb)
+                    for (int j = 0; j < 16 && c0 + j < epi.ncols; ++j)
+                        epi.outb[(size_t)row * epi.ld_outb + c0 + j] = __float2bfloat16_rn(v[j]);
+            }
+            if (out) {
+                float* o = out + (size_t)row * epi.ld_out + c0;
+                if (full && ((reinterpret_cast<uintptr_t>(o) & 15) == 0)) {
+#pragma unroll
+                    for (int j = 0; j < 16; j += 4)
+                        *reinterpret_cast<float4*>(o + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+                } else {
+                    for (int j = 0; j < 16 && c0 + j < epi.ncols; ++j) o[j] = v[j];
+                }
             }
         }
     } else if (threadIdx.x == 0 && err) {

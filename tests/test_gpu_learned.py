@@ -110,12 +110,13 @@ def test_tensor_core_training_matches_fp64_oracle(sph, gpu, seed):
         off += size
 
 
-@pytest.mark.parametrize("seed,precision", [(5, 1), (6, 1), (5, 3), (6, 3)])
+@pytest.mark.parametrize("seed,precision", [(5, 1), (6, 1), (5, 3), (6, 3), (5, 4), (6, 4)])
 def test_bf16_tensor_core_inference_matches_fp32_forward(sph, gpu, seed, precision):
     """The inference kernels -- precision 1: the macro-step's default mma.sync kernels (BF16,
     FP32 accumulation); 3: the tcgen05 kernels (BF16 MMAs, FP32 accumulation in TMEM, f16 edge
-    sums) -- against the FP32 forward on the same frame: BF16 rounds weights and activations to
-    8 mantissa bits, so the outputs agree to a few percent of their scale."""
+    sums); 4: round 1 on tcgen05 with the features on the TMEM lanes, round 2 mma.sync --
+    against the FP32 forward on the same frame: BF16 rounds weights and activations to 8
+    mantissa bits, so the outputs agree to a few percent of their scale."""
     from oracle import mpnn_oracle as MO
 
     pos, vel, rho, nb, cnt, target, fc = random_frame(seed, n=200)
@@ -141,9 +142,10 @@ INF_TOL, INF_RMS, INF_CORR = 5e-2, 1.5e-2, 0.999
 WEIGHTS = __import__("pathlib").Path(__file__).resolve().parents[1] / "npr-sph_gb300" / "weights" / "mpnn_w64.npy"
 
 
-@pytest.mark.parametrize("steps,precision", [(8, 1), (60, 1), (8, 3), (60, 3)])
+@pytest.mark.parametrize("steps,precision", [(8, 1), (60, 1), (8, 3), (60, 3), (8, 4), (60, 4)])
 def test_tensor_core_inference_matches_fp64_oracle_on_dam_break(sph, gpu, steps, precision):
-    """The BF16 inference kernels (precision 1: mma.sync, the macro-step's default; 3: tcgen05)
+    """The BF16 inference kernels (precision 1: mma.sync, the macro-step's default; 3: tcgen05;
+    4: tcgen05 round 1 with the features on the TMEM lanes, mma.sync round 2)
     with the committed trained weights, on the neighbour lists, densities and state of a
     16,384-particle dam break after `steps` plain steps, against oracle/mpnn_oracle.py in FP64
     on the same inputs."""
