@@ -479,12 +479,17 @@ struct SmemLanes {
     static constexpr int kBytes = kOffX + kTP * kKX1 * 2;
 };
 
-__global__ void __launch_bounds__(kThr) k_tc_r1_lanes(const float4* __restrict__ pos, const float4* __restrict__ vel,
-                                                      const float2* __restrict__ rhop, const int* __restrict__ nb,
-                                                      const int* __restrict__ cnt, FrameConst fc, int n,
-                                                      const __nv_bfloat16* __restrict__ img,
-                                                      __nv_bfloat16* __restrict__ H1, uint4* __restrict__ Pperm,
-                                                      uint32_t* __restrict__ err) {
+// 256 threads: warps w and w + 4 reach the same 32 TMEM lanes and split the work of a lane
+// group (the columns of the edge accumulator, the halves of a node row), so twice the warps
+// hide the neighbour gathers. Thread t builds edge column t % 128 of sub-tile t / 128.
+constexpr int kThrL = 256;
+
+__global__ void __launch_bounds__(kThrL, 4) k_tc_r1_lanes(const float4* __restrict__ pos, const float4* __restrict__ vel,
+                                                       const float2* __restrict__ rhop, const int* __restrict__ nb,
+                                                       const int* __restrict__ cnt, FrameConst fc, int n,
+                                                       const __nv_bfloat16* __restrict__ img,
+                                                       __nv_bfloat16* __restrict__ H1, uint4* __restrict__ Pperm,
+                                                       uint32_t* __restrict__ err) {
     using L = SmemLanes;
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ __align__(8) uint64_t mbar[2];
@@ -496,10 +501,10 @@ __global__ void __launch_bounds__(kThr) k_tc_r1_lanes(const float4* __restrict__
     {
         const uint4* a = reinterpret_cast<const uint4*>(img + kImgAE1);
         uint4* da = reinterpret_cast<uint4*>(smem + L::kOffAE);
-        for (int i = tid; i < 128 * kKA * 2 / 16; i += kThr) da[i] = __ldg(a + i);
+        for (int i = tid; i < 128 * kKA * 2 / 16; i += kThrL) da[i] = __ldg(a + i);
         const uint4* w = reinterpret_cast<const uint4*>(img + kImgWn1);
         uint4* dw = reinterpret_cast<uint4*>(smem + L::kOffWn);
-        for (int i = tid; i < (kImgWe2 - kImgWn1) * 2 / 16; i += kThr) dw[i] = __ldg(w + i);
+        for (int i = tid; i < (kImgWe2 - kImgWn1) * 2 / 16; i += kThrL) dw[i] = __ldg(w + i);
     }
     if (tid == 0) {
         tc::mbar_init(&mbar[0], 1);
@@ -519,13 +524,17 @@ __global__ void __launch_bounds__(kThr) k_tc_r1_lanes(const float4* __restrict__
     const uint32_t id_e = tc::idesc_bf16_f32(128, 128), id_n = tc::idesc_bf16_f32(128, W);
     const float ih = 1.0f / fc.h, ic = 1.0f / fc.c;
     const int ntiles = (n + kTP - 1) / kTP;
-    const int q = tid >> 5, e = tid & 31;   // the edge column this thread builds: particle q, slot e
-    const int f = tid & 63, half = tid >> 6;  // the TMEM lane it drains: feature f of sub-tile half
+    const int lane_t = tid & 127;                  // the TMEM lane (and node row) this thread serves
+    const int grp = tid >> 7;                      // which half of that lane's work it does
+    const int col = tid & 127, sub = tid >> 7;     // the edge it builds: column col of sub-tile sub
+    const int q = col >> 5, e = col & 31;          //   = particle q of the sub-tile, slot e
+    const int f = lane_t & 63, half = lane_t >> 6; // the lane it drains: feature f of sub-tile half
+    const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
 
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int tile0 = tile * kTP;
-        {  // node features, bias column and padding (columns 64 .. 79) of particle tid
-            const int p = tile0 + tid;
+        if (grp == 0) {  // node features, bias column and padding (columns 64 .. 79) of particle lane_t
+            const int p = tile0 + lane_t;
             float v[16];
 #pragma unroll
             for (int c = 0; c < 16; ++c) v[c] = 0.0f;
@@ -543,24 +552,21 @@ __global__ void __launch_bounds__(kThr) k_tc_r1_lanes(const float4* __restrict__
             }
 #pragma unroll
             for (int c = 0; c < 2; ++c)
-                *reinterpret_cast<uint4*>(sX + tile_off(tid, 8 + c, kKX1)) =
+                *reinterpret_cast<uint4*>(sX + tile_off(lane_t, 8 + c, kKX1)) =
                     make_uint4(pk_bf16(v[8 * c], v[8 * c + 1]), pk_bf16(v[8 * c + 2], v[8 * c + 3]),
                                pk_bf16(v[8 * c + 4], v[8 * c + 5]), pk_bf16(v[8 * c + 6], v[8 * c + 7]));
         }
-        // edge phase: MMA i takes sub-tile X = particles 8 i .. 8 i + 3, Y = 8 i + 4 .. 8 i + 7
-        int jx = edge_j(tile0 + q, e, n, nb, cnt), jy = edge_j(tile0 + 4 + q, e, n, nb, cnt);
-        EdgeIn ix = edge_load(tile0 + q, jx, pos, vel), iy = edge_load(tile0 + 4 + q, jy, pos, vel);
-        jx = edge_j(tile0 + 8 + q, e, n, nb, cnt);
-        jy = edge_j(tile0 + 12 + q, e, n, nb, cnt);
+        // edge phase: MMA i takes sub-tile 0 = particles 8 i .. 8 i + 3, sub-tile 1 = 8 i + 4 .. 8 i + 7
+        int jn = edge_j(tile0 + 4 * sub + q, e, n, nb, cnt);
+        EdgeIn in = edge_load(tile0 + 4 * sub + q, jn, pos, vel);
+        jn = edge_j(tile0 + 8 + 4 * sub + q, e, n, nb, cnt);
         bool quit = false;
         for (int i = 0; i < kLanesMma; ++i) {
             {
-                uint4 w[4] = {make_uint4(0u, 0u, 0u, 0u), make_uint4(0u, 0u, 0u, 0u), make_uint4(0u, 0u, 0u, 0u),
-                              make_uint4(0u, 0u, 0u, 0u)};
-                if (ix.j >= 0) edge_feat16(ix.pi, ix.vi, ix.pj, ix.vj, ih, ic, w[0], w[1]);
-                if (iy.j >= 0) edge_feat16(iy.pi, iy.vi, iy.pj, iy.vj, ih, ic, w[2], w[3]);
-#pragma unroll
-                for (int c = 0; c < 4; ++c) *reinterpret_cast<uint4*>(sB + tile_off(tid, c, kKA)) = w[c];
+                uint4 w0 = make_uint4(0u, 0u, 0u, 0u), w1 = w0;
+                if (in.j >= 0) edge_feat16(in.pi, in.vi, in.pj, in.vj, ih, ic, w0, w1);
+                *reinterpret_cast<uint4*>(sB + tile_off(col, 2 * sub, kKA)) = w0;
+                *reinterpret_cast<uint4*>(sB + tile_off(col, 2 * sub + 1, kKA)) = w1;
             }
             tc::fence_smem_to_async();
             tc::fence_before_sync();
@@ -572,28 +578,27 @@ __global__ void __launch_bounds__(kThr) k_tc_r1_lanes(const float4* __restrict__
                                  id_e, k > 0 ? 1u : 0u);
                 tc::mma_commit(&mbar[0]);
             }
-            if (i + 1 < kLanesMma) {  // gathers of MMA i + 1, neighbour indices of MMA i + 2, in flight
-                const int b1 = tile0 + 8 * (i + 1);
-                ix = edge_load(b1 + q, jx, pos, vel);
-                iy = edge_load(b1 + 4 + q, jy, pos, vel);
-                jx = i + 2 < kLanesMma ? edge_j(b1 + 8 + q, e, n, nb, cnt) : -1;
-                jy = i + 2 < kLanesMma ? edge_j(b1 + 12 + q, e, n, nb, cnt) : -1;
+            if (i + 1 < kLanesMma) {  // gathers of MMA i + 1, neighbour index of MMA i + 2, in flight
+                const int b1 = tile0 + 8 * (i + 1) + 4 * sub + q;
+                in = edge_load(b1, jn, pos, vel);
+                jn = i + 2 < kLanesMma ? edge_j(b1 + 8, e, n, nb, cnt) : -1;
             }
             if (!tc::mbar_wait(&mbar[0], i & 1)) bad = 1;
             if (__syncthreads_or(bad)) { quit = true; break; }
             tc::fence_after_sync();
 #pragma unroll 1
-            for (int pq = 0; pq < 4; ++pq) {
+            for (int k = 0; k < 2; ++k) {  // this thread's two particles of the lane's sub-tile
+                const int pq = 2 * grp + k;
                 uint32_t r[32];
-                tc::tmem_ld32(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(32 * pq), r);
+                tc::tmem_ld32(tmem + lane_base + (uint32_t)(32 * pq), r);
                 tc::tmem_wait_ld();
                 uint32_t h[16];
 #pragma unroll
-                for (int k = 0; k < 16; ++k) h[k] = relu_f16x2(__uint_as_float(r[2 * k]), __uint_as_float(r[2 * k + 1]));
+                for (int u = 0; u < 16; ++u) h[u] = relu_f16x2(__uint_as_float(r[2 * u]), __uint_as_float(r[2 * u + 1]));
 #pragma unroll
                 for (int w = 8; w >= 1; w >>= 1)
 #pragma unroll
-                    for (int k = 0; k < w; ++k) h[k] = hadd2(h[k], h[k + w]);
+                    for (int u = 0; u < w; ++u) h[u] = hadd2(h[u], h[u + w]);
                 const float2 s2 = __half22float2(*reinterpret_cast<__half2*>(&h[0]));
                 const int row = 8 * i + 4 * half + pq;
                 *reinterpret_cast<__nv_bfloat16*>(sX + tile_off(row, f >> 3, kKX1) + (f & 7) * 2) =
@@ -602,7 +607,7 @@ __global__ void __launch_bounds__(kThr) k_tc_r1_lanes(const float4* __restrict__
             tc::fence_before_sync();  // the next MMA overwrites the accumulator
         }
         if (quit) break;
-        // node layers: H1 = relu([M1 n 1] Wn1'), then P = H1 Wp
+        // node layers: H1 = relu([M1 n 1] Wn1'), then P = H1 Wp; node row lane_t, columns 32 grp ..
         tc::fence_smem_to_async();
         tc::fence_before_sync();
         if (__syncthreads_or(bad)) break;
@@ -616,23 +621,23 @@ __global__ void __launch_bounds__(kThr) k_tc_r1_lanes(const float4* __restrict__
         if (!tc::mbar_wait(&mbar[1], 0)) bad = 1;
         if (__syncthreads_or(bad)) break;
         tc::fence_after_sync();
-        const int p = tile0 + tid;
-        {
-            float hv[64];
+        const int p = tile0 + lane_t;
+        {  // the X tile is no longer read (its MMA completed): H1 goes over it
+            float hv[32];
 #pragma unroll
-            for (int c = 0; c < 4; ++c) {
+            for (int c = 0; c < 2; ++c) {
                 float v[16];
-                tc::tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(16 * c), v);
+                tc::tmem_ld16(tmem + lane_base + (uint32_t)(32 * grp + 16 * c), v);
 #pragma unroll
                 for (int j = 0; j < 16; ++j) hv[16 * c + j] = fmaxf(v[j], 0.0f);
             }
             tc::tmem_wait_ld();
 #pragma unroll
-            for (int c = 0; c < 8; ++c) {
+            for (int c = 0; c < 4; ++c) {
                 const uint4 w = make_uint4(pk_bf16(hv[8 * c], hv[8 * c + 1]), pk_bf16(hv[8 * c + 2], hv[8 * c + 3]),
                                            pk_bf16(hv[8 * c + 4], hv[8 * c + 5]), pk_bf16(hv[8 * c + 6], hv[8 * c + 7]));
-                *reinterpret_cast<uint4*>(sX + tile_off(tid, c, kKH1)) = w;
-                if (p < n) reinterpret_cast<uint4*>(H1 + (size_t)p * W)[c] = w;
+                *reinterpret_cast<uint4*>(sX + tile_off(lane_t, 4 * grp + c, kKH1)) = w;
+                if (p < n) reinterpret_cast<uint4*>(H1 + (size_t)p * W)[4 * grp + c] = w;
             }
         }
         tc::fence_smem_to_async();
@@ -649,21 +654,20 @@ __global__ void __launch_bounds__(kThr) k_tc_r1_lanes(const float4* __restrict__
         if (__syncthreads_or(bad)) break;
         tc::fence_after_sync();
         {
-            float pv[64];
+            float pv[32];  // features 32 grp .. 32 grp + 31
 #pragma unroll
-            for (int c = 0; c < 4; ++c) {
+            for (int c = 0; c < 2; ++c) {
                 float v[16];
-                tc::tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(W + 16 * c), v);
+                tc::tmem_ld16(tmem + lane_base + (uint32_t)(W + 32 * grp + 16 * c), v);
 #pragma unroll
                 for (int j = 0; j < 16; ++j) pv[16 * c + j] = v[j];
             }
             tc::tmem_wait_ld();
-            if (p < n) {  // word mt of lane group g: features (16 mt + g, 16 mt + g + 8)
+            if (p < n) {  // words 2 grp, 2 grp + 1 of lane group g: features (16 mt + g, 16 mt + g + 8)
+                uint2* dst = reinterpret_cast<uint2*>(Pperm + (size_t)p * 8);
 #pragma unroll
                 for (int g = 0; g < 8; ++g)
-                    Pperm[(size_t)p * 8 + g] =
-                        make_uint4(pk_bf16(pv[g], pv[g + 8]), pk_bf16(pv[16 + g], pv[24 + g]),
-                                   pk_bf16(pv[32 + g], pv[40 + g]), pk_bf16(pv[48 + g], pv[56 + g]));
+                    dst[2 * g + grp] = make_uint2(pk_bf16(pv[g], pv[g + 8]), pk_bf16(pv[16 + g], pv[24 + g]));
             }
         }
         tc::fence_before_sync();
@@ -736,7 +740,7 @@ void tc_infer_round1_lanes(const Frame& f, const __nv_bfloat16* img, __nv_bfloat
                            cudaStream_t st) {
     if (f.n <= 0) return;
     const int g = lanes_grid(f.n);
-    k_tc_r1_lanes<<<g, kThr, SmemLanes::kBytes, st>>>(f.pos, f.vel, f.rhop, f.nb, f.cnt, f.fc, f.n, img, H1,
+    k_tc_r1_lanes<<<g, kThrL, SmemLanes::kBytes, st>>>(f.pos, f.vel, f.rhop, f.nb, f.cnt, f.fc, f.n, img, H1,
                                                      reinterpret_cast<uint4*>(Pperm), err);
 }
 
