@@ -298,7 +298,7 @@ sph_status create_impl(const sph_params* params, const uint32_t* counts, uint32_
         dalloc(&b.rhop, n) || dalloc(&b.force_s, n) || dalloc(&b.force_up, n) || dalloc(&b.aux, n) ||
         dalloc(&b.key, n) || dalloc(&b.rank, n) || dalloc(&b.perm, n) || dalloc(&b.slot_of_id, n) ||
         dalloc(&b.err, 1) || dalloc(&b.scenes, nscene) || dalloc(&b.tile_stats, 2) ||
-        dalloc(&b.pmask, n * kPairMaskWords) ||
+        dalloc(&b.pmask, n * kPairMaskWords) || dalloc(&b.rec, 2 * n) ||
         dalloc(&b.partials, reduce_partials_doubles((int)nscene)) ||
         dalloc(&ctx->diag_dev, (size_t)nscene * kDiagFields) || dalloc(&ctx->scene_first_dev, nscene + 1))
         return bail(SPH_ERR_OUT_OF_MEMORY);
@@ -473,7 +473,7 @@ sph_status sph_destroy(sph_ctx* ctx) {
     Buffers& b = ctx->b;
     void* ptrs[] = {b.pos, b.vel, b.pos_s, b.vel_s, b.rhop, b.force_s, b.force_up, b.aux, b.aos, b.key, b.rank,
                     b.perm, b.count, b.start, b.scan_state, b.slot_of_id, b.err, b.partials,
-                    b.scenes, b.tile_stats, b.pmask, ctx->diag_dev, ctx->scene_first_dev, ctx->q_ids, ctx->q_cnt, ctx->q_dig,
+                    b.scenes, b.tile_stats, b.pmask, b.rec, ctx->diag_dev, ctx->scene_first_dev, ctx->q_ids, ctx->q_cnt, ctx->q_dig,
                     ctx->fd_cnt, ctx->fd_sum, ctx->pc_dev,
                     ctx->render_buf, ctx->sdf_dev};
     for (void* p : ptrs)

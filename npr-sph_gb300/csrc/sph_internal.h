@@ -75,6 +75,8 @@ struct Buffers {
     int nscene = 1;
     uint32_t* tile_stats = nullptr;  // [0] chunks staged, [1] chunks on the global-memory path
     uint32_t* pmask = nullptr; // [kPairMaskWords][n]: the density pass's neighbour predicates for the force pass
+    float4* rec = nullptr;     // [n][2]: (x, y, z, p), (vx, vy, vz, 1/rho) per sorted slot, written by the
+                               // density pass (stencil 1) for the force pass's neighbour reads
 };
 
 // Stencil 1 (cells of edge h): the density pass stores, per particle and per neighbour-row

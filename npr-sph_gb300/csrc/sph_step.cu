@@ -271,10 +271,11 @@ static_assert(stage_cap<2, 256>() < 65536, "staged indices are 16-bit");
 static_assert(kNbCapNb >= kNbList + 2, "the nearest-kNbList pruning runs when two more entries could overflow");
 
 template <bool BATCHED, int R, int BLOCK>
-__global__ void __launch_bounds__(BLOCK) k_density(const float4* __restrict__ pos_s, const int* __restrict__ start,
-                                                   SceneDev s0, const SceneDev* __restrict__ scenes, int nscene,
-                                                   float2* __restrict__ rhop, uint32_t* __restrict__ pmask, int n,
-                                                   uint32_t* __restrict__ stats) {
+__global__ void __launch_bounds__(BLOCK) k_density(const float4* __restrict__ pos_s, const float4* __restrict__ vel_s,
+                                                   const int* __restrict__ start, SceneDev s0,
+                                                   const SceneDev* __restrict__ scenes, int nscene,
+                                                   float2* __restrict__ rhop, uint32_t* __restrict__ pmask,
+                                                   float4* __restrict__ rec, int n, uint32_t* __restrict__ stats) {
     using G = TileGeom<R>;
     constexpr int kCap = stage_cap<R, BLOCK>();
     constexpr bool kMask = R == 1;  // pair masks for the force pass (kPairMaskWords words per particle)
@@ -360,11 +361,24 @@ __global__ void __launch_bounds__(BLOCK) k_density(const float4* __restrict__ po
             }
             const float rho = S.poly6c * sum;
             const float pr = S.gas_k * (rho - S.rho0);
-            rhop[t] = make_float2(rho, pr < 0.0f ? 0.0f : pr);  // GLSL max(x, 0): NaN stays NaN
+            const float prc = pr < 0.0f ? 0.0f : pr;  // GLSL max(x, 0): NaN stays NaN
+            rhop[t] = make_float2(rho, prc);
+            if constexpr (kMask) {  // the force pass's neighbour record: one 32-byte load per neighbour
+                const float4 v = vel_s[t];
+                rec[2 * (size_t)t] = make_float4(p.x, p.y, p.z, prc);
+                rec[2 * (size_t)t + 1] = make_float4(v.x, v.y, v.z, __fdividef(1.0f, rho));
+            }
         }
         if (!tiled && threadIdx.x == 0 && stats) atomicAdd(&stats[0], 1u);
         __syncthreads();  // the next chunk reuses the tile
     }
+}
+
+// One 32-byte record (two float4) in a single 256-bit read-only load; r is 32-byte aligned.
+__device__ __forceinline__ void ld_record(const float4* r, float4& a, float4& b) {
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(r));
 }
 
 struct ForceAcc {
@@ -374,12 +388,16 @@ struct ForceAcc {
     // lanes of the two vector sums run as packed FP32x2 operations.
     __device__ __forceinline__ void add(float dx, float dy, float dz, float h, float pi, float4 v, float2 rj,
                                         float4 vj) {
+        add(dx, dy, dz, h, pi, v, rj.y, __fdividef(1.0f, rj.x), vj);
+    }
+    // The same with the neighbour's pressure pj and 1/rho_j (as __fdividef(1, rho_j)) given.
+    __device__ __forceinline__ void add(float dx, float dy, float dz, float h, float pi, float4 v, float pj, float irho,
+                                        float4 vj) {
         const float d2 = dx * dx + dy * dy + dz * dz;
-        const float irho = __fdividef(1.0f, rj.x);
         const float inv_r = rsqrtf(d2);
         const float r = d2 > 0.0f ? d2 * inv_r : 0.0f;
         const float hr = h - r;
-        const float s = d2 > 0.0f ? (pi + rj.y) * irho * hr * hr * inv_r : 0.0f;  // spiky gradient
+        const float s = d2 > 0.0f ? (pi + pj) * irho * hr * hr * inv_r : 0.0f;  // spiky gradient
         fp_xy = __ffma2_rn(make_float2(s, s), make_float2(dx, dy), fp_xy);
         fpz = fmaf(s, dz, fpz);
         const float c = irho * hr;                                                // Laplacian
@@ -398,7 +416,8 @@ __global__ void __launch_bounds__(BLOCK) k_force_integrate(const float4* __restr
                                                            float4* __restrict__ pos_out, float4* __restrict__ vel_out,
                                                            float4* __restrict__ force_out, int* __restrict__ key_out,
                                                            int* __restrict__ rank_out, int* __restrict__ count,
-                                                           const uint32_t* __restrict__ pmask, int n,
+                                                           const uint32_t* __restrict__ pmask,
+                                                           const float4* __restrict__ rec, int n,
                                                            uint32_t* __restrict__ stats, uint32_t* __restrict__ dig_cnt,
                                                            unsigned long long* __restrict__ dig_sum) {
     using G = TileGeom<R>;
@@ -435,15 +454,16 @@ __global__ void __launch_bounds__(BLOCK) k_force_integrate(const float4* __restr
             int cnt = 0;
             uint32_t dcount = 1;                                                 // DIGEST: self
             unsigned long long dsum = mix64((unsigned long long)id_of(v));
-            // Stencil 1: neighbours come from global memory. List entry e is candidate e & 4095 of
-            // row segment e >> 12, whose first candidate is global slot seg_slot[segment].
+            // Stencil 1: neighbours come from global memory, each as the density pass's 32-byte
+            // record (position, p_j, velocity, 1/rho_j) in one load. List entry e is candidate
+            // e & 4095 of row segment e >> 12, whose first candidate is global slot seg_slot[segment].
             auto interact = [&](int g) {
-                const float4 q = __ldg(pos_s + g);
-                const float4 vj = __ldg(vel_s + g);
-                acc.add(p.x - q.x, p.y - q.y, p.z - q.z, h, rp.y, v, __ldg(rhop + g), vj);
+                float4 q, vj;
+                ld_record(rec + 2 * (size_t)g, q, vj);
+                acc.add(p.x - q.x, p.y - q.y, p.z - q.z, h, rp.y, v, q.w, vj.w, vj);
                 if constexpr (DIGEST) {
                     ++dcount;
-                    dsum += mix64((unsigned long long)id_of(vj));
+                    dsum += mix64((unsigned long long)id_of(__ldg(vel_s + g)));
                 }
             };
             auto flush_slots = [&]() {
@@ -751,8 +771,8 @@ template <bool B, int R, int BLOCK>
 void density_impl(const Buffers& b, const SceneDev& s0, cudaStream_t st) {
     auto k = k_density<B, R, BLOCK>;
     constexpr size_t sm = density_smem<R, BLOCK>();
-    k<<<grid_size(k, BLOCK, sm, b.n), BLOCK, sm, st>>>(b.pos_s, b.start, s0, b.scenes, b.nscene, b.rhop, b.pmask,
-                                                       b.n, b.tile_stats);
+    k<<<grid_size(k, BLOCK, sm, b.n), BLOCK, sm, st>>>(b.pos_s, b.vel_s, b.start, s0, b.scenes, b.nscene, b.rhop,
+                                                       b.pmask, b.rec, b.n, b.tile_stats);
 }
 
 template <bool B, int R, int BLOCK>
@@ -762,7 +782,8 @@ void force_impl(const Buffers& b, const SceneDev& s0, float4* force_out, uint32_
     auto launch = [&](auto k) {
         k<<<grid_size(k, BLOCK, sm, b.n), BLOCK, sm, st>>>(b.pos_s, b.vel_s, b.rhop, b.start, s0, b.scenes, b.nscene,
                                                            b.pos, b.vel, force_out, s0.sdf ? nullptr : b.key, b.rank,
-                                                           b.count, b.pmask, b.n, b.tile_stats, dig_cnt, dig_sum);
+                                                           b.count, b.pmask, b.rec, b.n, b.tile_stats, dig_cnt,
+                                                           dig_sum);
     };
     if constexpr (R == 1) {
         if (dig_cnt) {
