@@ -214,6 +214,15 @@ sph_status sph_pair_counts(sph_ctx* ctx, uint64_t out[2]);
  * that did not fit a shared-memory tile and read their neighbours from global
  * memory instead (heavy pile-ups). Synchronous. */
 sph_status sph_tile_stats(sph_ctx* ctx, uint32_t out[2]);
+/* Steps since creation whose force pass read each neighbour as one 32-byte
+ * record written by the density pass (out[0]), steps that read position,
+ * velocity and (rho, p) from the state arrays (out[1]), and the same-cell
+ * pairs (sum over the grid's cells of count^2, self included) that the last
+ * sort seen by the host found (out[2]). A step uses records when out[2] is
+ * above 2.6 per particle (stencil 1 only; dense fluid); both forms compute
+ * the same interactions from the same values, so the choice changes only the
+ * speed. */
+sph_status sph_record_stats(const sph_ctx* ctx, uint64_t out[3]);
 
 /* ---- learned macro-step (new; no reference counterpart) -----------------
  * A message-passing network (2 rounds over the <= 32 nearest neighbours,

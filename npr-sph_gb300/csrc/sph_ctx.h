@@ -22,9 +22,11 @@ struct sph_ctx {
     sphgb::LaunchCfg cfg;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t gexec = nullptr;
-    bool graph_dirty = true;
+    // the step's graph without [0] and with [1] the neighbour records (captured when first used)
+    cudaGraph_t graph[2] = {nullptr, nullptr};
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    unsigned long long* pair_host = nullptr;  // mapped host word: same-cell pairs of the last sort
+    uint64_t record_steps[2] = {0, 0};        // steps run with [0] / without [1] neighbour records
     bool have_state = false, need_hash = true, stepped = false;
     uint64_t steps = 0;
     // judge state of the learned macro-step, kept across sph_learned_step calls (cleared by uploads)

@@ -127,11 +127,12 @@ cudaError_t dalloc(T** p, size_t count) {
 }
 
 void free_graph(sph_ctx* ctx) {
-    if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
-    if (ctx->graph) cudaGraphDestroy(ctx->graph);
-    ctx->gexec = nullptr;
-    ctx->graph = nullptr;
-    ctx->graph_dirty = true;
+    for (int m = 0; m < 2; ++m) {
+        if (ctx->gexec[m]) cudaGraphExecDestroy(ctx->gexec[m]);
+        if (ctx->graph[m]) cudaGraphDestroy(ctx->graph[m]);
+        ctx->gexec[m] = nullptr;
+        ctx->graph[m] = nullptr;
+    }
 }
 
 // Recompute the scene table (cell ranges, particle ranges, constants) and grow
@@ -191,26 +192,38 @@ void enqueue_sort(sph_ctx* ctx) {
     launch_gather(ctx->b, ctx->stream);
 }
 
-void enqueue_pairs(sph_ctx* ctx) {
-    launch_density(ctx->b, ctx->s0, ctx->batched, ctx->cfg, ctx->stream);
-    launch_force_integrate(ctx->b, ctx->s0, ctx->batched, ctx->cfg, ctx->stream);
+// Whether the next step uses the neighbour records: from the same-cell pairs of the last sort
+// that has written them to host-mapped memory (the host may be a few steps ahead of the device).
+// Only the speed depends on the answer.
+bool record_mode(const sph_ctx* ctx) {
+    if (ctx->cfg.stencil != 1 || !ctx->pair_host || ctx->b.n <= 0) return false;
+    const unsigned long long pairs = *reinterpret_cast<const volatile unsigned long long*>(ctx->pair_host);
+    return (double)pairs > kRecordCellPairs * (double)ctx->b.n;
 }
 
-sph_status capture_graph(sph_ctx* ctx) {
-    free_graph(ctx);
+void enqueue_pairs(sph_ctx* ctx, bool rec) {
+    launch_density(ctx->b, ctx->s0, ctx->batched, ctx->cfg, rec, ctx->stream);
+    launch_force_integrate(ctx->b, ctx->s0, ctx->batched, ctx->cfg, rec, ctx->stream);
+}
+
+sph_status capture_graph(sph_ctx* ctx, int m) {
+    if (ctx->gexec[m]) cudaGraphExecDestroy(ctx->gexec[m]);
+    if (ctx->graph[m]) cudaGraphDestroy(ctx->graph[m]);
+    ctx->gexec[m] = nullptr;
+    ctx->graph[m] = nullptr;
     CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     enqueue_sort(ctx);
-    enqueue_pairs(ctx);
-    cudaError_t e = cudaStreamEndCapture(ctx->stream, &ctx->graph);
+    enqueue_pairs(ctx, m != 0);
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &ctx->graph[m]);
     cudaError_t launch_err = cudaGetLastError();  // also clears the thread's error state
     if (e == cudaSuccess) e = launch_err;
     if (e != cudaSuccess) {
-        if (ctx->graph) cudaGraphDestroy(ctx->graph);
-        ctx->graph = nullptr;
+        if (ctx->graph[m]) cudaGraphDestroy(ctx->graph[m]);
+        ctx->graph[m] = nullptr;
         return fail(ctx, SPH_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
     }
-    CK(cudaGraphInstantiate(&ctx->gexec, ctx->graph, 0));
-    ctx->graph_dirty = false;
+    CK(cudaGraphInstantiate(&ctx->gexec[m], ctx->graph[m], 0));
+    CK(cudaGraphUpload(ctx->gexec[m], ctx->stream));  // not on the first launch
     return SPH_OK;
 }
 
@@ -234,9 +247,11 @@ sph_status run_steps(sph_ctx* ctx, int n) {
             if (ctx->need_hash) { launch_hash(ctx->b, ctx->s0, ctx->batched, ctx->stream); ctx->need_hash = false; }
             enqueue_sort(ctx);
             CK(cudaEventRecord(ctx->ev[1], ctx->stream));
-            launch_density(ctx->b, ctx->s0, ctx->batched, ctx->cfg, ctx->stream);
+            const bool rec = record_mode(ctx);
+            ++ctx->record_steps[rec ? 0 : 1];
+            launch_density(ctx->b, ctx->s0, ctx->batched, ctx->cfg, rec, ctx->stream);
             CK(cudaEventRecord(ctx->ev[2], ctx->stream));
-            launch_force_integrate(ctx->b, ctx->s0, ctx->batched, ctx->cfg, ctx->stream);
+            launch_force_integrate(ctx->b, ctx->s0, ctx->batched, ctx->cfg, rec, ctx->stream);
             CK(cudaEventRecord(ctx->ev[3], ctx->stream));
             CK(cudaEventSynchronize(ctx->ev[3]));
             for (int k = 0; k < 3; ++k) {
@@ -250,11 +265,18 @@ sph_status run_steps(sph_ctx* ctx, int n) {
             launch_hash(ctx->b, ctx->s0, ctx->batched, ctx->stream);
             ctx->need_hash = false;
         }
-        if (ctx->graph_dirty) {
-            sph_status st = capture_graph(ctx);
-            if (st) return st;
+        for (int s = 0; s < n; ++s) {
+            const int m = record_mode(ctx) ? 1 : 0;
+            if (!ctx->gexec[m]) {  // both forms at once: a later switch costs no capture
+                for (int k = 0; k < (ctx->cfg.stencil == 1 ? 2 : 1); ++k) {
+                    if (ctx->gexec[k]) continue;
+                    sph_status st = capture_graph(ctx, k);
+                    if (st) return st;
+                }
+            }
+            CK(cudaGraphLaunch(ctx->gexec[m], ctx->stream));
+            ++ctx->record_steps[1 - m];
         }
-        for (int s = 0; s < n; ++s) CK(cudaGraphLaunch(ctx->gexec, ctx->stream));
     }
     CK(cudaGetLastError());
     ctx->steps += (uint64_t)n;
@@ -298,13 +320,18 @@ sph_status create_impl(const sph_params* params, const uint32_t* counts, uint32_
         dalloc(&b.rhop, n) || dalloc(&b.force_s, n) || dalloc(&b.force_up, n) || dalloc(&b.aux, n) ||
         dalloc(&b.key, n) || dalloc(&b.rank, n) || dalloc(&b.perm, n) || dalloc(&b.slot_of_id, n) ||
         dalloc(&b.err, 1) || dalloc(&b.scenes, nscene) || dalloc(&b.tile_stats, 2) ||
-        dalloc(&b.pmask, n * kPairMaskWords) || dalloc(&b.rec, 2 * n) ||
+        dalloc(&b.pmask, n * kPairMaskWords) || dalloc(&b.rec, 2 * n) || dalloc(&b.cell_pairs, 1) ||
         dalloc(&b.partials, reduce_partials_doubles((int)nscene)) ||
         dalloc(&ctx->diag_dev, (size_t)nscene * kDiagFields) || dalloc(&ctx->scene_first_dev, nscene + 1))
         return bail(SPH_ERR_OUT_OF_MEMORY);
     if (cudaMemsetAsync(b.err, 0, sizeof(uint32_t), ctx->stream) ||
-        cudaMemsetAsync(b.tile_stats, 0, sizeof(uint32_t) * 2, ctx->stream))
+        cudaMemsetAsync(b.tile_stats, 0, sizeof(uint32_t) * 2, ctx->stream) ||
+        cudaMemsetAsync(b.cell_pairs, 0, sizeof(unsigned long long), ctx->stream))
         return bail(SPH_ERR_CUDA);
+    if (cudaHostAlloc(&ctx->pair_host, sizeof(unsigned long long), cudaHostAllocMapped) != cudaSuccess)
+        return bail(SPH_ERR_OUT_OF_MEMORY);
+    *ctx->pair_host = 0;
+    if (cudaHostGetDevicePointer(&b.cell_pairs_map, ctx->pair_host, 0) != cudaSuccess) return bail(SPH_ERR_CUDA);
     for (auto& e : ctx->ev)
         if (cudaEventCreate(&e) != cudaSuccess) return bail(SPH_ERR_CUDA);
     if (cudaStreamCreateWithFlags(&ctx->xfer, cudaStreamNonBlocking) != cudaSuccess) return bail(SPH_ERR_CUDA);
@@ -473,11 +500,12 @@ sph_status sph_destroy(sph_ctx* ctx) {
     Buffers& b = ctx->b;
     void* ptrs[] = {b.pos, b.vel, b.pos_s, b.vel_s, b.rhop, b.force_s, b.force_up, b.aux, b.aos, b.key, b.rank,
                     b.perm, b.count, b.start, b.scan_state, b.slot_of_id, b.err, b.partials,
-                    b.scenes, b.tile_stats, b.pmask, b.rec, ctx->diag_dev, ctx->scene_first_dev, ctx->q_ids, ctx->q_cnt, ctx->q_dig,
+                    b.scenes, b.tile_stats, b.pmask, b.rec, b.cell_pairs, ctx->diag_dev, ctx->scene_first_dev, ctx->q_ids, ctx->q_cnt, ctx->q_dig,
                     ctx->fd_cnt, ctx->fd_sum, ctx->pc_dev,
                     ctx->render_buf, ctx->sdf_dev};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    if (ctx->pair_host) cudaFreeHost(ctx->pair_host);
     for (auto& e : ctx->ev)
         if (e) cudaEventDestroy(e);
     if (ctx->xfer) cudaStreamDestroy(ctx->xfer);
@@ -691,8 +719,8 @@ sph_status sph_step_neighbor_digest(sph_ctx* ctx, const uint32_t* query_ids, uin
         ctx->need_hash = false;
     }
     enqueue_sort(ctx);
-    launch_density(ctx->b, ctx->s0, ctx->batched, ctx->cfg, ctx->stream);
-    launch_force_integrate(ctx->b, ctx->s0, ctx->batched, ctx->cfg, ctx->stream, ctx->fd_cnt, ctx->fd_sum);
+    launch_density(ctx->b, ctx->s0, ctx->batched, ctx->cfg, false, ctx->stream);
+    launch_force_integrate(ctx->b, ctx->s0, ctx->batched, ctx->cfg, false, ctx->stream, ctx->fd_cnt, ctx->fd_sum);
     launch_slot_of_id(ctx->b, ctx->stream);  // id -> slot of the step's sorted state
     if (n_query) {
         CK(cudaMemcpyAsync(ctx->q_ids, query_ids, sizeof(uint32_t) * n_query, cudaMemcpyHostToDevice, ctx->stream));
@@ -747,6 +775,14 @@ sph_status sph_tile_stats(sph_ctx* ctx, uint32_t out[2]) {
     CK(cudaSetDevice(ctx->device));
     CK(cudaMemcpyAsync(out, ctx->b.tile_stats, sizeof(uint32_t) * 2, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    return SPH_OK;
+}
+
+sph_status sph_record_stats(const sph_ctx* ctx, uint64_t out[3]) {
+    if (!ctx || !out) return SPH_ERR_INVALID_ARG;
+    out[0] = ctx->record_steps[0];
+    out[1] = ctx->record_steps[1];
+    out[2] = ctx->pair_host ? *reinterpret_cast<const volatile unsigned long long*>(ctx->pair_host) : 0;
     return SPH_OK;
 }
 

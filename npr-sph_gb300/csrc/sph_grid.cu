@@ -79,17 +79,26 @@ __device__ __forceinline__ int block_sum(int x, int* s_warp) {
     return t;
 }
 
+// Also adds the tile's same-cell pairs, sum of count^2 (self included), to *cell_pairs.
 __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const int* __restrict__ count, int ncell,
-                                                             int* __restrict__ tile_sum) {
+                                                             int* __restrict__ tile_sum,
+                                                             unsigned long long* __restrict__ cell_pairs) {
     __shared__ int s_warp[kScanThreads / 32];
     const long long base = (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanItems;
     int v[kScanItems];
     load_tile_counts(count, base, ncell, v);
     int sum = 0;
+    unsigned long long sq = 0;
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) sum += v[k];
+    for (int k = 0; k < kScanItems; ++k) {
+        sum += v[k];
+        sq += (unsigned long long)((long long)v[k] * v[k]);
+    }
     const int total = block_sum(sum, s_warp);
     if (threadIdx.x == 0) tile_sum[blockIdx.x] = total;
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
+    if ((threadIdx.x & 31) == 0 && sq) atomicAdd(cell_pairs, sq);
 }
 
 __global__ void __launch_bounds__(kScanThreads) k_scan_apply(int* __restrict__ count, int* __restrict__ start, int ncell,
@@ -139,7 +148,12 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_apply(int* __restrict__ c
 
 __global__ void __launch_bounds__(kThreads) k_scatter(const int* __restrict__ key, const int* __restrict__ rank,
                                                       const int* __restrict__ start, int* __restrict__ perm,
-                                                      int n, uint32_t* err) {
+                                                      int n, uint32_t* err, unsigned long long* cell_pairs,
+                                                      unsigned long long* cell_pairs_map) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {  // this sort's same-cell pairs, out to the host
+        *cell_pairs_map = *cell_pairs;
+        *cell_pairs = 0;
+    }
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
         int t = start[key[s]] + rank[s];
         if (t >= 0 && t < n) perm[t] = s;
@@ -359,13 +373,14 @@ void launch_hash(const Buffers& b, const SceneDev& s0, bool batched, cudaStream_
 void launch_scan(const Buffers& b, cudaStream_t st) {
     const int ntiles = (b.ncell + kScanTile - 1) / kScanTile;
     int* tile_sum = reinterpret_cast<int*>(b.scan_state);  // ntiles 8-byte slots, used as ints
-    k_scan_tiles<<<ntiles, kScanThreads, 0, st>>>(b.count, b.ncell, tile_sum);
+    k_scan_tiles<<<ntiles, kScanThreads, 0, st>>>(b.count, b.ncell, tile_sum, b.cell_pairs);
     k_scan_apply<<<ntiles, kScanThreads, 0, st>>>(b.count, b.start, b.ncell, tile_sum);
 }
 
 void launch_scatter(const Buffers& b, cudaStream_t st) {
     if (b.n <= 0) return;
-    k_scatter<<<grid_for(b.n), kThreads, 0, st>>>(b.key, b.rank, b.start, b.perm, b.n, b.err);
+    k_scatter<<<grid_for(b.n), kThreads, 0, st>>>(b.key, b.rank, b.start, b.perm, b.n, b.err, b.cell_pairs,
+                                                  b.cell_pairs_map);
 }
 
 void launch_gather(const Buffers& b, cudaStream_t st) {

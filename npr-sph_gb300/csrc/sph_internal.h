@@ -77,12 +77,23 @@ struct Buffers {
     uint32_t* pmask = nullptr; // [kPairMaskWords][n]: the density pass's neighbour predicates for the force pass
     float4* rec = nullptr;     // [n][2]: (x, y, z, p), (vx, vy, vz, 1/rho) per sorted slot, written by the
                                // density pass (stencil 1) for the force pass's neighbour reads
+    unsigned long long* cell_pairs = nullptr;      // the running sort's sum over cells of count^2
+    unsigned long long* cell_pairs_map = nullptr;  // host-mapped: that of the last sort
 };
 
 // Stencil 1 (cells of edge h): the density pass stores, per particle and per neighbour-row
 // segment, which candidates passed r < h as two 32-bit masks (even and odd candidates), and the
 // force pass reads them instead of testing the candidates again.
 constexpr int kPairMaskWords = 2 * 9;
+
+// The neighbour records cost the density pass a fixed 48 bytes per particle (velocity read,
+// record write) and save the force pass a part of every neighbour read: they pay in dense fluid.
+// A step uses them when the last sort the host has seen found more than this many same-cell
+// pairs per particle (sum over cells of count^2 over n, self included). On the 1M dam break
+// pairs within h run at ~3.7 times that (8 on its starting 0.5h lattice, ~29 neighbours), and the
+// records pay down to ~10 pairs within h. The choice changes only the speed: both forms compute
+// the same interactions from the same values.
+constexpr double kRecordCellPairs = 2.6;
 
 // Launch shape chosen by the autotuner.
 struct LaunchCfg {
@@ -114,11 +125,13 @@ void launch_query_gather(const Buffers& b, const uint32_t* qids, int nq, const u
 // ---- launchers (sph_step.cu) ----
 // Kernel attributes (shared-memory opt-in); called once per process before any capture.
 void init_step_kernels();
-void launch_density(const Buffers& b, const SceneDev& s0, bool batched, const LaunchCfg& c,
+// rec (stencil 1): the density pass also writes the neighbour records and the force pass reads
+// them; a step's two passes take the same rec.
+void launch_density(const Buffers& b, const SceneDev& s0, bool batched, const LaunchCfg& c, bool rec,
                     cudaStream_t st);
-// With dig_cnt/dig_sum (per sorted slot; stencil 1 only), the force pass also reports the
-// neighbour set it used: count (self included) and digest sum mix64(id).
-void launch_force_integrate(const Buffers& b, const SceneDev& s0, bool batched, const LaunchCfg& c,
+// With dig_cnt/dig_sum (per sorted slot; stencil 1 only, without records), the force pass also
+// reports the neighbour set it used: count (self included) and digest sum mix64(id).
+void launch_force_integrate(const Buffers& b, const SceneDev& s0, bool batched, const LaunchCfg& c, bool rec,
                             cudaStream_t st, uint32_t* dig_cnt = nullptr, unsigned long long* dig_sum = nullptr);
 // Density (bit-identical to launch_density) plus, per particle, the kNbList nearest neighbours
 // j != i with r < h as sorted slots into nb[n][kNbList] (-1 padded) and their number in cnt

@@ -307,7 +307,7 @@ sph_status ensure_ctx_scratch(sph_mpnn* net, int n) {
 // Density at the current positions; the sorted copy becomes the state (so rhop lines up with it).
 sph_status refresh_density(sph_ctx* ctx) {
     engine::sort_state(ctx);
-    launch_density(ctx->b, ctx->s0, ctx->batched, ctx->cfg, ctx->stream);
+    launch_density(ctx->b, ctx->s0, ctx->batched, ctx->cfg, false, ctx->stream);
     const size_t n = (size_t)ctx->b.n;
     cudaMemcpyAsync(ctx->b.pos, ctx->b.pos_s, n * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->stream);
     cudaMemcpyAsync(ctx->b.vel, ctx->b.vel_s, n * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->stream);

@@ -270,7 +270,8 @@ constexpr size_t nb_smem() { return (size_t)4 * stage_cap<R, BLOCK>() * 4 + (siz
 static_assert(stage_cap<2, 256>() < 65536, "staged indices are 16-bit");
 static_assert(kNbCapNb >= kNbList + 2, "the nearest-kNbList pruning runs when two more entries could overflow");
 
-template <bool BATCHED, int R, int BLOCK>
+// REC (stencil 1): also the force pass's neighbour records (position, p, velocity, 1/rho).
+template <bool BATCHED, int R, int BLOCK, bool REC>
 __global__ void __launch_bounds__(BLOCK) k_density(const float4* __restrict__ pos_s, const float4* __restrict__ vel_s,
                                                    const int* __restrict__ start, SceneDev s0,
                                                    const SceneDev* __restrict__ scenes, int nscene,
@@ -280,6 +281,7 @@ __global__ void __launch_bounds__(BLOCK) k_density(const float4* __restrict__ po
     constexpr int kCap = stage_cap<R, BLOCK>();
     constexpr bool kMask = R == 1;  // pair masks for the force pass (kPairMaskWords words per particle)
     static_assert(!kMask || 2 * G::kSegPerRow == kPairMaskWords, "two mask words per segment");
+    static_assert(!REC || kMask, "neighbour records are written for stencil 1");
     __shared__ TileShared<R, BLOCK> T;
     extern __shared__ float4 dyn_d[];
     float* base = reinterpret_cast<float*>(dyn_d);
@@ -363,7 +365,7 @@ __global__ void __launch_bounds__(BLOCK) k_density(const float4* __restrict__ po
             const float pr = S.gas_k * (rho - S.rho0);
             const float prc = pr < 0.0f ? 0.0f : pr;  // GLSL max(x, 0): NaN stays NaN
             rhop[t] = make_float2(rho, prc);
-            if constexpr (kMask) {  // the force pass's neighbour record: one 32-byte load per neighbour
+            if constexpr (REC) {  // the force pass's neighbour record: one 32-byte load per neighbour
                 const float4 v = vel_s[t];
                 rec[2 * (size_t)t] = make_float4(p.x, p.y, p.z, prc);
                 rec[2 * (size_t)t + 1] = make_float4(v.x, v.y, v.z, __fdividef(1.0f, rho));
@@ -409,7 +411,9 @@ struct ForceAcc {
 
 // DIGEST (stencil 1): also the count (self included) and the digest sum mix64(id) of the
 // neighbours each particle interacted with, per sorted slot, as sph_neighbor_digest reports them.
-template <bool BATCHED, int R, int BLOCK, bool DIGEST = false>
+// REC (stencil 1): each neighbour is read as the density pass's 32-byte record, otherwise from
+// the state arrays; the interactions are the same either way.
+template <bool BATCHED, int R, int BLOCK, bool DIGEST, bool REC>
 __global__ void __launch_bounds__(BLOCK) k_force_integrate(const float4* __restrict__ pos_s, const float4* __restrict__ vel_s,
                                                            const float2* __restrict__ rhop, const int* __restrict__ start,
                                                            SceneDev s0, const SceneDev* __restrict__ scenes, int nscene,
@@ -424,6 +428,7 @@ __global__ void __launch_bounds__(BLOCK) k_force_integrate(const float4* __restr
     constexpr int kCap = stage_cap<R, BLOCK>();
     constexpr bool kMask = R == 1;  // the density pass's pair masks replace the candidate tests
     static_assert(!DIGEST || kMask, "the neighbour digest of the force pass is for stencil 1");
+    static_assert(!REC || kMask, "neighbour records are written for stencil 1");
     __shared__ TileShared<R, BLOCK> T;
     extern __shared__ float4 dyn_f[];
     float* base = reinterpret_cast<float*>(dyn_f);
@@ -454,13 +459,20 @@ __global__ void __launch_bounds__(BLOCK) k_force_integrate(const float4* __restr
             int cnt = 0;
             uint32_t dcount = 1;                                                 // DIGEST: self
             unsigned long long dsum = mix64((unsigned long long)id_of(v));
-            // Stencil 1: neighbours come from global memory, each as the density pass's 32-byte
-            // record (position, p_j, velocity, 1/rho_j) in one load. List entry e is candidate
+            // Stencil 1: neighbours come from global memory: the density pass's 32-byte record
+            // (position, p_j, velocity, 1/rho_j) in one load when this step has records, else
+            // position, velocity and (rho, p) from the state arrays. List entry e is candidate
             // e & 4095 of row segment e >> 12, whose first candidate is global slot seg_slot[segment].
             auto interact = [&](int g) {
                 float4 q, vj;
-                ld_record(rec + 2 * (size_t)g, q, vj);
-                acc.add(p.x - q.x, p.y - q.y, p.z - q.z, h, rp.y, v, q.w, vj.w, vj);
+                if constexpr (REC) {
+                    ld_record(rec + 2 * (size_t)g, q, vj);
+                    acc.add(p.x - q.x, p.y - q.y, p.z - q.z, h, rp.y, v, q.w, vj.w, vj);
+                } else {
+                    q = __ldg(pos_s + g);
+                    vj = __ldg(vel_s + g);
+                    acc.add(p.x - q.x, p.y - q.y, p.z - q.z, h, rp.y, v, __ldg(rhop + g), vj);
+                }
                 if constexpr (DIGEST) {
                     ++dcount;
                     dsum += mix64((unsigned long long)id_of(__ldg(vel_s + g)));
@@ -768,30 +780,42 @@ int grid_size(K, int block, size_t, int n) {
 }
 
 template <bool B, int R, int BLOCK>
-void density_impl(const Buffers& b, const SceneDev& s0, cudaStream_t st) {
-    auto k = k_density<B, R, BLOCK>;
+void density_impl(const Buffers& b, const SceneDev& s0, bool rec, cudaStream_t st) {
     constexpr size_t sm = density_smem<R, BLOCK>();
-    k<<<grid_size(k, BLOCK, sm, b.n), BLOCK, sm, st>>>(b.pos_s, b.vel_s, b.start, s0, b.scenes, b.nscene, b.rhop,
-                                                       b.pmask, b.rec, b.n, b.tile_stats);
+    auto launch = [&](auto k) {
+        k<<<grid_size(k, BLOCK, sm, b.n), BLOCK, sm, st>>>(b.pos_s, b.vel_s, b.start, s0, b.scenes, b.nscene, b.rhop,
+                                                           b.pmask, b.rec, b.n, b.tile_stats);
+    };
+    if constexpr (R == 1) {
+        if (rec) {
+            launch(k_density<B, R, BLOCK, true>);
+            return;
+        }
+    }
+    launch(k_density<B, R, BLOCK, false>);
 }
 
 template <bool B, int R, int BLOCK>
-void force_impl(const Buffers& b, const SceneDev& s0, float4* force_out, uint32_t* dig_cnt,
+void force_impl(const Buffers& b, const SceneDev& s0, bool rec, float4* force_out, uint32_t* dig_cnt,
                 unsigned long long* dig_sum, cudaStream_t st) {
     constexpr size_t sm = force_smem<R, BLOCK>();
     auto launch = [&](auto k) {
         k<<<grid_size(k, BLOCK, sm, b.n), BLOCK, sm, st>>>(b.pos_s, b.vel_s, b.rhop, b.start, s0, b.scenes, b.nscene,
                                                            b.pos, b.vel, force_out, s0.sdf ? nullptr : b.key, b.rank,
-                                                           b.count, b.pmask, b.rec, b.n, b.tile_stats, dig_cnt,
-                                                           dig_sum);
+                                                           b.count, b.pmask, b.rec, b.n, b.tile_stats,
+                                                           dig_cnt, dig_sum);
     };
     if constexpr (R == 1) {
-        if (dig_cnt) {
-            launch(k_force_integrate<B, R, BLOCK, true>);
+        if (dig_cnt) {  // the digest pass runs without records
+            launch(k_force_integrate<B, R, BLOCK, true, false>);
+            return;
+        }
+        if (rec) {
+            launch(k_force_integrate<B, R, BLOCK, false, true>);
             return;
         }
     }
-    launch(k_force_integrate<B, R, BLOCK>);
+    launch(k_force_integrate<B, R, BLOCK, false, false>);
 }
 
 // The static obstacle's rule (sph_set_obstacle) on the integrated state, then the cell hash of
@@ -829,13 +853,18 @@ void density_nb_impl(const Buffers& b, const SceneDev& s0, int* nb, int* cnt, cu
 
 template <bool B, int R, int BLOCK>
 void set_attrs() {
-    cudaFuncSetAttribute(k_density<B, R, BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(k_density<B, R, BLOCK, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)density_smem<R, BLOCK>());
-    cudaFuncSetAttribute(k_force_integrate<B, R, BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(k_force_integrate<B, R, BLOCK, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)force_smem<R, BLOCK>());
-    if constexpr (R == 1)
-        cudaFuncSetAttribute(k_force_integrate<B, R, BLOCK, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if constexpr (R == 1) {
+        cudaFuncSetAttribute(k_density<B, R, BLOCK, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)density_smem<R, BLOCK>());
+        cudaFuncSetAttribute(k_force_integrate<B, R, BLOCK, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)force_smem<R, BLOCK>());
+        cudaFuncSetAttribute(k_force_integrate<B, R, BLOCK, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)force_smem<R, BLOCK>());
+    }
     cudaFuncSetAttribute(k_density_nb<B, R, BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)nb_smem<R, BLOCK>());
 }
@@ -864,24 +893,24 @@ void init_step_kernels() {
     set_attrs<true, 2, 256>();
 }
 
-void launch_density(const Buffers& b, const SceneDev& s0, bool batched, const LaunchCfg& c, cudaStream_t st) {
+void launch_density(const Buffers& b, const SceneDev& s0, bool batched, const LaunchCfg& c, bool rec, cudaStream_t st) {
     if (b.n <= 0) return;
     if (batched)
-        dispatch(c.block, c.stencil, [&](auto R, auto BL) { density_impl<true, R.value, BL.value>(b, s0, st); });
+        dispatch(c.block, c.stencil, [&](auto R, auto BL) { density_impl<true, R.value, BL.value>(b, s0, rec, st); });
     else
-        dispatch(c.block, c.stencil, [&](auto R, auto BL) { density_impl<false, R.value, BL.value>(b, s0, st); });
+        dispatch(c.block, c.stencil, [&](auto R, auto BL) { density_impl<false, R.value, BL.value>(b, s0, rec, st); });
 }
 
-void launch_force_integrate(const Buffers& b, const SceneDev& s0, bool batched, const LaunchCfg& c,
+void launch_force_integrate(const Buffers& b, const SceneDev& s0, bool batched, const LaunchCfg& c, bool rec,
                             cudaStream_t st, uint32_t* dig_cnt, unsigned long long* dig_sum) {
     if (b.n <= 0) return;
     float4* f = s0.keep_force ? b.force_s : nullptr;
     if (batched)
         dispatch(c.block, c.stencil,
-                 [&](auto R, auto BL) { force_impl<true, R.value, BL.value>(b, s0, f, dig_cnt, dig_sum, st); });
+                 [&](auto R, auto BL) { force_impl<true, R.value, BL.value>(b, s0, rec, f, dig_cnt, dig_sum, st); });
     else
         dispatch(c.block, c.stencil,
-                 [&](auto R, auto BL) { force_impl<false, R.value, BL.value>(b, s0, f, dig_cnt, dig_sum, st); });
+                 [&](auto R, auto BL) { force_impl<false, R.value, BL.value>(b, s0, rec, f, dig_cnt, dig_sum, st); });
     if (s0.sdf) {
         const int blocks = std::min((b.n + 255) / 256, device_sm_count() * 8);
         if (batched)

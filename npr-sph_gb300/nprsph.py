@@ -122,6 +122,7 @@ _SIGS = {
     "sph_get_launch": (C.c_int32, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "sph_autotune": (C.c_int32, [_P, C.c_int32, C.POINTER(C.c_float)]),
     "sph_tile_stats": (C.c_int32, [_P, C.POINTER(C.c_uint32)]),
+    "sph_record_stats": (C.c_int32, [_P, C.POINTER(C.c_uint64)]),
     "sph_reduce_aos_noalloc": (C.c_int32, [_P, C.c_uint32, C.POINTER(Params), _P, _P]),
     "sph_mpnn_num_params": (C.c_uint32, []),
     "sph_mpnn_create": (C.c_int32, [C.c_uint32, _P, C.POINTER(_P)]),
@@ -530,6 +531,14 @@ class Sim:
         out = (C.c_uint64 * 2)()
         _check(lib.sph_pair_counts(self._ctx, out), self._ctx)
         return int(out[0]), int(out[1])
+
+    def record_stats(self) -> tuple[int, int, int]:
+        """(steps with, steps without) the force pass's 32-byte neighbour records since creation,
+        and the same-cell pairs (sum of count^2 over the cells) the last sort seen by the host
+        found (sph_record_stats)."""
+        a = (C.c_uint64 * 3)()
+        _check(lib.sph_record_stats(self._ctx, a), self._ctx)
+        return int(a[0]), int(a[1]), int(a[2])
 
     def tile_stats(self) -> tuple[int, int]:
         """(density, force) chunks that fell back to the global-memory path since creation."""
