@@ -619,6 +619,7 @@ def run_ours(args) -> None:
     sim.synchronize()
 
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    rec0 = sim.record_stats()
     barrier(world)
     torch.cuda.synchronize()
     with ClockSampler(dev.index) as clk:
@@ -636,6 +637,7 @@ def run_ours(args) -> None:
     total_s = max_over_ranks(local_s, world)
     diag = sim.reduce()
     fallback = sim.tile_stats()
+    rec1 = sim.record_stats()
 
     # Per-pass device times over the same trajectory (events between passes, eager launches).
     sim.upload(sc.particles)
@@ -710,7 +712,9 @@ def run_ours(args) -> None:
                    "l2": "flushed between steps (256 MiB write outside the timed events)",
                    "launch": {"threads_per_block": blk, "stencil": sten}, "parallelism": f"replicas x{world}",
                    "global_path_chunks": {"density": fallback[0], "force": fallback[1],
-                                          "of": (args.warmup + args.steps) * ((n + blk - 1) // blk)}},
+                                          "of": (args.warmup + args.steps) * ((n + blk - 1) // blk)},
+                   "neighbour_records": {"timed_steps_with": rec1[0] - rec0[0],
+                                         "timed_steps_without": rec1[1] - rec0[1]}},
         "roofline": roofline,
         "passes_ms": {"sort": pass_avg[0], "density": pass_avg[1], "force_integrate": pass_avg[2]},
         "cpu_baseline": cpu,
