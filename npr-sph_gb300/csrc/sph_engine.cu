@@ -266,6 +266,10 @@ sph_status run_steps(sph_ctx* ctx, int n) {
             ctx->need_hash = false;
         }
         for (int s = 0; s < n; ++s) {
+            // A fresh context has no same-cell count yet: the first step publishes one before
+            // the next is launched (one synchronisation per context).
+            const bool first = s == 0 && ctx->cfg.stencil == 1 && ctx->pair_host &&
+                               *reinterpret_cast<const volatile unsigned long long*>(ctx->pair_host) == 0;
             const int m = record_mode(ctx) ? 1 : 0;
             if (!ctx->gexec[m]) {  // both forms at once: a later switch costs no capture
                 for (int k = 0; k < (ctx->cfg.stencil == 1 ? 2 : 1); ++k) {
@@ -276,6 +280,7 @@ sph_status run_steps(sph_ctx* ctx, int n) {
             }
             CK(cudaGraphLaunch(ctx->gexec[m], ctx->stream));
             ++ctx->record_steps[1 - m];
+            if (first) CK(cudaStreamSynchronize(ctx->stream));
         }
     }
     CK(cudaGetLastError());
@@ -320,13 +325,12 @@ sph_status create_impl(const sph_params* params, const uint32_t* counts, uint32_
         dalloc(&b.rhop, n) || dalloc(&b.force_s, n) || dalloc(&b.force_up, n) || dalloc(&b.aux, n) ||
         dalloc(&b.key, n) || dalloc(&b.rank, n) || dalloc(&b.perm, n) || dalloc(&b.slot_of_id, n) ||
         dalloc(&b.err, 1) || dalloc(&b.scenes, nscene) || dalloc(&b.tile_stats, 2) ||
-        dalloc(&b.pmask, n * kPairMaskWords) || dalloc(&b.rec, 2 * n) || dalloc(&b.cell_pairs, 1) ||
+        dalloc(&b.pmask, n * kPairMaskWords) || dalloc(&b.rec, 2 * n) ||
         dalloc(&b.partials, reduce_partials_doubles((int)nscene)) ||
         dalloc(&ctx->diag_dev, (size_t)nscene * kDiagFields) || dalloc(&ctx->scene_first_dev, nscene + 1))
         return bail(SPH_ERR_OUT_OF_MEMORY);
     if (cudaMemsetAsync(b.err, 0, sizeof(uint32_t), ctx->stream) ||
-        cudaMemsetAsync(b.tile_stats, 0, sizeof(uint32_t) * 2, ctx->stream) ||
-        cudaMemsetAsync(b.cell_pairs, 0, sizeof(unsigned long long), ctx->stream))
+        cudaMemsetAsync(b.tile_stats, 0, sizeof(uint32_t) * 2, ctx->stream))
         return bail(SPH_ERR_CUDA);
     if (cudaHostAlloc(&ctx->pair_host, sizeof(unsigned long long), cudaHostAllocMapped) != cudaSuccess)
         return bail(SPH_ERR_OUT_OF_MEMORY);
@@ -500,7 +504,7 @@ sph_status sph_destroy(sph_ctx* ctx) {
     Buffers& b = ctx->b;
     void* ptrs[] = {b.pos, b.vel, b.pos_s, b.vel_s, b.rhop, b.force_s, b.force_up, b.aux, b.aos, b.key, b.rank,
                     b.perm, b.count, b.start, b.scan_state, b.slot_of_id, b.err, b.partials,
-                    b.scenes, b.tile_stats, b.pmask, b.rec, b.cell_pairs, ctx->diag_dev, ctx->scene_first_dev, ctx->q_ids, ctx->q_cnt, ctx->q_dig,
+                    b.scenes, b.tile_stats, b.pmask, b.rec, ctx->diag_dev, ctx->scene_first_dev, ctx->q_ids, ctx->q_cnt, ctx->q_dig,
                     ctx->fd_cnt, ctx->fd_sum, ctx->pc_dev,
                     ctx->render_buf, ctx->sdf_dev};
     for (void* p : ptrs)

@@ -79,35 +79,62 @@ __device__ __forceinline__ int block_sum(int x, int* s_warp) {
     return t;
 }
 
-// Also adds the tile's same-cell pairs, sum of count^2 (self included), to *cell_pairs.
+// Also the tile's same-cell pairs, the sum of count^2 over its cells (self included), into
+// tile_sq[tile].
 __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const int* __restrict__ count, int ncell,
                                                              int* __restrict__ tile_sum,
-                                                             unsigned long long* __restrict__ cell_pairs) {
+                                                             unsigned* __restrict__ tile_sq) {
     __shared__ int s_warp[kScanThreads / 32];
+    __shared__ unsigned s_sq[kScanThreads / 32];
     const long long base = (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanItems;
     int v[kScanItems];
     load_tile_counts(count, base, ncell, v);
     int sum = 0;
-    unsigned long long sq = 0;
+    unsigned sq = 0;  // a cell counts at most 1024^2: a tile's 2048 cells stay below 2^31
 #pragma unroll
     for (int k = 0; k < kScanItems; ++k) {
         sum += v[k];
-        sq += (unsigned long long)((long long)v[k] * v[k]);
+        const unsigned c = (unsigned)min(max(v[k], 0), 1024);
+        sq += c * c;
     }
-    const int total = block_sum(sum, s_warp);
-    if (threadIdx.x == 0) tile_sum[blockIdx.x] = total;
+    sq = __reduce_add_sync(0xffffffffu, sq);
+    if ((threadIdx.x & 31) == 0) s_sq[threadIdx.x >> 5] = sq;
+    const int total = block_sum(sum, s_warp);  // its barrier also publishes s_sq
+    if (threadIdx.x == 0) {
+        unsigned t = 0;
 #pragma unroll
-    for (int o = 16; o >= 1; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
-    if ((threadIdx.x & 31) == 0 && sq) atomicAdd(cell_pairs, sq);
+        for (int w = 0; w < kScanThreads / 32; ++w) t += s_sq[w];
+        tile_sum[blockIdx.x] = total;
+        tile_sq[blockIdx.x] = t;
+    }
 }
 
+// The last tile's block also adds up the tiles' same-cell pairs and writes the sum to host-mapped
+// memory (*cell_pairs_map: the host's choice of the neighbour-record form of the next steps).
 __global__ void __launch_bounds__(kScanThreads) k_scan_apply(int* __restrict__ count, int* __restrict__ start, int ncell,
-                                                             const int* __restrict__ tile_sum) {
+                                                             const int* __restrict__ tile_sum,
+                                                             const unsigned* __restrict__ tile_sq,
+                                                             unsigned long long* __restrict__ cell_pairs_map) {
     __shared__ int s_warp[kScanThreads / 32];
+    __shared__ unsigned long long s_sq[kScanThreads / 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int tile = blockIdx.x;
     int before = 0;
     for (int t = threadIdx.x; t < tile; t += kScanThreads) before += tile_sum[t];
+    if (tile == (int)gridDim.x - 1) {  // uniform per block
+        unsigned long long sq = 0;
+        for (int t = threadIdx.x; t < (int)gridDim.x; t += kScanThreads) sq += tile_sq[t];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
+        if (lane == 0) s_sq[warp] = sq;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long t = 0;
+#pragma unroll
+            for (int w = 0; w < kScanThreads / 32; ++w) t += s_sq[w];
+            *cell_pairs_map = t;
+        }
+    }
     const int prefix = block_sum(before, s_warp);
     const long long base = (long long)tile * kScanTile + (long long)threadIdx.x * kScanItems;
     int v[kScanItems];
@@ -148,12 +175,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_apply(int* __restrict__ c
 
 __global__ void __launch_bounds__(kThreads) k_scatter(const int* __restrict__ key, const int* __restrict__ rank,
                                                       const int* __restrict__ start, int* __restrict__ perm,
-                                                      int n, uint32_t* err, unsigned long long* cell_pairs,
-                                                      unsigned long long* cell_pairs_map) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) {  // this sort's same-cell pairs, out to the host
-        *cell_pairs_map = *cell_pairs;
-        *cell_pairs = 0;
-    }
+                                                      int n, uint32_t* err) {
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
         int t = start[key[s]] + rank[s];
         if (t >= 0 && t < n) perm[t] = s;
@@ -372,15 +394,16 @@ void launch_hash(const Buffers& b, const SceneDev& s0, bool batched, cudaStream_
 
 void launch_scan(const Buffers& b, cudaStream_t st) {
     const int ntiles = (b.ncell + kScanTile - 1) / kScanTile;
-    int* tile_sum = reinterpret_cast<int*>(b.scan_state);  // ntiles 8-byte slots, used as ints
-    k_scan_tiles<<<ntiles, kScanThreads, 0, st>>>(b.count, b.ncell, tile_sum, b.cell_pairs);
-    k_scan_apply<<<ntiles, kScanThreads, 0, st>>>(b.count, b.start, b.ncell, tile_sum);
+    // ntiles 8-byte slots: the tiles' particle counts (int), then their same-cell pairs (unsigned)
+    int* tile_sum = reinterpret_cast<int*>(b.scan_state);
+    unsigned* tile_sq = reinterpret_cast<unsigned*>(b.scan_state) + ntiles;
+    k_scan_tiles<<<ntiles, kScanThreads, 0, st>>>(b.count, b.ncell, tile_sum, tile_sq);
+    k_scan_apply<<<ntiles, kScanThreads, 0, st>>>(b.count, b.start, b.ncell, tile_sum, tile_sq, b.cell_pairs_map);
 }
 
 void launch_scatter(const Buffers& b, cudaStream_t st) {
     if (b.n <= 0) return;
-    k_scatter<<<grid_for(b.n), kThreads, 0, st>>>(b.key, b.rank, b.start, b.perm, b.n, b.err, b.cell_pairs,
-                                                  b.cell_pairs_map);
+    k_scatter<<<grid_for(b.n), kThreads, 0, st>>>(b.key, b.rank, b.start, b.perm, b.n, b.err);
 }
 
 void launch_gather(const Buffers& b, cudaStream_t st) {

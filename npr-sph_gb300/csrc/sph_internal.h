@@ -77,8 +77,7 @@ struct Buffers {
     uint32_t* pmask = nullptr; // [kPairMaskWords][n]: the density pass's neighbour predicates for the force pass
     float4* rec = nullptr;     // [n][2]: (x, y, z, p), (vx, vy, vz, 1/rho) per sorted slot, written by the
                                // density pass (stencil 1) for the force pass's neighbour reads
-    unsigned long long* cell_pairs = nullptr;      // the running sort's sum over cells of count^2
-    unsigned long long* cell_pairs_map = nullptr;  // host-mapped: that of the last sort
+    unsigned long long* cell_pairs_map = nullptr;  // host-mapped: the last sort's sum over cells of count^2
 };
 
 // Stencil 1 (cells of edge h): the density pass stores, per particle and per neighbour-row

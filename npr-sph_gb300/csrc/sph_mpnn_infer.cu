@@ -35,6 +35,10 @@ constexpr int kTile = 16;         // particles per warp tile
 constexpr int kLd1 = 88;          // X1 tile row stride (80 used), bf16
 constexpr int kLd2 = 152;         // X2 tile row stride (144 used), bf16
 constexpr int kK1 = 80, kK2 = 144; // padded K of the two node layers (bias column at W+FN / 128)
+// Row stride (ints) of a warp's staged neighbour lists: 4 banks apart per particle, so the edge
+// build (lanes of 8 particles x 4 slots) and the P_j index reads (lanes of 4 particles) hit 32
+// and 4 distinct banks instead of one.
+constexpr int kNbRow = K + 4;
 constexpr int kBias1 = W + FN;     // bias column of the round-1 node layer
 static_assert(kBias1 < kK1, "round-1 node input does not fit its padded K");
 static_assert(2 * W + 16 == kK2, "round-2 node input: [M2 H1], bias column, padding");
@@ -168,7 +172,7 @@ __device__ __forceinline__ void edge_tile(const EdgeFrags& A, int base, int n, c
                 const int e = e0 + fs;
                 uint4 w0 = make_uint4(0u, 0u, 0u, 0u), w1 = w0;
                 if (e < cb) {
-                    const int j = nb_s[pb * K + e];
+                    const int j = nb_s[pb * kNbRow + e];
                     edge_features(pi, vi, pos[j], vel[j], ih, ic, w0, w1);
                 }
                 uint4* dst = reinterpret_cast<uint4*>(E + (fs * 8 + fp) * kFRow);
@@ -186,8 +190,8 @@ __device__ __forceinline__ void edge_tile(const EdgeFrags& A, int base, int n, c
                 if constexpr (ROUND2) {
                     // accumulators start at P_j of the two column particles 2 tq, 2 tq + 1
                     uint4 p0 = make_uint4(0, 0, 0, 0), p1 = make_uint4(0, 0, 0, 0);
-                    if (e < c0) p0 = Pperm[(size_t)nb_s[(grp * 8 + 2 * tq) * K + e] * 8 + g];
-                    if (e < c1) p1 = Pperm[(size_t)nb_s[(grp * 8 + 2 * tq + 1) * K + e] * 8 + g];
+                    if (e < c0) p0 = Pperm[(size_t)nb_s[(grp * 8 + 2 * tq) * kNbRow + e] * 8 + g];
+                    if (e < c1) p1 = Pperm[(size_t)nb_s[(grp * 8 + 2 * tq + 1) * kNbRow + e] * 8 + g];
                     const uint32_t q0[4] = {p0.x, p0.y, p0.z, p0.w}, q1[4] = {p1.x, p1.y, p1.z, p1.w};
 #pragma unroll
                     for (int mt = 0; mt < 4; ++mt) {  // word mt holds features (16 mt + g, 16 mt + g + 8)
@@ -229,7 +233,7 @@ __device__ __forceinline__ void stage_tile_lists(int base, int n, const int* __r
 #pragma unroll 4
     for (int q = lane; q < kTile * K; q += 32) {
         const int i = base + q / K;
-        nb_s[q] = i < n ? nb[(size_t)base * K + q] : 0;
+        nb_s[(q / K) * kNbRow + q % K] = i < n ? nb[(size_t)base * K + q] : 0;
     }
     if (lane < kTile) {
         const int i = base + lane;
@@ -287,7 +291,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_infer_r1(const float4* __restri
                                                       __nv_bfloat16* __restrict__ H1out, uint16_t* __restrict__ Pperm) {
     __shared__ __align__(16) __nv_bfloat16 xs[kWarps][kTile * kLd1];
     __shared__ __align__(16) __nv_bfloat16 es[kWarps][kFBuf];
-    __shared__ int nbs[kWarps][kTile * K];
+    __shared__ int nbs[kWarps][kTile * kNbRow];
     __shared__ int cns[kWarps][kTile];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
     __nv_bfloat16* X = xs[warp];
@@ -377,7 +381,7 @@ __global__ void __launch_bounds__(kThreads, 6) k_infer_r2(const float4* __restri
                                                       int* __restrict__ rank_out, int* __restrict__ count,
                                                       int integrate) {
     __shared__ __align__(16) __nv_bfloat16 xs[kWarps][kTile * kLd2];
-    __shared__ int nbs[kWarps][kTile * K];
+    __shared__ int nbs[kWarps][kTile * kNbRow];
     __shared__ int cns[kWarps][kTile];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
     __nv_bfloat16* X = xs[warp];
