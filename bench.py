@@ -581,7 +581,7 @@ def roofline_block(n, steps, pass_avg, step_s, cand, pairs, hbm, src, peaks, dev
         "frac": d["fp32_frac"] if bound == "fp32" else d["hbm_frac"],
         "traffic": traffic,
         "traffic_source": f"ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_{kern} launch at the "
-                          f"dense start, from the capture summarised in {PROFILE} (not measured in this run)",
+                          f"dense start, cold L2, from the capture summarised in {PROFILE} (not measured in this run)",
         "hbm_peak": hbm, "hbm_peak_source": f"{src} hbm_gbs",
         "fp32_peak": fp32_peak, "fp32_peak_source": f"{sms} SMs x {FP32_LANES_PER_SM} lanes x 2 flop x {mhz:.0f} MHz",
         "passes": per,
