@@ -1,7 +1,8 @@
 """Train the learned macro-step network on trajectories the GPU SPH step generates.
 
     python npr-sph_gb300/train_mpnn.py [--scenes 200] [--particles 65536] [--frames 24]
-                                       [--gap 8] [--steps 60000] [--out npr-sph_gb300/weights/mpnn_w64.npy]
+                                       [--gap 8] [--steps 60000] [--rollout-schedule 8:7:60000,...]
+                                       [--out npr-sph_gb300/weights/mpnn_w64.npy]
 
 Training data: `scenes` seeded runs of `particles` particles each, advanced together in one
 batched context with the literal mass and smoothing length and g = -9.81. Per run the stiffness k
@@ -16,6 +17,14 @@ density of every particle, and as targets the mean accelerations of the next 4 p
 backward kernels), one frame per step, with a cosine-decayed learning rate. By default the
 node layers and all weight gradients run as BF16 GEMMs on the tensor cores (FP32 accumulation,
 FP32 master weights); --precision 0 runs every layer in FP32.
+
+Rollout rounds (--rollout-schedule) then fine-tune the network on states it produces itself:
+a macro-step judged after a run of learned macro-steps starts from such a state, and a network
+trained on plain-SPH states alone errs more there. Each round re-records the plain frames and,
+per run, `frames` rollouts: the run's initial state, plain SPH for 8-192 steps, 1-`macro`
+unjudged learned macro-steps of the current network (BF16 inference), and a frame recorded
+there, its targets again from 4 plain steps. Adam then runs `steps` steps over both kinds of
+frames from the current weights, the learning rate cosine-decayed from --rollout-lr.
 """
 from __future__ import annotations
 
@@ -77,6 +86,9 @@ def main() -> None:
     ap.add_argument("--seed", type=int, default=4)
     ap.add_argument("--precision", type=int, default=1, choices=[0, 1],
                     help="1: node layers and weight gradients as BF16 tensor-core (tcgen05) GEMMs; 0: FP32")
+    ap.add_argument("--rollout-schedule", default="8:7:60000,16:8:60000,16:8:60000,24:24:120000",
+                    help="rollout rounds frames:macro:steps, comma-separated ('' for none)")
+    ap.add_argument("--rollout-lr", type=float, default=3e-4)
     ap.add_argument("--out", type=Path, default=DEFAULT_OUT)
     args = ap.parse_args()
 
@@ -93,28 +105,70 @@ def main() -> None:
                 sim.step(args.gap)
         sim.synchronize()
     t_rec = time.time() - t0
-    losses = []
-    chunk = 500
-    done = 0
     t1 = time.time()
-    while done < args.steps:
-        k = min(chunk, args.steps - done)
-        lr = args.lr * (0.01 + 0.99 * 0.5 * (1 + math.cos(math.pi * done / args.steps)))
-        losses.append(net.train(k, lr=lr, seed=args.seed * 1000003 + done))
-        done += k
+    losses = [train_steps(net, args.steps, args.lr, args.seed * 1000003)]
     t_train = time.time() - t1
+    loss = np.concatenate(losses)
+    rounds = []
+    for r, spec in enumerate(x for x in args.rollout_schedule.split(",") if x):
+        frames, macro, steps = (int(v) for v in spec.split(":"))
+        t2 = time.time()
+        net.clear_frames()
+        with S.Sim(plist, counts=counts) as sim:
+            sim.upload(parts)
+            for f in range(args.frames):
+                n_plain = net.record(sim, 1)
+                if f + 1 < args.frames:
+                    sim.step(args.gap)
+            sim.synchronize()
+        n_roll = rollout_frames(net, plist, counts, parts, frames, macro, args.seed + 99 + r)
+        t3 = time.time()
+        rl = train_steps(net, steps, args.rollout_lr, args.seed * 1000003 + 77 + 1000 * r)
+        rounds.append({"rollout_frames_per_run": frames, "max_macro_steps": macro, "adam_steps": steps,
+                       "frames": {"plain": int(n_plain), "rollout": int(n_roll - n_plain)},
+                       "loss_first_500": float(rl[:500].mean()), "loss_last_500": float(rl[-500:].mean()),
+                       "record_s": t3 - t2, "train_s": time.time() - t3})
+        print(json.dumps({"rollout_round": r, **rounds[-1]}), flush=True)
     params = net.get_params()
     net.close()
     args.out.parent.mkdir(parents=True, exist_ok=True)
     np.save(args.out, params)
-    loss = np.concatenate(losses)
     meta = {"scenes": args.scenes, "particles": args.particles, "frames_per_run": args.frames, "gap": args.gap,
             "frames": int(total), "adam_steps": args.steps, "lr": args.lr, "seed": args.seed,
             "train_precision": "bf16 tcgen05 GEMMs" if args.precision == 1 else "fp32",
             "loss_first_500": float(loss[:500].mean()), "loss_last_500": float(loss[-500:].mean()),
-            "record_s": t_rec, "train_s": t_train}
+            "record_s": t_rec, "train_s": t_train, "rollout_lr": args.rollout_lr, "rollout_rounds": rounds}
     args.out.with_suffix(".json").write_text(json.dumps(meta, indent=1))
     print(json.dumps(meta))
+
+
+def train_steps(net, steps: int, lr0: float, seed: int) -> np.ndarray:
+    """`steps` Adam steps over the recorded frames, the learning rate cosine-decayed from lr0 to lr0/100."""
+    losses, done, chunk = [], 0, 500
+    while done < steps:
+        k = min(chunk, steps - done)
+        lr = lr0 * (0.01 + 0.99 * 0.5 * (1 + math.cos(math.pi * done / steps)))
+        losses.append(net.train(k, lr=lr, seed=seed + done))
+        done += k
+    return np.concatenate(losses)
+
+
+def rollout_frames(net, plist, counts, parts, per_run: int, macro: int, seed: int) -> int:
+    """Record per_run frames of every run at states the network reached itself: from the run's
+    initial state, 8-192 plain steps, then 1-macro unjudged learned macro-steps. Returns the
+    frames recorded in total."""
+    rng = np.random.default_rng(seed)
+    offs = [0] + [int(x) for x in np.cumsum(counts)]
+    total = 0
+    for i, p in enumerate(plist):
+        with S.Sim(p, n_max=int(counts[i])) as sim:
+            for _ in range(per_run):
+                sim.upload(parts[offs[i]:offs[i + 1]])
+                sim.step(int(8 * rng.integers(1, 25)))
+                sim.learned_step(net, int(rng.integers(1, macro + 1)), 0, 1e30, 1e30)
+                total = net.record(sim, 1)
+            sim.synchronize()
+    return total
 
 
 def init_params(seed: int) -> np.ndarray:
