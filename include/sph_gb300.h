@@ -223,6 +223,10 @@ sph_status sph_tile_stats(sph_ctx* ctx, uint32_t out[2]);
  * the same interactions from the same values, so the choice changes only the
  * speed. */
 sph_status sph_record_stats(const sph_ctx* ctx, uint64_t out[3]);
+/* The choice above: SPH_RECORDS_AUTO (default), SPH_RECORDS_ALWAYS or
+ * SPH_RECORDS_NEVER (stencil 1; stencil 2 never uses records). */
+enum { SPH_RECORDS_AUTO = 0, SPH_RECORDS_ALWAYS = 1, SPH_RECORDS_NEVER = 2 };
+sph_status sph_set_record_mode(sph_ctx* ctx, int32_t mode);
 
 /* ---- learned macro-step (new; no reference counterpart) -----------------
  * A message-passing network (2 rounds over the <= 32 nearest neighbours,

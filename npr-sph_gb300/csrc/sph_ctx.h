@@ -27,6 +27,7 @@ struct sph_ctx {
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};
     unsigned long long* pair_host = nullptr;  // mapped host word: same-cell pairs of the last sort
     uint64_t record_steps[2] = {0, 0};        // steps run with [0] / without [1] neighbour records
+    int record_mode = SPH_RECORDS_AUTO;       // sph_set_record_mode
     bool have_state = false, need_hash = true, stepped = false;
     uint64_t steps = 0;
     // judge state of the learned macro-step, kept across sph_learned_step calls (cleared by uploads)

@@ -196,7 +196,9 @@ void enqueue_sort(sph_ctx* ctx) {
 // that has written them to host-mapped memory (the host may be a few steps ahead of the device).
 // Only the speed depends on the answer.
 bool record_mode(const sph_ctx* ctx) {
-    if (ctx->cfg.stencil != 1 || !ctx->pair_host || ctx->b.n <= 0) return false;
+    if (ctx->cfg.stencil != 1 || ctx->record_mode == SPH_RECORDS_NEVER) return false;
+    if (ctx->record_mode == SPH_RECORDS_ALWAYS) return true;
+    if (!ctx->pair_host || ctx->b.n <= 0) return false;
     const unsigned long long pairs = *reinterpret_cast<const volatile unsigned long long*>(ctx->pair_host);
     return (double)pairs > kRecordCellPairs * (double)ctx->b.n;
 }
@@ -787,6 +789,14 @@ sph_status sph_record_stats(const sph_ctx* ctx, uint64_t out[3]) {
     out[0] = ctx->record_steps[0];
     out[1] = ctx->record_steps[1];
     out[2] = ctx->pair_host ? *reinterpret_cast<const volatile unsigned long long*>(ctx->pair_host) : 0;
+    return SPH_OK;
+}
+
+sph_status sph_set_record_mode(sph_ctx* ctx, int32_t mode) {
+    if (!ctx) return SPH_ERR_INVALID_ARG;
+    if (mode != SPH_RECORDS_AUTO && mode != SPH_RECORDS_ALWAYS && mode != SPH_RECORDS_NEVER)
+        return fail(ctx, SPH_ERR_INVALID_ARG, "record mode: 0 auto, 1 always, 2 never");
+    ctx->record_mode = mode;
     return SPH_OK;
 }
 

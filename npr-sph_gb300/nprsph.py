@@ -28,6 +28,7 @@ assert PARTICLE_DTYPE.itemsize == 64
 
 FLAG_KEEP_FORCE = 0x1
 JUDGE_MEAN_DENSITY, JUDGE_PARTICLE_DENSITY = 0, 1
+RECORDS_AUTO, RECORDS_ALWAYS, RECORDS_NEVER = 0, 1, 2
 
 OK, ERR_INVALID_ARG, ERR_CUDA, ERR_OUT_OF_MEMORY, ERR_CAPACITY, ERR_NOT_READY, ERR_DEVICE, ERR_UNSUPPORTED = (
     0, -1, -2, -3, -4, -5, -6, -7)
@@ -123,6 +124,7 @@ _SIGS = {
     "sph_autotune": (C.c_int32, [_P, C.c_int32, C.POINTER(C.c_float)]),
     "sph_tile_stats": (C.c_int32, [_P, C.POINTER(C.c_uint32)]),
     "sph_record_stats": (C.c_int32, [_P, C.POINTER(C.c_uint64)]),
+    "sph_set_record_mode": (C.c_int32, [_P, C.c_int32]),
     "sph_reduce_aos_noalloc": (C.c_int32, [_P, C.c_uint32, C.POINTER(Params), _P, _P]),
     "sph_mpnn_num_params": (C.c_uint32, []),
     "sph_mpnn_create": (C.c_int32, [C.c_uint32, _P, C.POINTER(_P)]),
@@ -539,6 +541,10 @@ class Sim:
         a = (C.c_uint64 * 3)()
         _check(lib.sph_record_stats(self._ctx, a), self._ctx)
         return int(a[0]), int(a[1]), int(a[2])
+
+    def set_record_mode(self, mode: int) -> None:
+        """0: neighbour records chosen per step (default), 1: always, 2: never (sph_set_record_mode)."""
+        _check(lib.sph_set_record_mode(self._ctx, int(mode)), self._ctx)
 
     def tile_stats(self) -> tuple[int, int]:
         """(density, force) chunks that fell back to the global-memory path since creation."""
