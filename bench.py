@@ -544,7 +544,7 @@ def learned_workload(args, stream, flush) -> dict:
 
 
 FP32_LANES_PER_SM = 128  # FP32 FMA lanes per SM (4 sub-partitions x 32)
-# FP32 work per unit (SURVEY d2): a candidate test (3 sub, 3 mul/FMA, the compare: ~9 flop),
+# FP32 work per unit: a candidate test (3 sub, 3 mul/FMA, the compare: ~9 flop),
 # a density interaction (~10), a force interaction (~40).
 FLOP_CAND, FLOP_DENS, FLOP_FORCE = 9, 10, 40
 
