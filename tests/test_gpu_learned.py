@@ -331,3 +331,25 @@ def test_max_density_bound(sph, trained):
             sim.set_max_density_tol(-1.0)
     assert (out["tight"].learned_macro_steps, out["tight"].fallbacks) == (0, 1)
     assert (out["loose"].learned_macro_steps, out["loose"].fallbacks) == (1, 0)
+
+
+def test_rollout_rounds_record_states_the_network_reached(sph, trained):
+    """train_mpnn's rollout round on two small runs: frames recorded after unjudged learned
+    macro-steps of the current network (plain steps first), then Adam over plain and rollout
+    frames from the current weights: the frame count, a finite loss and changed weights."""
+    import train_mpnn as TM
+
+    net, _ = trained
+    before = net.get_params()
+    plist, counts, parts = TM.training_scenes(2, 4096, seed=7)
+    net.clear_frames()
+    with sph.Sim(plist, counts=counts) as sim:
+        sim.upload(parts)
+        n_plain = net.record(sim, 2)
+    assert n_plain == 4
+    total = TM.rollout_frames(net, plist, counts, parts, per_run=3, macro=4, seed=1)
+    assert total == n_plain + 2 * 3
+    losses = TM.train_steps(net, 200, 3e-4, seed=2)
+    assert losses.shape == (200,) and np.all(np.isfinite(losses))
+    assert not np.array_equal(net.get_params(), before)
+    net.set_params(before)
