@@ -519,6 +519,23 @@ def learned_workload(args, stream, flush) -> dict:
             torch.cuda.synchronize()
             kernels[name] = {"ms_per_macro_step": e0.elapsed_time(e1) / 8}
         net.set_precision(3)
+        # BF16 tensor-core bound of the learned macro-step: its algorithmic flops from the layer
+        # shapes (fixed 32 neighbour slots, padded ones included), per particle and macro-step,
+        # over the default kernel set's CUDA-event time, against the sustained cuBLAS BF16 rate.
+        K_NB, W_H, F_E, F_N, F_O = 32, 64, 14, 9, 6
+        flop = 2 * (2 * K_NB * F_E * W_H) + 2 * ((W_H + F_N) * W_H + W_H * W_H) + 2 * (2 * W_H * W_H + W_H * F_O)
+        peaks, psrc = measured_peaks()
+        peak = float(peaks.get("bf16_tflops_sustained", peaks["bf16_tflops"]))
+        ms_macro = kernels["tcgen05_round1_lanes+mma_sync_round2 (default)"]["ms_per_macro_step"]
+        achieved = flop * n / (ms_macro * 1e-3) / 1e12
+        tensor_roofline = {
+            "bound": "tensor", "flop_per_particle_per_macro_step": flop,
+            "flop_model": "2 rounds x 32 edges x 14 x 64 edge MACs, node layers 73x64 + 64x64 (round 1), "
+                          "128x64 + 64x6 (round 2 and output); 2 flop per MAC",
+            "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+            "peak_source": f"{psrc} bf16_tflops_sustained" if "bf16_tflops_sustained" in peaks else f"{psrc} bf16_tflops",
+            "ms_per_macro_step": ms_macro,
+        }
         # What the network gains: one judged macro-step from the same state (the plain run's
         # end state) with the trained network and with a zero network (v' = v, x' = x + 4 dt v,
         # then the momentum projection adds gravity).
@@ -536,6 +553,7 @@ def learned_workload(args, stream, flush) -> dict:
         "judge_mean_density": runs["judge_mean_density"],
         "one_macro_step_vs_4_plain_steps": gain,
         "inference_kernels": kernels,
+        "tensor_roofline": tensor_roofline,
         "precision": "BF16 weights/activations, FP32 accumulate: round 1 tcgen05 MMAs (TMEM accumulators), "
                      "round 2 mma.sync m16n8k16; every kernel set is timed in inference_kernels",
         "weights": str(WEIGHTS.relative_to(REPO)),
