@@ -181,8 +181,7 @@ __device__ __forceinline__ void edge_tile(const EdgeFrags& A, int base, int n, c
             }
             __syncwarp();
             const int nsl = min(4, emax - e0);
-#pragma unroll 1
-            for (int sl = 0; sl < nsl; ++sl) {
+            auto slot = [&](int sl) {
                 const int e = e0 + sl;
                 uint32_t b0, b1;
                 ldmatrix_x2(b0, b1, lrow + sl * 8 * kFRow);
@@ -212,6 +211,16 @@ __device__ __forceinline__ void edge_tile(const EdgeFrags& A, int base, int n, c
                     s[mt][1][0] += fmaxf(c[mt][2], 0.0f);
                     s[mt][1][1] += fmaxf(c[mt][3], 0.0f);
                 }
+            };
+            if constexpr (ROUND2) {  // unrolled: later slots' P_j loads are issued early
+#pragma unroll
+                for (int sl = 0; sl < 4; ++sl) {
+                    if (sl >= nsl) break;
+                    slot(sl);
+                }
+            } else {  // round 1 spills when unrolled
+#pragma unroll 1
+                for (int sl = 0; sl < nsl; ++sl) slot(sl);
             }
             __syncwarp();
         }
