@@ -650,7 +650,8 @@ __device__ __forceinline__ void prune_nearest(unsigned short* lst, int& cnt, con
 }
 
 template <bool BATCHED, int R, int BLOCK>
-__global__ void __launch_bounds__(BLOCK) k_density_nb(const float4* __restrict__ pos_s, const int* __restrict__ start,
+// 64 registers at most (shared memory holds it to fewer CTAs per SM than that allows).
+__global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) k_density_nb(const float4* __restrict__ pos_s, const int* __restrict__ start,
                                                       SceneDev s0, const SceneDev* __restrict__ scenes, int nscene,
                                                       float2* __restrict__ rhop, int* __restrict__ nb,
                                                       int* __restrict__ nbc, int n, uint32_t* __restrict__ stats) {
@@ -690,15 +691,40 @@ __global__ void __launch_bounds__(BLOCK) k_density_nb(const float4* __restrict__
                     int a, b;
                     seg_range<R, BLOCK>(T, lrow * G::kSegPerRow + r, cx, S.dim[0], start, a, b);
                     float2 seg = make_float2(0.f, 0.f);
+                    uint32_t mx = 0, my = 0;  // the predicates, as in k_density: pair k at bit np-1-k
 #pragma unroll 2
                     for (int j = a; j < b; j += 2) {
                         const float2 d2 = pair_d2(st, j, npx, npy, npz);
                         const float2 e = __fadd2_rn(d2, ncut);
                         const float2 w = make_float2(fmaxf(-e.x, 0.0f), fmaxf(-e.y, 0.0f));
                         seg = __ffma2_rn(__fmul2_rn(w, w), w, seg);
-                        if (d2.x < cut && j != self_j) lst[BLOCK * c++] = (unsigned short)j;
-                        if (d2.y < cut && j + 1 != self_j) lst[BLOCK * c++] = (unsigned short)(j + 1);
-                        if (c > kNbCapNb - 2) prune_nearest<BLOCK>(lst, c, st, p.x, p.y, p.z);
+                        mx = __funnelshift_l(__float_as_uint(e.x), mx, 1);
+                        my = __funnelshift_l(__float_as_uint(e.y), my, 1);
+                    }
+                    // The segment's neighbours into the list, from the masks (a segment of more
+                    // than 32 pairs lost its first bits and is tested again). d2 < cut exactly
+                    // where the sign bit of d2 - cut is set.
+                    const int np = (b - a + 1) >> 1;
+                    if (np <= 32) {
+#pragma unroll
+                        for (int par = 0; par < 2; ++par) {
+                            uint32_t mk = par ? my : mx;
+                            while (mk) {
+                                const int bit = 31 - __clz(mk);
+                                mk ^= 1u << bit;
+                                const int j = a + 2 * (np - 1 - bit) + par;
+                                if (j == self_j) continue;
+                                lst[BLOCK * c++] = (unsigned short)j;
+                                if (c > kNbCapNb - 2) prune_nearest<BLOCK>(lst, c, st, p.x, p.y, p.z);
+                            }
+                        }
+                    } else {
+                        for (int j = a; j < b; j += 2) {
+                            const float2 d2 = pair_d2(st, j, npx, npy, npz);
+                            if (d2.x < cut && j != self_j) lst[BLOCK * c++] = (unsigned short)j;
+                            if (d2.y < cut && j + 1 != self_j) lst[BLOCK * c++] = (unsigned short)(j + 1);
+                            if (c > kNbCapNb - 2) prune_nearest<BLOCK>(lst, c, st, p.x, p.y, p.z);
+                        }
                     }
                     {  // Kahan, per lane, of the segment's sum
                         const float2 y = __fadd2_rn(seg, make_float2(-c2.x, -c2.y));
