@@ -471,13 +471,25 @@ __global__ void __launch_bounds__(kThr) k_tc_round(const float4* __restrict__ po
 // written in the permuted BF16 layout that the mma.sync round 2 (sph_mpnn_infer.cu) reads.
 constexpr int kLanesMma = kTP / 8;  // edge MMAs per tile (even: the barrier's phases restart)
 static_assert(kLanesMma % 2 == 0, "barrier phases must restart with every tile");
+// The node tile's first 64 columns (M1, then H1) keep the K-major core-matrix layout with a
+// K stride of 144 bytes instead of 128: a row's eight 16-byte chunks then fall on eight
+// different bank groups, and the drain, whose warp stores 32 features of one row, stores without
+// bank conflicts. Its last 16 columns (node features, bias, padding) are a separate tile.
+constexpr int kLboM = 144;                 // K stride of the M1 / H1 core matrices
+constexpr int kSboM = 8 * kLboM - 16;      // row-group stride: 8 core matrices, no trailing pad
+__host__ __device__ constexpr uint32_t m_off(int r, int k8) {
+    return (uint32_t)((r >> 3) * kSboM + k8 * kLboM + (r & 7) * 16);
+}
 struct SmemLanes {
     static constexpr int kOffAE = 0;                          // [128][32] block-diagonal We1'
     static constexpr int kOffWn = kOffAE + 128 * kKA * 2;     // Wn1' [64][80] then Wp [64][64]
     static constexpr int kOffB = kOffWn + (kImgWe2 - kImgWn1) * 2;  // edge tile [128][32]
-    static constexpr int kOffX = kOffB + 128 * kKA * 2;       // node tile [128][80]
-    static constexpr int kBytes = kOffX + kTP * kKX1 * 2;
+    static constexpr int kOffM = kOffB + 128 * kKA * 2;       // M1 / H1 tile [128][64] (m_off)
+    static constexpr int kOffXN = kOffM + (kTP / 8) * kSboM;  // node features [128][16]
+    static constexpr int kBytes = kOffXN + kTP * 16 * 2;
 };
+static_assert(m_off(kTP - 1, 7) + 16 <= SmemLanes::kOffXN - SmemLanes::kOffM, "M1 tile inside its region");
+static_assert(SmemLanes::kOffM % 16 == 0 && SmemLanes::kOffXN % 16 == 0, "16-byte aligned operand tiles");
 
 // 256 threads: warps w and w + 4 reach the same 32 TMEM lanes and split the work of a lane
 // group (the columns of the edge accumulator, the halves of a node row), so twice the warps
@@ -491,12 +503,13 @@ __global__ void __launch_bounds__(kThrL, 4) k_tc_r1_lanes(const float4* __restri
                                                        __nv_bfloat16* __restrict__ H1, uint4* __restrict__ Pperm,
                                                        uint32_t* __restrict__ err) {
     using L = SmemLanes;
-    extern __shared__ __align__(1024) uint8_t smem[];
+    extern __shared__ __align__(128) uint8_t smem[];  // no-swizzle operands: 16-byte alignment
     __shared__ __align__(8) uint64_t mbar[2];
     __shared__ uint32_t tmem_slot;
     __shared__ int bad;
     uint8_t* const sB = smem + L::kOffB;
-    uint8_t* const sX = smem + L::kOffX;
+    uint8_t* const sM = smem + L::kOffM;
+    uint8_t* const sXN = smem + L::kOffXN;
     const int tid = threadIdx.x, warp = tid >> 5;
     {
         const uint4* a = reinterpret_cast<const uint4*>(img + kImgAE1);
@@ -520,7 +533,7 @@ __global__ void __launch_bounds__(kThrL, 4) k_tc_r1_lanes(const float4* __restri
     const uint32_t tmem = tmem_slot;
     const uint32_t s_ae = smem_u32(smem + L::kOffAE), s_wn = smem_u32(smem + L::kOffWn);
     const uint32_t s_wp = s_wn + (uint32_t)((kImgWp - kImgWn1) * 2);
-    const uint32_t sb = smem_u32(sB), sx = smem_u32(sX);
+    const uint32_t sb = smem_u32(sB), sm = smem_u32(sM), sxn = smem_u32(sXN);
     const uint32_t id_e = tc::idesc_bf16_f32(128, 128), id_n = tc::idesc_bf16_f32(128, W);
     const float ih = 1.0f / fc.h, ic = 1.0f / fc.c;
     const int ntiles = (n + kTP - 1) / kTP;
@@ -552,7 +565,7 @@ __global__ void __launch_bounds__(kThrL, 4) k_tc_r1_lanes(const float4* __restri
             }
 #pragma unroll
             for (int c = 0; c < 2; ++c)
-                *reinterpret_cast<uint4*>(sX + tile_off(lane_t, 8 + c, kKX1)) =
+                *reinterpret_cast<uint4*>(sXN + tile_off(lane_t, c, 16)) =
                     make_uint4(pk_bf16(v[8 * c], v[8 * c + 1]), pk_bf16(v[8 * c + 2], v[8 * c + 3]),
                                pk_bf16(v[8 * c + 4], v[8 * c + 5]), pk_bf16(v[8 * c + 6], v[8 * c + 7]));
         }
@@ -601,7 +614,7 @@ __global__ void __launch_bounds__(kThrL, 4) k_tc_r1_lanes(const float4* __restri
                     for (int u = 0; u < w; ++u) h[u] = hadd2(h[u], h[u + w]);
                 const float2 s2 = __half22float2(*reinterpret_cast<__half2*>(&h[0]));
                 const int row = 8 * i + 4 * half + pq;
-                *reinterpret_cast<__nv_bfloat16*>(sX + tile_off(row, f >> 3, kKX1) + (f & 7) * 2) =
+                *reinterpret_cast<__nv_bfloat16*>(sM + m_off(row, f >> 3) + (f & 7) * 2) =
                     __float2bfloat16_rn((s2.x + s2.y) * (1.0f / K));
             }
             tc::fence_before_sync();  // the next MMA overwrites the accumulator
@@ -613,9 +626,12 @@ __global__ void __launch_bounds__(kThrL, 4) k_tc_r1_lanes(const float4* __restri
         if (__syncthreads_or(bad)) break;
         if (tid == 0) {
             tc::fence_after_sync();
-            for (int k = 0; k < kKX1 / 16; ++k)
-                tc::mma_bf16(tmem, smem_desc(sx + 256u * k, 128u, sbo(kKX1)), smem_desc(s_wn + 256u * k, 128u, sbo(kKX1)),
-                             id_n, k > 0 ? 1u : 0u);
+            for (int k = 0; k < W / 16; ++k)  // K 0 .. 63: M1
+                tc::mma_bf16(tmem, smem_desc(sm + 2u * kLboM * k, (uint32_t)kLboM, (uint32_t)kSboM),
+                             smem_desc(s_wn + 256u * k, 128u, sbo(kKX1)), id_n, k > 0 ? 1u : 0u);
+            // K 64 .. 79: node features, bias, padding
+            tc::mma_bf16(tmem, smem_desc(sxn, 128u, sbo(16)), smem_desc(s_wn + 256u * (W / 16), 128u, sbo(kKX1)),
+                         id_n, 1u);
             tc::mma_commit(&mbar[1]);
         }
         if (!tc::mbar_wait(&mbar[1], 0)) bad = 1;
@@ -636,7 +652,7 @@ __global__ void __launch_bounds__(kThrL, 4) k_tc_r1_lanes(const float4* __restri
             for (int c = 0; c < 4; ++c) {
                 const uint4 w = make_uint4(pk_bf16(hv[8 * c], hv[8 * c + 1]), pk_bf16(hv[8 * c + 2], hv[8 * c + 3]),
                                            pk_bf16(hv[8 * c + 4], hv[8 * c + 5]), pk_bf16(hv[8 * c + 6], hv[8 * c + 7]));
-                *reinterpret_cast<uint4*>(sX + tile_off(lane_t, 4 * grp + c, kKH1)) = w;
+                *reinterpret_cast<uint4*>(sM + m_off(lane_t, 4 * grp + c)) = w;
                 if (p < n) reinterpret_cast<uint4*>(H1 + (size_t)p * W)[4 * grp + c] = w;
             }
         }
@@ -646,7 +662,7 @@ __global__ void __launch_bounds__(kThrL, 4) k_tc_r1_lanes(const float4* __restri
         if (tid == 0) {
             tc::fence_after_sync();
             for (int k = 0; k < kKH1 / 16; ++k)
-                tc::mma_bf16(tmem + (uint32_t)W, smem_desc(sx + 256u * k, 128u, sbo(kKH1)),
+                tc::mma_bf16(tmem + (uint32_t)W, smem_desc(sm + 2u * kLboM * k, (uint32_t)kLboM, (uint32_t)kSboM),
                              smem_desc(s_wp + 256u * k, 128u, sbo(kKH1)), id_n, k > 0 ? 1u : 0u);
             tc::mma_commit(&mbar[1]);
         }
