@@ -89,17 +89,23 @@ inline int nblk(long long n, int t = kT) { return (int)((n + t - 1) / t); }
 
 static_assert(M::K == kNbList, "the network reads the neighbour lists of launch_density_nb");
 
-constexpr int kSumBlocks = 256;
+constexpr int kSumBlocks = 1024;
 
-// Momentum projection, step 1: FP64 partial sums of the outputs (fixed order: deterministic).
+// Momentum projection, step 1: partial sums of the outputs, per thread in FP32 over its few rows
+// (two 16-byte loads per 32-byte row), per block in FP64 (fixed order: deterministic).
 __global__ void __launch_bounds__(kT) k_out_partial(const float* __restrict__ O, int n, double* __restrict__ part) {
+    static_assert(M::kOS == 8 && M::FO <= 8, "an output row is two float4");
     __shared__ double sh[M::FO][kT];
-    double a[M::FO] = {};
-    for (int i = blockIdx.x * kT + threadIdx.x; i < n; i += gridDim.x * kT)
+    float a[M::FO] = {};
+    for (int i = blockIdx.x * kT + threadIdx.x; i < n; i += gridDim.x * kT) {
+        const float4* row = reinterpret_cast<const float4*>(O + (size_t)i * M::kOS);
+        const float4 r0 = __ldg(row), r1 = __ldg(row + 1);
+        const float v[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
 #pragma unroll
-        for (int q = 0; q < M::FO; ++q) a[q] += (double)O[(size_t)i * M::kOS + q];
+        for (int q = 0; q < M::FO; ++q) a[q] += v[q];
+    }
 #pragma unroll
-    for (int q = 0; q < M::FO; ++q) sh[q][threadIdx.x] = a[q];
+    for (int q = 0; q < M::FO; ++q) sh[q][threadIdx.x] = (double)a[q];
     __syncthreads();
     for (int o = kT / 2; o > 0; o >>= 1) {
         if (threadIdx.x < o)
@@ -112,14 +118,29 @@ __global__ void __launch_bounds__(kT) k_out_partial(const float* __restrict__ O,
 
 // Step 2: the shift that makes the mean of each head G/A. Pressure and viscosity forces are
 // pairwise antisymmetric (force_comp.glsl:59-60 with m_i = m_j), so over all particles the
-// sum of m a over the 4 sub-steps is N m G exactly: both target heads average G/A.
-__global__ void k_out_corr(const double* __restrict__ part, int blocks, int n, SceneDev S, float* __restrict__ corr) {
-    const int q = threadIdx.x;
-    if (q >= M::FO) return;
-    double s = 0.0;
-    for (int b = 0; b < blocks; ++b) s += part[b * M::FO + q];
-    const double ga = (double)S.g[q % 3] * (double)S.h / (double)S.gas_k;
-    corr[q] = (float)(ga - s / (double)n);
+// sum of m a over the 4 sub-steps is N m G exactly: both target heads average G/A. One block
+// sums the partials in a fixed-order FP64 tree.
+__global__ void __launch_bounds__(kT) k_out_corr(const double* __restrict__ part, int blocks, int n, SceneDev S,
+                                                 float* __restrict__ corr) {
+    __shared__ double sh[M::FO][kT];
+    double a[M::FO] = {};
+    for (int b = threadIdx.x; b < blocks; b += kT)
+#pragma unroll
+        for (int q = 0; q < M::FO; ++q) a[q] += part[b * M::FO + q];
+#pragma unroll
+    for (int q = 0; q < M::FO; ++q) sh[q][threadIdx.x] = a[q];
+    __syncthreads();
+    for (int o = kT / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o)
+#pragma unroll
+            for (int q = 0; q < M::FO; ++q) sh[q][threadIdx.x] += sh[q][threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x < M::FO) {
+        const int q = threadIdx.x;
+        const double ga = (double)S.g[q % 3] * (double)S.h / (double)S.gas_k;
+        corr[q] = (float)(ga - sh[q][0] / (double)n);
+    }
 }
 
 // Macro-step update from the network outputs O plus the projection corr, fused with the hash.
@@ -384,7 +405,7 @@ sph_status learned_macro(sph_ctx* ctx, sph_mpnn* net) {
     }
     // momentum projection, then the update
     k_out_partial<<<kSumBlocks, kT, 0, ctx->stream>>>(O, n, net->osum);
-    k_out_corr<<<1, 32, 0, ctx->stream>>>(net->osum, kSumBlocks, n, ctx->s0, net->ocorr);
+    k_out_corr<<<1, kT, 0, ctx->stream>>>(net->osum, kSumBlocks, n, ctx->s0, net->ocorr);
     k_macro_integrate<<<nblk(n), kT, 0, ctx->stream>>>(ctx->b.pos_s, ctx->b.vel_s, O, net->ocorr, ctx->s0, ctx->b.pos,
                                                        ctx->b.vel, ctx->b.key, ctx->b.rank, ctx->b.count, n);
     ctx->need_hash = false;  // the integrate hashed the new positions
