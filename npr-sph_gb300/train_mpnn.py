@@ -89,13 +89,17 @@ def main() -> None:
     ap.add_argument("--rollout-schedule", default="8:7:60000,16:8:60000,16:8:60000,24:24:120000",
                     help="rollout rounds frames:macro:steps, comma-separated ('' for none)")
     ap.add_argument("--rollout-lr", type=float, default=3e-4)
+    ap.add_argument("--rollout-plain-max", type=int, default=192,
+                    help="a rollout starts after 8 .. this many plain steps (a multiple of 8)")
+    ap.add_argument("--init", type=Path, default=None,
+                    help="start from these parameters (with --steps 0: rollout rounds only)")
     ap.add_argument("--out", type=Path, default=DEFAULT_OUT)
     args = ap.parse_args()
 
     t0 = time.time()
     plist, counts, parts = training_scenes(args.scenes, args.particles, args.seed)
     net = S.Net(args.particles)
-    net.set_params(init_params(args.seed))
+    net.set_params(np.load(args.init).astype(np.float32) if args.init else init_params(args.seed))
     net.set_train_precision(args.precision)
     with S.Sim(plist, counts=counts) as sim:
         sim.upload(parts)
@@ -106,9 +110,8 @@ def main() -> None:
         sim.synchronize()
     t_rec = time.time() - t0
     t1 = time.time()
-    losses = [train_steps(net, args.steps, args.lr, args.seed * 1000003)]
+    loss = train_steps(net, args.steps, args.lr, args.seed * 1000003) if args.steps > 0 else np.zeros(0)
     t_train = time.time() - t1
-    loss = np.concatenate(losses)
     rounds = []
     for r, spec in enumerate(x for x in args.rollout_schedule.split(",") if x):
         frames, macro, steps = (int(v) for v in spec.split(":"))
@@ -121,7 +124,8 @@ def main() -> None:
                 if f + 1 < args.frames:
                     sim.step(args.gap)
             sim.synchronize()
-        n_roll = rollout_frames(net, plist, counts, parts, frames, macro, args.seed + 99 + r)
+        n_roll = rollout_frames(net, plist, counts, parts, frames, macro, args.seed + 99 + r,
+                                plain_max=args.rollout_plain_max)
         t3 = time.time()
         rl = train_steps(net, steps, args.rollout_lr, args.seed * 1000003 + 77 + 1000 * r)
         rounds.append({"rollout_frames_per_run": frames, "max_macro_steps": macro, "adam_steps": steps,
@@ -136,8 +140,10 @@ def main() -> None:
     meta = {"scenes": args.scenes, "particles": args.particles, "frames_per_run": args.frames, "gap": args.gap,
             "frames": int(total), "adam_steps": args.steps, "lr": args.lr, "seed": args.seed,
             "train_precision": "bf16 tcgen05 GEMMs" if args.precision == 1 else "fp32",
-            "loss_first_500": float(loss[:500].mean()), "loss_last_500": float(loss[-500:].mean()),
-            "record_s": t_rec, "train_s": t_train, "rollout_lr": args.rollout_lr, "rollout_rounds": rounds}
+            "loss_first_500": float(loss[:500].mean()) if len(loss) else None,
+            "loss_last_500": float(loss[-500:].mean()) if len(loss) else None,
+            "record_s": t_rec, "train_s": t_train, "init": str(args.init) if args.init else None,
+            "rollout_lr": args.rollout_lr, "rollout_plain_max": args.rollout_plain_max, "rollout_rounds": rounds}
     args.out.with_suffix(".json").write_text(json.dumps(meta, indent=1))
     print(json.dumps(meta))
 
@@ -153,10 +159,10 @@ def train_steps(net, steps: int, lr0: float, seed: int) -> np.ndarray:
     return np.concatenate(losses)
 
 
-def rollout_frames(net, plist, counts, parts, per_run: int, macro: int, seed: int) -> int:
+def rollout_frames(net, plist, counts, parts, per_run: int, macro: int, seed: int, plain_max: int = 192) -> int:
     """Record per_run frames of every run at states the network reached itself: from the run's
-    initial state, 8-192 plain steps, then 1-macro unjudged learned macro-steps. Returns the
-    frames recorded in total."""
+    initial state, 8-plain_max plain steps (multiples of 8), then 1-macro unjudged learned
+    macro-steps. Returns the frames recorded in total."""
     rng = np.random.default_rng(seed)
     offs = [0] + [int(x) for x in np.cumsum(counts)]
     total = 0
@@ -164,7 +170,7 @@ def rollout_frames(net, plist, counts, parts, per_run: int, macro: int, seed: in
         with S.Sim(p, n_max=int(counts[i])) as sim:
             for _ in range(per_run):
                 sim.upload(parts[offs[i]:offs[i + 1]])
-                sim.step(int(8 * rng.integers(1, 25)))
+                sim.step(int(8 * rng.integers(1, plain_max // 8 + 1)))
                 sim.learned_step(net, int(rng.integers(1, macro + 1)), 0, 1e30, 1e30)
                 total = net.record(sim, 1)
             sim.synchronize()
